@@ -1,0 +1,153 @@
+/*
+ * vnm_gb300 -- GB300-native V:N:M graph reordering and SpMM, C ABI.
+ *
+ * This header is the drop-in boundary of libvnm_gb300.so.  The reference
+ * (PictureResearch/vnm-graph-reordering) ships no library API: its path is the
+ * `spmm` command built from main.cu over header templates.  Each entry point
+ * below names the reference function it replaces (file:line).  The `spmm`
+ * drop-in command of this project is a thin C++ program over these calls.
+ *
+ * Conventions
+ *   - Plain C types only.  Every call returns a vnm_status (0 = success); no
+ *     call exits the process or throws across the ABI.
+ *   - Matrices are COO, 0-based, int32 indices, float32 values, square with
+ *     `nrows` already padded to a multiple of M (as Mtx::init_from_file does),
+ *     sorted by (row, col) with no repeated (row, col) -- the state a matrix
+ *     is in after the reference's reader (mtx/readMtx.hpp:354-425).
+ *   - `mem` says where the caller's arrays live: VNM_MEM_HOST (pageable or
+ *     pinned host memory; the call copies them) or VNM_MEM_DEVICE (device
+ *     memory of the context's GPU; nothing is copied).
+ *   - A context owns one CUDA stream and its scratch memory; use one context
+ *     per host thread.  Calls are synchronous with respect to the host unless
+ *     stated otherwise.
+ */
+#ifndef VNM_GB300_H
+#define VNM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int vnm_status;
+#define VNM_OK 0
+#define VNM_ERR_ARG 1          /* invalid argument (sizes, N/M/V, schedule) */
+#define VNM_ERR_CUDA 2         /* a CUDA runtime call failed */
+#define VNM_ERR_UNSORTED 3     /* COO not sorted by (row, col) or has repeats */
+#define VNM_ERR_RANGE 4        /* an index outside [0, nrows) */
+#define VNM_ERR_NOMEM 5        /* device allocation failed */
+#define VNM_ERR_INTERNAL 6     /* a kernel reported a broken invariant */
+#define VNM_ERR_IO 7           /* file could not be read or written */
+#define VNM_ERR_FORMAT 8       /* Matrix Market banner/size/type not supported */
+#define VNM_ERR_NO_DEVICE 9    /* no usable CUDA device */
+#define VNM_ERR_LIMIT 10       /* a size above a documented maximum */
+
+#define VNM_MEM_HOST 0
+#define VNM_MEM_DEVICE 1
+
+typedef struct vnm_ctx vnm_ctx;
+
+/* Human-readable text of a status code (static storage). */
+const char* vnm_status_string(vnm_status s);
+
+/* Library version string, e.g. "0.1.0 sm_103a". */
+const char* vnm_version(void);
+
+/* Create a context on CUDA device `device` with its own non-blocking stream. */
+vnm_status vnm_create(vnm_ctx** ctx, int device);
+vnm_status vnm_destroy(vnm_ctx* ctx);
+
+/* Milliseconds of device time spent in the kernels of the last call
+ * (CUDA events on the context's stream, first launch to last). */
+float vnm_last_kernel_ms(const vnm_ctx* ctx);
+/* Number of kernels the last call launched. */
+int vnm_last_launch_count(const vnm_ctx* ctx);
+
+/* Milliseconds of the last call's main kernel alone (the persistent reorder
+ * kernel for the NM calls), CUDA events on the context's stream. */
+float vnm_last_main_kernel_ms(const vnm_ctx* ctx);
+
+/* Work counters of the last NM call (for roofline accounting):
+ * out[0] rounds summed over jobs, out[1] column entries gathered,
+ * out[2] row records touched, out[3] segments per job, out[4] jobs,
+ * out[5] nonzero-valued entries of the pattern.  n <= 8 values. */
+vnm_status vnm_last_stats(const vnm_ctx* ctx, long long* out, int n);
+
+/* ---------------------------------------------------------------------------
+ * NM reorder
+ * ------------------------------------------------------------------------- */
+
+/* One reorder job: reorderUtil<float>(mat, nm_maxiter) followed by
+ * run_onepair (sched 0), run_onepair_double (1), run_onepair_reverse (2) or
+ * run_onepair_reverse_double (3).  Replaces reorder/reorder.h:1805-2474
+ * together with LocateinvalidSegment, GetSegSwapScore, LocateAllZeroSegment,
+ * Reorder and Mtx::reset (reorder/reorder.h:23-317, :392-418,
+ * mtx/Mtx.h:437-478).
+ *
+ * Entries whose value is 0.0f are not part of the N:M bitmap, as in
+ * reorder/reorder.h:93.  Requires 1 <= N < M <= 8.
+ *
+ * Outputs (host memory, caller-owned):
+ *   res5[5]   = {init_size, final_size, init_cnt, final_cnt, rounds}, the
+ *               vector run_onepair* returns (reorder/reorder.h:1966)
+ *   newpos    = optional (NULL to skip), length nrows: final position of each
+ *               node.  Apply it to a COO with vnm_permute_coo().
+ */
+vnm_status vnm_nm_reorder(vnm_ctx* ctx, int nrows, int nnz, const int* row, const int* col, const float* val,
+                          int mem, int N, int M, int sched, int nm_maxiter, int* res5, int* newpos);
+
+/* All four schedules of one matrix in a single persistent launch, one
+ * thread block per schedule; then the choice of find_best_2toX
+ * (main.cu:72-114): the largest improve rate (init_cnt-final_cnt)/init_cnt,
+ * ties to the lowest schedule id (the reference breaks ties by wall time).
+ * Returns 0 as the best schedule when nnz == 0 or init_size == 0 (main.cu:85).
+ *   res5x4[20]  = res5 of schedules 0..3
+ *   newpos_best = optional, length nrows, the best schedule's permutation
+ */
+vnm_status vnm_nm_search(vnm_ctx* ctx, int nrows, int nnz, const int* row, const int* col, const float* val,
+                         int mem, int N, int M, int nm_maxiter, int* best_sched, int* res5x4, int* newpos_best);
+
+/* Many independent matrices, each with one schedule, reordered in one
+ * persistent launch (one thread block per matrix).  Matrix b occupies
+ * row/col/val[nnz_offset[b] .. nnz_offset[b+1]) and has nrows[b] rows;
+ * newpos (optional) is laid out at row_offset[b] = sum of nrows[0..b).
+ * All arrays are host arrays.  res5 is [nmat][5]. */
+vnm_status vnm_nm_reorder_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int64_t* nnz_offset,
+                                const int* row, const int* col, const float* val, int N, int M, int sched,
+                                int nm_maxiter, int* res5, int* newpos);
+
+/* Record of the swaps committed by one job (parity diagnostics): after a
+ * vnm_nm_reorder call with tracing on, `pairs` receives up to `cap` (v1, v2)
+ * position pairs in commit order and round_end[r] the number of pairs
+ * committed by the end of round r.  Tracing is off unless enabled. */
+vnm_status vnm_nm_set_trace(vnm_ctx* ctx, int enable);
+vnm_status vnm_nm_get_trace(vnm_ctx* ctx, int* pairs, int cap_pairs, int* npairs, int* round_end, int cap_rounds,
+                            int* nrounds);
+
+/* Apply a node permutation to a COO in place: row = newpos[row],
+ * col = newpos[col] -- the Reorder kernel of reorder/reorder.h:23-35 with all
+ * rounds composed.  The order of the entries does not change. */
+vnm_status vnm_permute_coo(vnm_ctx* ctx, int nrows, int nnz, int* row, int* col, int mem, const int* newpos);
+
+/* Per-segment counts of the current matrix: invalid[s] = rows whose M-group
+ * in segment s has more than N nonzeros (LocateinvalidSegment,
+ * reorder/reorder.h:262-289); allzero[s] = rows whose group is empty
+ * (LocateAllZeroSegment, :291-317).  Host outputs of length nrows/M. */
+vnm_status vnm_nm_segment_counts(vnm_ctx* ctx, int nrows, int nnz, const int* row, const int* col,
+                                 const float* val, int mem, int N, int M, int* invalid, int* allzero);
+
+/* Swap gains of one segment pair (GetSegSwapScore, reorder/reorder.h:74-131):
+ * score[(i*M+j)*2+0] = left gain, score[(i*M+j)*2+1] = right gain. */
+vnm_status vnm_nm_pair_score(vnm_ctx* ctx, int nrows, int nnz, const int* row, const int* col, const float* val,
+                             int mem, int N, int M, int seg1, int seg2, int* score);
+
+/* Host helper: the pop order of the SwapPair priority queue of
+ * reorder/reorder.h:521-532 (Comparator, reorder/swappair.h:112-120) for n
+ * pairs pushed in index order -- the exact emulation the kernels use. */
+vnm_status vnm_swap_heap_order(int n, const int* lg, const int* rg, int* order);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VNM_GB300_H */

@@ -1,0 +1,1091 @@
+// CPU oracle for the V:N:M graph-reordering path -- TEST INFRASTRUCTURE ONLY.
+// Only tests/, the smoke check and the benchmark's CPU-baseline leg call this
+// library, and only as the checker or the timed CPU port of the reference.
+//
+// A plain C++17 restatement of PictureResearch/vnm-graph-reordering; every
+// function names the reference lines it follows.  Where the reference has
+// undefined behaviour, the choice made here is stated in a comment.
+#include "vnm_oracle.h"
+
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <functional>
+#include <queue>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+int g_threads = 1;
+
+// ---------------------------------------------------------------------------
+// Matrix Market input (mtx/mmio.hpp:128-228, mtx/readMtx.hpp:84-219, :354-425)
+// ---------------------------------------------------------------------------
+struct Coo {
+  int nrows = 0, ncols = 0;
+  std::vector<int> row, col;
+  std::vector<float> val;
+  int nnz() const { return (int)row.size(); }
+};
+
+// customSort (mtx/readMtx.hpp:56-82): std::sort of (row, col, val, idx)
+// tuples compared on (row, col) only.  Same library, same comparator, same
+// input order => the same permutation as the reference, ties included.
+bool tuple_less(const std::tuple<int, int, float, int>& a,
+                const std::tuple<int, int, float, int>& b) {
+  int ra = std::get<0>(a), rb = std::get<0>(b);
+  int ca = std::get<1>(a), cb = std::get<1>(b);
+  if (ra == rb) return ca < cb;
+  return ra < rb;
+}
+
+void custom_sort(std::vector<int>& r, std::vector<int>& c, std::vector<float>& v) {
+  int n = (int)r.size();
+  std::vector<std::tuple<int, int, float, int>> t;
+  t.reserve(n);
+  for (int i = 0; i < n; ++i) t.emplace_back(r[i], c[i], v[i], i);
+  std::sort(t.begin(), t.end(), tuple_less);
+  std::vector<int> r0 = r, c0 = c;
+  std::vector<float> v0 = v;
+  for (int i = 0; i < n; ++i) {
+    int k = std::get<3>(t[i]);
+    r[i] = r0[k];
+    c[i] = c0[k];
+    v[i] = v0[k];
+  }
+}
+
+// removeSelfloop (mtx/readMtx.hpp:152-219) with remove_self_loops = false.
+// Mirror (symmetric banner), sort, then drop repeated (row, col) entries.  The
+// reference compacts rows/cols but NOT values (:201-213), then truncates all
+// three; we reproduce that value misalignment.  (When the last sorted entry
+// is a repeat, the reference also reads one element past the end; we follow
+// the outcome it has whenever that stray word is not -1.)
+void remove_duplicates(std::vector<int>& r, std::vector<int>& c,
+                       std::vector<float>& v, bool undirected, int header_nvals) {
+  if (undirected) {
+    int n0 = std::min(header_nvals, (int)r.size());
+    for (int i = 0; i < n0; ++i) {
+      if (c[i] != r[i]) {
+        int rr = r[i], cc = c[i];
+        float vv = v[i];
+        r.push_back(cc);
+        c.push_back(rr);
+        v.push_back(vv);
+      }
+    }
+  }
+  custom_sort(r, c, v);
+  int n = (int)r.size();
+  if (n == 0) return;
+  std::vector<char> dead(n, 0);
+  for (int i = 1; i < n; ++i)
+    if (r[i] == r[i - 1] && c[i] == c[i - 1]) dead[i] = 1;
+  int k = 0;
+  for (int i = 0; i < n; ++i) {
+    if (dead[i]) continue;
+    r[k] = r[i];
+    c[k] = c[i];
+    ++k;
+  }
+  r.resize(k);
+  c.resize(k);
+  v.resize(k);  // first k sorted values, as in the reference
+}
+
+void lower(char* p) {
+  for (; *p; ++p) *p = (char)tolower((unsigned char)*p);
+}
+
+// mm_read_banner + mm_read_mtx_crd_size + readTuples + removeSelfloop +
+// customSort + Mtx::init_from_file padding.
+int read_mtx_file(const char* path, int aligned, Coo& out) {
+  FILE* f = fopen(path, "r");
+  if (!f) return ORC_ERR_IO;
+  char line[1025], banner[64], mtx[64], crd[64], dtype[64], storage[64];
+  if (!fgets(line, sizeof line, f) ||
+      sscanf(line, "%63s %63s %63s %63s %63s", banner, mtx, crd, dtype, storage) != 5) {
+    fclose(f);
+    return ORC_ERR_FORMAT;
+  }
+  lower(mtx);
+  lower(crd);
+  lower(dtype);
+  lower(storage);
+  if (strncmp(banner, "%%MatrixMarket", 14) != 0 || strcmp(mtx, "matrix") != 0 ||
+      strcmp(crd, "coordinate") != 0) {
+    fclose(f);
+    return ORC_ERR_FORMAT;
+  }
+  int kind;  // 0 real, 1 integer, 2 pattern
+  if (!strcmp(dtype, "real")) kind = 0;
+  else if (!strcmp(dtype, "integer")) kind = 1;
+  else if (!strcmp(dtype, "pattern")) kind = 2;
+  else {  // complex: the reference reads no tuples and then indexes an empty vector
+    fclose(f);
+    return ORC_ERR_FORMAT;
+  }
+  bool symmetric;
+  if (!strcmp(storage, "general")) symmetric = false;
+  else if (!strcmp(storage, "symmetric")) symmetric = true;
+  else if (!strcmp(storage, "hermitian") || !strcmp(storage, "skew-symmetric")) symmetric = false;
+  else {
+    fclose(f);
+    return ORC_ERR_FORMAT;
+  }
+  int nr = 0, nc = 0, nz = 0;
+  do {
+    if (!fgets(line, sizeof line, f)) {
+      fclose(f);
+      return ORC_ERR_FORMAT;
+    }
+  } while (line[0] == '%');
+  if (sscanf(line, "%d %d %d", &nr, &nc, &nz) != 3) {
+    int got;
+    do {
+      got = fscanf(f, "%d %d %d", &nr, &nc, &nz);
+      if (got == EOF) {
+        fclose(f);
+        return ORC_ERR_FORMAT;
+      }
+    } while (got != 3);
+  }
+  if (nr < 0 || nc < 0 || nz < 0) {
+    fclose(f);
+    return ORC_ERR_FORMAT;
+  }
+  Coo a;
+  a.row.reserve(nz);
+  a.col.reserve(nz);
+  a.val.reserve(nz);
+  for (int i = 0; i < nz; ++i) {
+    int r, c;
+    if (fscanf(f, "%d", &r) == EOF) break;  // "Not enough rows" (readMtx.hpp:105)
+    if (fscanf(f, "%d", &c) != 1) break;
+    float v = 1.0f;
+    if (kind == 0) {
+      float x = 0.f;
+      if (fscanf(f, "%f", &x) == 1) v = x;
+    } else if (kind == 1) {
+      int x = 0;
+      if (fscanf(f, "%d", &x) == 1) v = (float)x;
+    }
+    a.row.push_back(r - 1);
+    a.col.push_back(c - 1);
+    a.val.push_back(v);
+  }
+  fclose(f);
+  for (size_t i = 0; i < a.row.size(); ++i) {
+    // the reference indexes host arrays with these ids without checks; we refuse
+    if (a.row[i] < 0 || a.col[i] < 0 || a.row[i] >= nr || a.col[i] >= nc) return ORC_ERR_FORMAT;
+  }
+  remove_duplicates(a.row, a.col, a.val, symmetric, nz);
+  custom_sort(a.row, a.col, a.val);
+  a.nrows = nr;
+  a.ncols = nc;
+  if (aligned > 0 && a.nrows % aligned != 0) {  // Mtx.h:106-109
+    a.nrows = (a.nrows + aligned - 1) / aligned * aligned;
+    a.ncols = (a.ncols + aligned - 1) / aligned * aligned;
+  }
+  out = std::move(a);
+  return ORC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// NM reorder (reorder/reorder.h, reorder/swappair.h)
+// ---------------------------------------------------------------------------
+class SwapPair {  // reorder/swappair.h:5-20
+ public:
+  SwapPair(int a, int b, int lg, int rg) : v1(a), v2(b), left_gain(lg), right_gain(rg) {}
+  int v1, v2, left_gain, right_gain;
+};
+
+// reorder/swappair.h:112-120 (non-strict on full ties, kept as is)
+bool Comparator(SwapPair* p1, SwapPair* p2) {
+  if (p1->left_gain + p1->right_gain == p2->left_gain + p2->right_gain)
+    return p1->right_gain <= p2->right_gain;
+  return p1->left_gain + p1->right_gain < p2->left_gain + p2->right_gain;
+}
+// reorder/reorder.h:422-434
+bool cmp(std::pair<int, int>& a, std::pair<int, int>& b) {
+  if (a.second == b.second) return a.first > b.first;
+  return a.second < b.second;
+}
+bool cmp_reverse(std::pair<int, int>& a, std::pair<int, int>& b) {
+  if (a.second == b.second) return a.first < b.first;
+  return a.second > b.second;
+}
+
+typedef std::priority_queue<std::pair<int, int>, std::vector<std::pair<int, int>>,
+                            std::function<bool(std::pair<int, int>&, std::pair<int, int>&)>>
+    InvalSegList;
+typedef std::priority_queue<SwapPair*, std::vector<SwapPair*>, std::function<bool(SwapPair*, SwapPair*)>>
+    SwapPairList;
+
+// Bitmap view of the current matrix, rebuilt after every round the way
+// Mtx::reset rebuilds CSR/BSR (mtx/Mtx.h:437-478).  Bit k of a group holds
+// column offset k (the reference stores offset k at bit M-1-k; popcounts and
+// gains are identical).
+struct Groups {
+  int R = 0, M = 0, nseg = 0;
+  // segment-major list of the nonzero groups: rows ascending within a segment
+  std::vector<int> seg_ptr, seg_row;
+  std::vector<uint8_t> seg_bits;
+};
+
+void build_groups(int R, int M, int nnz, const int* row, const int* col, const float* val,
+                  Groups& g) {
+  g.R = R;
+  g.M = M;
+  g.nseg = (R + M - 1) / M;
+  // CSR of the nonzero-valued entries (counting sort by row)
+  std::vector<int> rp(R + 1, 0);
+  for (int i = 0; i < nnz; ++i)
+    if (val[i] != 0.0f) rp[row[i] + 1]++;
+  for (int r = 0; r < R; ++r) rp[r + 1] += rp[r];
+  std::vector<int> ci(rp[R]);
+  {
+    std::vector<int> fill(rp.begin(), rp.end() - 1);
+    for (int i = 0; i < nnz; ++i)
+      if (val[i] != 0.0f) ci[fill[row[i]]++] = col[i];
+  }
+  // per row: columns ascending, so a row's groups come out ordered by segment
+#pragma omp parallel for schedule(dynamic, 256) num_threads(g_threads)
+  for (int r = 0; r < R; ++r) std::sort(ci.begin() + rp[r], ci.begin() + rp[r + 1]);
+  // counting sort of groups by segment, rows ascending
+  g.seg_ptr.assign(g.nseg + 1, 0);
+  for (int r = 0; r < R; ++r) {
+    int last = -1;
+    for (int k = rp[r]; k < rp[r + 1]; ++k) {
+      int s = ci[k] / M;
+      if (s != last) {
+        if (s < g.nseg) g.seg_ptr[s + 1]++;
+        last = s;
+      }
+    }
+  }
+  for (int s = 0; s < g.nseg; ++s) g.seg_ptr[s + 1] += g.seg_ptr[s];
+  g.seg_row.assign(g.seg_ptr[g.nseg], 0);
+  g.seg_bits.assign(g.seg_ptr[g.nseg], 0);
+  std::vector<int> fill(g.seg_ptr.begin(), g.seg_ptr.end() - 1);
+  for (int r = 0; r < R; ++r) {
+    int last = -1, slot = -1;
+    for (int k = rp[r]; k < rp[r + 1]; ++k) {
+      int s = ci[k] / M;
+      if (s >= g.nseg) continue;  // columns past the padded row count: not scanned
+      if (s != last) {
+        slot = fill[s]++;
+        g.seg_row[slot] = r;
+        g.seg_bits[slot] = 0;
+        last = s;
+      }
+      g.seg_bits[slot] |= (uint8_t)(1u << (ci[k] % M));
+    }
+  }
+}
+
+// LocateinvalidSegment / LocateAllZeroSegment (reorder/reorder.h:262-317)
+void segment_counts(const Groups& g, int N, std::vector<int>& invalid, std::vector<int>& allzero) {
+  invalid.assign(g.nseg, 0);
+  allzero.assign(g.nseg, 0);
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (int s = 0; s < g.nseg; ++s) {
+    int inv = 0;
+    for (int k = g.seg_ptr[s]; k < g.seg_ptr[s + 1]; ++k)
+      if (__builtin_popcount(g.seg_bits[k]) > N) ++inv;
+    invalid[s] = inv;
+    allzero[s] = g.R - (g.seg_ptr[s + 1] - g.seg_ptr[s]);
+  }
+}
+
+// GetSegSwapScore (reorder/reorder.h:74-131): sum over rows of the change of
+// the invalid indicator on each side for every single-bit exchange (i, j).
+// Rows where both groups are empty contribute nothing, so only the union of
+// the two row lists is visited.
+void pair_score(const Groups& g, int N, int s1, int s2, std::vector<int>& score) {
+  const int M = g.M;
+  score.assign(2 * M * M, 0);
+  int a = g.seg_ptr[s1], ae = g.seg_ptr[s1 + 1];
+  int b = g.seg_ptr[s2], be = g.seg_ptr[s2 + 1];
+  auto add_row = [&](unsigned L, unsigned Rb) {
+    int pl = __builtin_popcount(L) > N, pr = __builtin_popcount(Rb) > N;
+    for (int i = 0; i < M; ++i) {
+      unsigned bi = (L >> i) & 1u;
+      for (int j = 0; j < M; ++j) {
+        unsigned bj = (Rb >> j) & 1u;
+        unsigned Ln = (L & ~(1u << i)) | (bj << i);
+        unsigned Rn = (Rb & ~(1u << j)) | (bi << j);
+        score[(i * M + j) * 2 + 0] += pl - (__builtin_popcount(Ln) > N);
+        score[(i * M + j) * 2 + 1] += pr - (__builtin_popcount(Rn) > N);
+      }
+    }
+  };
+  if (s1 == s2) {  // the single-segment fallback may pair a segment with itself
+    for (int k = a; k < ae; ++k) add_row(g.seg_bits[k], g.seg_bits[k]);
+    return;
+  }
+  while (a < ae || b < be) {
+    int ra = a < ae ? g.seg_row[a] : INT32_MAX;
+    int rb = b < be ? g.seg_row[b] : INT32_MAX;
+    if (ra == rb) {
+      add_row(g.seg_bits[a++], g.seg_bits[b++]);
+    } else if (ra < rb) {
+      add_row(g.seg_bits[a++], 0u);
+    } else {
+      add_row(0u, g.seg_bits[b++]);
+    }
+  }
+}
+
+struct NMRunner {
+  int R, M, N, nnz, sched, MAXITER;
+  int* row;
+  int* col;
+  const float* val;
+  std::vector<int> newid;
+  Groups g;
+  std::vector<int> invalid, allzero;
+  std::vector<SwapPair> pool;  // backing store of one score list
+  std::vector<int>* trace_pairs = nullptr;
+  std::vector<int>* trace_ptr = nullptr;
+  std::vector<int> pos;  // start position -> current position
+  bool broken = false;
+
+  void rebuild() {
+    build_groups(R, M, nnz, row, col, val, g);
+    segment_counts(g, N, invalid, allzero);
+  }
+  // locate_invalid_segment[_reverse] (reorder/reorder.h:436-496)
+  InvalSegList locate(bool reverse) {
+    InvalSegList l(reverse ? cmp_reverse : cmp);
+    for (int i = 0; i < g.nseg; ++i)
+      if (invalid[i] != 0) l.push({i, invalid[i]});
+    return l;
+  }
+  static int total(InvalSegList l) {  // get_total_invalid_segment_cnt (:588-599)
+    int c = 0;
+    while (!l.empty()) {
+      c += l.top().second;
+      l.pop();
+    }
+    return c;
+  }
+  bool visited(int v) const { return newid[v] != -1; }
+  bool seg_visited(int s) const {  // reorder/reorder.h:756-764
+    for (int i = 0; i < M; ++i)
+      if (!visited(s * M + i)) return false;
+    return true;
+  }
+  void swap(int v1, int v2) {
+    newid[v1] = v2;
+    newid[v2] = v1;
+    if (trace_pairs) {
+      trace_pairs->push_back(v1);
+      trace_pairs->push_back(v2);
+    }
+  }
+  // get_segment_swap_score (reorder/reorder.h:498-535)
+  SwapPairList score_list(int s1, int s2) {
+    std::vector<int> sc;
+    pair_score(g, N, s1, s2, sc);
+    pool.clear();
+    pool.reserve(M * M);
+    SwapPairList pq(Comparator);
+    for (int i = 0; i < M * M; ++i) pool.emplace_back(s1 * M + i / M, s2 * M + i % M, sc[i * 2], sc[i * 2 + 1]);
+    for (int i = 0; i < M * M; ++i) pq.push(&pool[i]);
+    return pq;
+  }
+  // locate_min_outdeg_seg (reorder/reorder.h:767-797): max all-zero count,
+  // ties to the largest segment id (ascending sort of (count, id), last one).
+  int min_outdeg_seg() {
+    std::vector<std::pair<int, int>> v;
+    for (int i = 0; i < g.nseg; ++i) v.push_back({allzero[i], i});
+    std::sort(v.begin(), v.end());
+    return v.back().second;
+  }
+  // reorderUtil::reorder (reorder/reorder.h:392-418): Reorder kernel + reset
+  void apply() {
+    for (int i = 0; i < nnz; ++i) {
+      int u = row[i], v = col[i];
+      if (newid[u] != -1) row[i] = newid[u];
+      if (newid[v] != -1) col[i] = newid[v];
+    }
+    for (int u = 0; u < R; ++u)
+      if (newid[pos[u]] != -1) pos[u] = newid[pos[u]];
+    std::fill(newid.begin(), newid.end(), -1);
+    rebuild();
+  }
+
+  // run_onepair / _double / _reverse / _reverse_double (reorder.h:1805-2474)
+  std::vector<int> run() {
+    const bool rev = (sched == 2 || sched == 3);
+    const bool redo_traversal = (sched == 1 || sched == 3);
+    newid.assign(R, -1);
+    pos.resize(R);
+    for (int i = 0; i < R; ++i) pos[i] = i;
+    rebuild();
+    InvalSegList L = locate(rev);
+    int init_cnt = total(L);
+    int init_size = (int)L.size();
+    if (init_size > MAXITER) MAXITER = init_size;
+    int round = 1;
+    if (trace_ptr) trace_ptr->push_back(0);
+    while (round <= MAXITER && L.size() >= 1) {
+      if (L.size() == 1) {
+        int minseg = min_outdeg_seg();
+        SwapPairList sc = score_list(L.top().first, minseg);
+        SwapPair* p = sc.top();
+        swap(p->v1, p->v2);
+      }
+      while (L.size() >= 2) {
+        int primary_seg = L.top().first;
+        int primary_cnt = L.top().second;
+        L.pop();
+        InvalSegList tempPQ(redo_traversal ? (rev ? cmp : cmp_reverse) : (rev ? cmp_reverse : cmp));
+        if (redo_traversal) {
+          while (!L.empty()) {
+            tempPQ.push(L.top());
+            L.pop();
+          }
+        } else {
+          tempPQ = L;
+        }
+        InvalSegList updatePQ(rev ? cmp_reverse : cmp);
+        while (!tempPQ.empty()) {
+          if (primary_cnt <= 0 || seg_visited(primary_seg)) break;
+          int target_seg = tempPQ.top().first;
+          int target_cnt = tempPQ.top().second;
+          SwapPairList sc = score_list(primary_seg, target_seg);
+          while (!sc.empty() && (visited(sc.top()->v1) || visited(sc.top()->v2))) sc.pop();
+          if (sc.empty()) {
+            // top() of an empty queue is undefined in the reference
+            // (reorder.h:1908); it cannot happen (a target is never fully
+            // visited while it is still being scored), so flag it.
+            broken = true;
+            return {0, 0, 0, 0, 0};
+          }
+          SwapPair* p = sc.top();
+          swap(p->v1, p->v2);
+          primary_cnt -= p->left_gain;
+          target_cnt -= p->right_gain;
+          if (target_cnt > 0) updatePQ.push({target_seg, target_cnt});
+          tempPQ.pop();
+        }
+        L = updatePQ;
+      }
+      apply();
+      if (trace_ptr) trace_ptr->push_back((int)(trace_pairs->size() / 2));
+      L = locate(rev);
+      round += 1;
+    }
+    L = locate(rev);
+    int final_cnt = total(L);
+    int final_size = (int)L.size();
+    return {init_size, final_size, init_cnt, final_cnt, round - 1};
+  }
+};
+
+int nm_run_impl(int nrows, int nnz, int* row, int* col, const float* val, int N, int M, int sched,
+                int nm_maxiter, int* res5, int* newpos, std::vector<int>* tp, std::vector<int>* tptr) {
+  if (nrows < 0 || nnz < 0 || M < 2 || M > 8 || N < 1 || N >= M || sched < 0 || sched > 3)
+    return ORC_ERR_ARG;
+  if (nrows % M != 0) return ORC_ERR_ARG;
+  // the Reorder kernel indexes newid[] (length nrows) with row and column ids
+  for (int i = 0; i < nnz; ++i)
+    if (row[i] < 0 || row[i] >= nrows || col[i] < 0 || col[i] >= nrows) return ORC_ERR_ARG;
+  NMRunner r;
+  r.R = nrows;
+  r.M = M;
+  r.N = N;
+  r.nnz = nnz;
+  r.sched = sched;
+  r.MAXITER = nm_maxiter;
+  r.row = row;
+  r.col = col;
+  r.val = val;
+  r.trace_pairs = tp;
+  r.trace_ptr = tptr;
+  std::vector<int> res = r.run();
+  if (r.broken) return ORC_ERR_INTERNAL;
+  for (int i = 0; i < 5; ++i) res5[i] = res[i];
+  if (newpos)
+    for (int i = 0; i < nrows; ++i) newpos[i] = r.pos[i];
+  return ORC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// VNM row sort (reordering.py)
+// ---------------------------------------------------------------------------
+struct Segmat {  // generate_segmat (reordering.py:113-119), sparse by row
+  int m = 0, nseg = 0, M = 0;
+  std::vector<int> rp;        // m+1
+  std::vector<int> seg;       // groups, segs ascending within a row
+  std::vector<uint8_t> bits;  // int(segmat[row][seg], 2): offset k at bit M-1-k
+};
+
+void build_segmat(int m, int n, int M, int nnz, const int* row, const int* col, Segmat& s) {
+  s.m = m;
+  s.M = M;
+  s.nseg = n / M;
+  std::vector<std::vector<std::pair<int, uint8_t>>> rows(m);
+  for (int i = 0; i < nnz; ++i) {
+    int sg = col[i] / M;
+    rows[row[i]].push_back({sg, (uint8_t)(1u << (M - 1 - col[i] % M))});
+  }
+  s.rp.assign(m + 1, 0);
+  s.seg.clear();
+  s.bits.clear();
+  for (int r = 0; r < m; ++r) {
+    auto& v = rows[r];
+    std::sort(v.begin(), v.end(), [](const std::pair<int, uint8_t>& a, const std::pair<int, uint8_t>& b) {
+      return a.first < b.first;
+    });
+    for (size_t k = 0; k < v.size(); ++k) {
+      if (!s.seg.empty() && s.rp[r] < (int)s.seg.size() && s.seg.back() == v[k].first) {
+        s.bits.back() |= v[k].second;
+      } else {
+        s.seg.push_back(v[k].first);
+        s.bits.push_back(v[k].second);
+      }
+    }
+    s.rp[r + 1] = (int)s.seg.size();
+  }
+}
+
+// count_invalid_venom_block[_strict] (reordering.py:125-152); both at once.
+void count_vnm(const Segmat& s, int V, int& inv, int& inv_strict) {
+  int nblk = (s.m + V - 1) / V;
+  std::vector<uint8_t> orb((size_t)nblk * s.nseg, 0), bad((size_t)nblk * s.nseg, 0);
+  for (int r = 0; r < s.m; ++r) {
+    int b = r / V;
+    for (int k = s.rp[r]; k < s.rp[r + 1]; ++k) {
+      size_t idx = (size_t)b * s.nseg + s.seg[k];
+      orb[idx] |= s.bits[k];
+      if (__builtin_popcount(s.bits[k]) > 2) bad[idx] = 1;
+    }
+  }
+  inv = inv_strict = 0;
+  for (size_t i = 0; i < orb.size(); ++i) {
+    bool a = __builtin_popcount(orb[i]) > 4;
+    inv += a;
+    inv_strict += (a || bad[i]);
+  }
+}
+
+// construct_bitcode_hash_tab (reordering.py:81-107): the reflected Gray code
+// list index of a bit pattern, negated when it has more than two ones.
+int gray_hash(unsigned code) {
+  unsigned idx = code;
+  for (unsigned sh = 1; sh < 32; sh <<= 1) idx ^= idx >> sh;
+  return __builtin_popcount(code) <= 2 ? (int)idx : -(int)idx;
+}
+
+// One VNM sort: hash_segmat + stable sorted() on the tuples (reordering.py:
+// 162-169, :219-226).  Python compares the per-segment hash lists
+// lexicographically; an absent group hashes to 0.
+std::vector<int> vnm_new_id(const Segmat& s) {
+  std::vector<int> h(s.seg.size());
+  for (size_t k = 0; k < s.seg.size(); ++k) h[k] = gray_hash(s.bits[k]);
+  std::vector<int> order(s.m);
+  for (int i = 0; i < s.m; ++i) order[i] = i;
+  auto less = [&](int a, int b) {
+    int i = s.rp[a], ie = s.rp[a + 1], j = s.rp[b], je = s.rp[b + 1];
+    while (true) {
+      int sa = i < ie ? s.seg[i] : INT32_MAX;
+      int sb = j < je ? s.seg[j] : INT32_MAX;
+      if (sa == INT32_MAX && sb == INT32_MAX) return false;
+      if (sa == sb) {
+        if (h[i] != h[j]) return h[i] < h[j];
+        ++i;
+        ++j;
+      } else if (sa < sb) {  // b has 0 at segment sa
+        if (h[i] != 0) return h[i] < 0;
+        ++i;
+      } else {
+        if (h[j] != 0) return 0 < h[j];
+        ++j;
+      }
+    }
+  };
+  std::stable_sort(order.begin(), order.end(), less);
+  return order;  // new_id[i] = sorted_data[i][0]
+}
+
+int vnm_run_impl(int m0, int n0, int nnz, int* row, int* col, int M, int V, int maxiter, int* out5,
+                 int* newpos) {
+  if (M < 2 || M > 8 || V < 1) return ORC_ERR_ARG;
+  int m = (m0 + M - 1) / M * M, n = (n0 + M - 1) / M * M;  // reordering.py:50-51
+  for (int i = 0; i < nnz; ++i)
+    if (row[i] < 0 || row[i] >= m || col[i] < 0 || col[i] >= n) return ORC_ERR_ARG;
+  Segmat s;
+  build_segmat(m, n, M, nnz, row, col, s);
+  int init_inv, init_strict;
+  count_vnm(s, V, init_inv, init_strict);
+  std::vector<int> prev_r(row, row + nnz), prev_c(col, col + nnz);
+  std::vector<int> comp(m);
+  for (int i = 0; i < m; ++i) comp[i] = i;
+  std::vector<int> prev_comp = comp;
+  int inv = init_inv, prev_inv = init_inv, prev_strict = init_strict;
+  int round = 1;
+  int MAXITER = maxiter;
+  if (init_inv > MAXITER) MAXITER = init_inv;
+  bool early = false;
+  while (inv > 0 && round <= MAXITER) {
+    std::vector<int> nid = vnm_new_id(s);
+    // reorder(): row' = new_id[row], col' = new_id[col] (reordering.py:171-177)
+    std::vector<int> nr(nnz), nc(nnz);
+    for (int i = 0; i < nnz; ++i) {
+      nr[i] = nid[prev_r[i]];
+      nc[i] = nid[prev_c[i]];
+    }
+    std::vector<int> ncomp(m);
+    for (int i = 0; i < m; ++i) ncomp[i] = nid[prev_comp[i]];
+    build_segmat(m, n, M, nnz, nr.data(), nc.data(), s);
+    int istrict;
+    count_vnm(s, V, inv, istrict);
+    if (inv > prev_inv) {  // reordering.py:242-246
+      early = true;
+      break;
+    }
+    prev_inv = inv;
+    prev_strict = istrict;
+    prev_r.swap(nr);
+    prev_c.swap(nc);
+    prev_comp.swap(ncomp);
+    round += 1;
+  }
+  out5[0] = init_inv;
+  out5[1] = init_strict;
+  out5[2] = prev_inv;
+  out5[3] = prev_strict;
+  out5[4] = early ? round : round - 1;
+  std::copy(prev_r.begin(), prev_r.end(), row);
+  std::copy(prev_c.begin(), prev_c.end(), col);
+  if (newpos)
+    for (int i = 0; i < m; ++i) newpos[i] = prev_comp[i];
+  return ORC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Text round trips of the hybrid driver (main.cu:246-311, reordering.py:179-181)
+// ---------------------------------------------------------------------------
+double parse_nm_text(float v) {  // "%.2f" as printed by Mtx::write_to_file
+  char b[64];
+  snprintf(b, sizeof b, "%.2f", (double)v);
+  return strtod(b, nullptr);
+}
+float parse_vnm_text(double d) {  // mmwrite(precision=1) then fscanf "%f"
+  char b[64];
+  snprintf(b, sizeof b, "%.0e", d);
+  return strtof(b, nullptr);
+}
+
+// scipy's MMFile._get_symmetry for a real coo matrix, used by mmwrite when
+// max(shape) < 100 (scipy/io/_fast_matrix_market mmwrite symmetry='AUTO').
+// Returns 0 general, 1 symmetric, 2 skew-symmetric.
+int scipy_symmetry(int n, int nnz, const int* r, const int* c, const double* v) {
+  long up = 0, lo = 0;
+  for (int i = 0; i < nnz; ++i) {
+    if (v[i] == 0.0) continue;
+    if (r[i] < c[i]) ++up;
+    else if (r[i] > c[i]) ++lo;
+  }
+  if (up != lo) return 0;
+  std::vector<std::tuple<int, int, double>> e;
+  for (int i = 0; i < nnz; ++i) e.emplace_back(r[i], c[i], v[i]);
+  std::sort(e.begin(), e.end(), [](const std::tuple<int, int, double>& a, const std::tuple<int, int, double>& b) {
+    return std::make_pair(std::get<0>(a), std::get<1>(a)) < std::make_pair(std::get<0>(b), std::get<1>(b));
+  });
+  auto lookup = [&](int i, int j) -> double {
+    auto it = std::lower_bound(e.begin(), e.end(), std::make_tuple(i, j, -INFINITY),
+                               [](const std::tuple<int, int, double>& a, const std::tuple<int, int, double>& b) {
+                                 return std::make_pair(std::get<0>(a), std::get<1>(a)) <
+                                        std::make_pair(std::get<0>(b), std::get<1>(b));
+                               });
+    if (it != e.end() && std::get<0>(*it) == i && std::get<1>(*it) == j) return std::get<2>(*it);
+    return 0.0;
+  };
+  bool issymm = true, isskew = true;
+  (void)n;
+  for (auto& t : e) {
+    int i = std::get<0>(t), j = std::get<1>(t);
+    double aij = std::get<2>(t);
+    if (i < j) continue;
+    double aji = (i == j) ? aij : lookup(j, i);
+    if (isskew && i == j && aij != 0) {
+      isskew = false;
+    } else {
+      if (issymm && aij != aji) issymm = false;
+      if (isskew && aij != -aji) isskew = false;
+    }
+    if (!(issymm || isskew)) break;
+  }
+  if (issymm) return 1;
+  if (isskew) return 2;
+  return 0;
+}
+
+// The file temp.mtx as the NM stage writes it and the VNM stage reads it.
+struct TextMatrix {
+  int nrows = 0, ncols = 0;
+  std::vector<int> row, col;
+  std::vector<double> val;  // float64 parsed from "%.2f"
+};
+
+TextMatrix nm_write(const Coo& a) {
+  TextMatrix t;
+  t.nrows = a.nrows;
+  t.ncols = a.ncols;
+  t.row = a.row;
+  t.col = a.col;
+  t.val.resize(a.val.size());
+  for (size_t i = 0; i < a.val.size(); ++i) t.val[i] = parse_nm_text(a.val[i]);
+  return t;
+}
+
+// VNM write (scipy mmwrite) + NM read (readMtx) of temp.mtx.
+Coo vnm_write_nm_read(int n, const std::vector<int>& r, const std::vector<int>& c,
+                      const std::vector<double>& v, int M) {
+  int sym = 0;
+  if (n < 100) sym = scipy_symmetry(n, (int)r.size(), r.data(), c.data(), v.data());
+  Coo a;
+  for (size_t i = 0; i < r.size(); ++i) {
+    if (sym != 0 && !(r[i] >= c[i])) continue;  // lower triangle only
+    a.row.push_back(r[i]);
+    a.col.push_back(c[i]);
+    a.val.push_back(parse_vnm_text(v[i]));
+  }
+  int header_nnz = (int)a.row.size();
+  remove_duplicates(a.row, a.col, a.val, sym == 1, header_nnz);
+  custom_sort(a.row, a.col, a.val);
+  a.nrows = n;
+  a.ncols = n;
+  if (a.nrows % M != 0) {
+    a.nrows = (a.nrows + M - 1) / M * M;
+    a.ncols = (a.ncols + M - 1) / M * M;
+  }
+  return a;
+}
+
+void vnm_eval_text(const TextMatrix& t, int M, int V, int* out2) {
+  std::vector<int> r = t.row, c = t.col;
+  orc_vnm_eval(t.nrows, t.ncols, (int)r.size(), r.data(), c.data(), M, V, out2);
+}
+
+int find_best_impl(const Coo& a, int N, int M, int nscheds, int* best, float* out12x4) {
+  int max_id = 0;
+  float max_imprv = 0.0f;
+  for (int s = 0; s < nscheds; ++s) {
+    Coo b = a;
+    int res[5] = {0, 0, 0, 0, 0};
+    int st = nm_run_impl(b.nrows, b.nnz(), b.row.data(), b.col.data(), b.val.data(), N, M, s, 10, res, nullptr,
+                         nullptr, nullptr);
+    if (st) return st;
+    float imp = (res[2] != 0) ? ((res[2] - res[3]) * 1.0f / res[2]) : 0;
+    float out[12] = {(float)b.nrows,
+                     (float)b.nnz(),
+                     b.nnz() * 1.0f / (b.nrows * b.nrows),
+                     (float)res[0],
+                     (float)res[1],
+                     (float)res[2],
+                     (float)res[3],
+                     imp,
+                     (float)res[4],
+                     0.0f,
+                     res[4] ? (res[2] - res[3]) * 1.0f / res[4] : 0.0f,
+                     res[4] ? (res[0] - res[1]) * 1.0f / res[4] : 0.0f};
+    if (out12x4) memcpy(out12x4 + 12 * s, out, sizeof out);
+    if (out[1] == 0 || out[3] == 0) {  // main.cu:85
+      *best = 0;
+      return ORC_OK;
+    }
+    if (out[7] > max_imprv) {  // ties keep the lower id (main.cu:94-101 uses time)
+      max_id = s;
+      max_imprv = out[7];
+    }
+  }
+  *best = max_id;
+  return ORC_OK;
+}
+
+template <class T>
+T* dup_array(const std::vector<T>& v) {
+  T* p = (T*)malloc(sizeof(T) * (v.size() ? v.size() : 1));
+  if (!v.empty()) memcpy(p, v.data(), sizeof(T) * v.size());
+  return p;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C entry points
+// ---------------------------------------------------------------------------
+extern "C" {
+
+void orc_free(void* p) { free(p); }
+
+void orc_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
+
+int orc_get_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_num_procs();
+#else
+  return 1;
+#endif
+}
+
+
+int orc_mtx_read(const char* path, int aligned, int* nrows, int* ncols, int* nnz, int** row, int** col,
+                 float** val) {
+  Coo a;
+  int st = read_mtx_file(path, aligned, a);
+  if (st) return st;
+  *nrows = a.nrows;
+  *ncols = a.ncols;
+  *nnz = a.nnz();
+  *row = dup_array(a.row);
+  *col = dup_array(a.col);
+  *val = dup_array(a.val);
+  return ORC_OK;
+}
+
+int orc_mtx_write(const char* path, int nrows, int ncols, int nnz, const int* row, const int* col,
+                  const float* val) {
+  FILE* f = fopen(path, "w");
+  if (!f) return ORC_ERR_IO;
+  fprintf(f, "%%%%MatrixMarket matrix coordinate real general\n");
+  fprintf(f, "%d %d %d\n", nrows, ncols, nnz);
+  for (int i = 0; i < nnz; ++i) fprintf(f, "%d %d %.2f\n", row[i] + 1, col[i] + 1, (double)val[i]);
+  fclose(f);
+  return ORC_OK;
+}
+
+int orc_nm_run(int nrows, int nnz, int* row, int* col, const float* val, int N, int M, int sched, int nm_maxiter,
+               int* res5, int* newpos) {
+  return nm_run_impl(nrows, nnz, row, col, val, N, M, sched, nm_maxiter, res5, newpos, nullptr, nullptr);
+}
+
+int orc_nm_run_trace(int nrows, int nnz, int* row, int* col, const float* val, int N, int M, int sched,
+                     int nm_maxiter, int* res5, int** pairs, int** round_ptr, int* nrounds) {
+  std::vector<int> tp, tptr;
+  int st = nm_run_impl(nrows, nnz, row, col, val, N, M, sched, nm_maxiter, res5, nullptr, &tp, &tptr);
+  if (st) return st;
+  *pairs = dup_array(tp);
+  *round_ptr = dup_array(tptr);
+  *nrounds = (int)tptr.size() - 1;
+  return ORC_OK;
+}
+
+int orc_nm_segment_counts(int nrows, int nnz, const int* row, const int* col, const float* val, int N, int M,
+                          int* invalid, int* allzero) {
+  if (M < 2 || M > 8 || nrows % M) return ORC_ERR_ARG;
+  Groups g;
+  build_groups(nrows, M, nnz, row, col, val, g);
+  std::vector<int> inv, az;
+  segment_counts(g, N, inv, az);
+  memcpy(invalid, inv.data(), sizeof(int) * inv.size());
+  memcpy(allzero, az.data(), sizeof(int) * az.size());
+  return ORC_OK;
+}
+
+int orc_nm_pair_score(int nrows, int nnz, const int* row, const int* col, const float* val, int N, int M, int seg1,
+                      int seg2, int* score) {
+  if (M < 2 || M > 8 || nrows % M) return ORC_ERR_ARG;
+  Groups g;
+  build_groups(nrows, M, nnz, row, col, val, g);
+  if (seg1 < 0 || seg2 < 0 || seg1 >= g.nseg || seg2 >= g.nseg) return ORC_ERR_ARG;
+  std::vector<int> sc;
+  pair_score(g, N, seg1, seg2, sc);
+  memcpy(score, sc.data(), sizeof(int) * sc.size());
+  return ORC_OK;
+}
+
+void orc_swap_heap_order(int n, const int* lg, const int* rg, int* order) {
+  std::vector<SwapPair> pool;
+  pool.reserve(n);
+  for (int i = 0; i < n; ++i) pool.emplace_back(i, i, lg[i], rg[i]);
+  SwapPairList pq(Comparator);
+  for (int i = 0; i < n; ++i) pq.push(&pool[i]);
+  for (int k = 0; k < n; ++k) {
+    order[k] = pq.top()->v1;
+    pq.pop();
+  }
+}
+
+int orc_vnm_eval(int m0, int n0, int nnz, const int* row, const int* col, int M, int V, int* out2) {
+  if (M < 2 || M > 8 || V < 1) return ORC_ERR_ARG;
+  int m = (m0 + M - 1) / M * M, n = (n0 + M - 1) / M * M;
+  for (int i = 0; i < nnz; ++i)
+    if (row[i] < 0 || row[i] >= m || col[i] < 0 || col[i] >= n) return ORC_ERR_ARG;
+  Segmat s;
+  build_segmat(m, n, M, nnz, row, col, s);
+  count_vnm(s, V, out2[0], out2[1]);
+  return ORC_OK;
+}
+
+int orc_vnm_run(int m, int n, int nnz, int* row, int* col, int M, int V, int maxiter, int* out5, int* newpos) {
+  return vnm_run_impl(m, n, nnz, row, col, M, V, maxiter, out5, newpos);
+}
+
+float orc_roundtrip_nm(float v) {
+  char b[64];
+  snprintf(b, sizeof b, "%.2f", (double)v);
+  return strtof(b, nullptr);
+}
+
+float orc_roundtrip_vnm(float v) { return parse_vnm_text((double)v); }
+
+int orc_find_best(int nrows, int nnz, const int* row, const int* col, const float* val, int N, int M, int nscheds,
+                  int* best, float* out12x4) {
+  if (nscheds < 1 || nscheds > 4) return ORC_ERR_ARG;
+  Coo a;
+  a.nrows = nrows;
+  a.ncols = nrows;
+  a.row.assign(row, row + nnz);
+  a.col.assign(col, col + nnz);
+  a.val.assign(val, val + nnz);
+  return find_best_impl(a, N, M, nscheds, best, out12x4);
+}
+
+int orc_spmm_cli(const char* mtxfile, const char* init_mb_path, int N, int M, int V, int maxiter, double* csv16,
+                 int* best_sched, int* out_nrows, int* out_nnz, int** out_row, int** out_col, float** out_val) {
+  if (M < 2 || M > 8 || N < 1 || N >= M || V < 1 || maxiter < 0) return ORC_ERR_ARG;
+  Coo a0;
+  int st = read_mtx_file(mtxfile, M, a0);
+  if (st) return st;
+  int best = 0;
+  st = find_best_impl(a0, N, M, 4, &best, nullptr);
+  if (st) return st;
+  *best_sched = best;
+  for (int i = 0; i < 16; ++i) csv16[i] = 0;
+  // hybrid_reordering (main.cu:195-337)
+  Coo a = a0;
+  if (a.nnz() == 0) {  // main.cu:204 prints an empty line
+    *out_nrows = a.nrows;
+    *out_nnz = 0;
+    *out_row = dup_array(a.row);
+    *out_col = dup_array(a.col);
+    *out_val = dup_array(a.val);
+    return ORC_OK;
+  }
+  int venom0[2] = {0, 0};
+  if (init_mb_path) {
+    Coo stale;
+    // eval_venom reads the stale temp.mtx through scipy (pattern, no padding
+    // beyond reordering.py:50-51)
+    st = read_mtx_file(init_mb_path, 1, stale);
+    if (st) return st;
+    orc_vnm_eval(stale.nrows, stale.ncols, stale.nnz(), stale.row.data(), stale.col.data(), M, V, venom0);
+  } else {
+    orc_vnm_eval(a.nrows, a.ncols, a.nnz(), a.row.data(), a.col.data(), M, V, venom0);
+  }
+  int res_first[5], res[5];
+  st = nm_run_impl(a.nrows, a.nnz(), a.row.data(), a.col.data(), a.val.data(), N, M, best, 10, res_first, nullptr,
+                   nullptr, nullptr);
+  if (st) return st;
+  memcpy(res, res_first, sizeof res);  // maxiter == 0: the reference indexes an empty vector
+  TextMatrix temp = nm_write(a);
+  Coo out = a;  // written with "%.2f" of these values
+  int nm_round = 0, vnm_round = 0;
+  for (int it = 0; it < maxiter; ++it) {
+    // VNM_reordering: python3 reordering.py on temp.mtx (main.cu:116-153)
+    std::vector<int> r = temp.row, c = temp.col;
+    int out5[5];
+    st = vnm_run_impl(temp.nrows, temp.ncols, (int)r.size(), r.data(), c.data(), M, V, 10, out5, nullptr);
+    if (st) return st;
+    vnm_round += out5[4];
+    int n = (temp.ncols + M - 1) / M * M;
+    Coo b = vnm_write_nm_read(n, r, c, temp.val, M);
+    st = nm_run_impl(b.nrows, b.nnz(), b.row.data(), b.col.data(), b.val.data(), N, M, best, 10, res, nullptr,
+                     nullptr, nullptr);
+    if (st) return st;
+    nm_round += res[4];
+    temp = nm_write(b);
+    if (it == maxiter - 1) out = b;
+  }
+  int venom1[2];
+  vnm_eval_text(temp, M, V, venom1);
+  float improve = (res_first[2] != 0) ? ((res_first[2] - res[3]) * 1.0f / res_first[2]) : 0;
+  csv16[0] = (float)a0.nrows;
+  csv16[1] = (float)a0.nnz();
+  // nrows*nrows is an int product in the reference (wraps past 46340 rows)
+  csv16[2] = a0.nnz() * 1.0f / (int)((unsigned)a0.nrows * (unsigned)a0.nrows);
+  csv16[3] = res_first[0];
+  csv16[4] = res[1];
+  csv16[5] = res_first[2];
+  csv16[6] = res[3];
+  csv16[7] = improve;
+  csv16[8] = venom0[0];
+  csv16[9] = venom1[0];
+  csv16[10] = venom0[1];
+  csv16[11] = venom1[1];
+  csv16[12] = nm_round;
+  csv16[13] = vnm_round;
+  csv16[14] = nm_round + vnm_round;
+  csv16[15] = 0;
+  *out_nrows = out.nrows;
+  *out_nnz = out.nnz();
+  *out_row = dup_array(out.row);
+  *out_col = dup_array(out.col);
+  *out_val = dup_array(out.val);
+  return ORC_OK;
+}
+
+int64_t orc_retained_nm(int nrows, int nnz, const int* row, const int* col, const float* val, int N, int M) {
+  Groups g;
+  build_groups(nrows, M, nnz, row, col, val, g);
+  int64_t t = 0;
+  for (size_t k = 0; k < g.seg_bits.size(); ++k) t += std::min(__builtin_popcount(g.seg_bits[k]), N);
+  return t;
+}
+
+int64_t orc_retained_vnm(int nrows, int nnz, const int* row, const int* col, const float* val, int N, int M,
+                         int V) {
+  Groups g;
+  build_groups(nrows, M, nnz, row, col, val, g);
+  int64_t t = 0;
+  for (int s = 0; s < g.nseg; ++s) {
+    int k = g.seg_ptr[s], ke = g.seg_ptr[s + 1];
+    while (k < ke) {
+      int blk = g.seg_row[k] / V;
+      int kb = k;
+      int colcnt[8] = {0};
+      while (k < ke && g.seg_row[k] / V == blk) {
+        for (int o = 0; o < M; ++o) colcnt[o] += (g.seg_bits[k] >> o) & 1;
+        ++k;
+      }
+      // keep the 4 columns with the most nonzeros, ties to the lower offset
+      unsigned kept = 0;
+      for (int pick = 0; pick < 4 && pick < M; ++pick) {
+        int bo = -1;
+        for (int o = 0; o < M; ++o)
+          if (!((kept >> o) & 1) && (bo < 0 || colcnt[o] > colcnt[bo])) bo = o;
+        kept |= 1u << bo;
+      }
+      for (int q = kb; q < k; ++q) t += std::min(__builtin_popcount(g.seg_bits[q] & kept), N);
+    }
+  }
+  return t;
+}
+
+void orc_spmm_f64(int nrows, int nnz, const int* row, const int* col, const double* val, const double* B, int n,
+                  double* C) {
+  memset(C, 0, sizeof(double) * (size_t)nrows * n);
+  for (int i = 0; i < nnz; ++i) {
+    const double a = val[i];
+    const double* b = B + (size_t)col[i] * n;
+    double* c = C + (size_t)row[i] * n;
+    for (int j = 0; j < n; ++j) c[j] += a * b[j];
+  }
+}
+
+}  // extern "C"

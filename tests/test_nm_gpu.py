@@ -1,0 +1,125 @@
+"""Parity of the CUDA NM reorder (through the C ABI) with the oracle and with
+the reference's own results (tests/golden/nm_ref_goldens.npz).
+
+Bit-exact throughout: the path is integer-only."""
+import numpy as np
+import pytest
+
+import oracle
+from golden_cases import nm_cases, nm_input
+
+pytestmark = pytest.mark.gpu
+
+
+def _keys(goldens):
+    return sorted({key for _, key, _, _, _ in nm_cases(goldens)})
+
+
+def test_segment_counts_match_oracle(ctx, goldens):
+    for key in _keys(goldens):
+        nr, r, c, v = nm_input(goldens, key)
+        N, M = int(key.split("__n")[1].split("_")[0]), int(key.split("_m")[-1])
+        inv, az = ctx.nm_segment_counts(nr, r, c, v, N, M)
+        oinv, oaz = oracle.nm_segment_counts(nr, r, c, v, N, M)
+        assert np.array_equal(inv, oinv), key
+        assert np.array_equal(az, oaz), key
+
+
+def test_pair_scores_match_oracle(ctx, goldens):
+    rng = np.random.default_rng(0)
+    for key in _keys(goldens):
+        nr, r, c, v = nm_input(goldens, key)
+        N, M = int(key.split("__n")[1].split("_")[0]), int(key.split("_m")[-1])
+        nseg = nr // M
+        pairs = [(0, 0), (0, nseg - 1)] + [tuple(rng.integers(0, nseg, 2)) for _ in range(6)]
+        for s1, s2 in pairs:
+            got = ctx.nm_pair_score(nr, r, c, v, N, M, int(s1), int(s2))
+            want = oracle.nm_pair_score(nr, r, c, v, N, M, int(s1), int(s2))
+            assert np.array_equal(got, want), (key, s1, s2)
+
+
+def test_reorder_matches_oracle_every_case(ctx, goldens):
+    bad = []
+    for case, key, N, M, s in nm_cases(goldens):
+        nr, r, c, v = nm_input(goldens, key)
+        res, newpos = ctx.nm_reorder(nr, r, c, v, N, M, s)
+        ores, _, _, opos = oracle.nm_run(nr, r, c, v, N, M, s)
+        if not (np.array_equal(res, ores) and np.array_equal(newpos, opos)):
+            bad.append((case, res.tolist(), ores.tolist()))
+    assert not bad, bad[:5]
+
+
+def test_reorder_trace_matches_oracle(ctx, goldens):
+    ctx.set_trace(True)
+    try:
+        for key in ("rmat_1024__n2_m8", "rmat_2048__n2_m4", "lund_b__n2_m8", "c1_512__n1_m4"):
+            nr, r, c, v = nm_input(goldens, key)
+            N, M = int(key.split("__n")[1].split("_")[0]), int(key.split("_m")[-1])
+            for s in range(4):
+                res, _ = ctx.nm_reorder(nr, r, c, v, N, M, s)
+                tr = ctx.get_trace()
+                ores, otr = oracle.nm_run_trace(nr, r, c, v, N, M, s)
+                assert len(tr) == len(otr), (key, s)
+                for k, (a, b) in enumerate(zip(tr, otr)):
+                    assert np.array_equal(a, b), (key, s, "round", k)
+    finally:
+        ctx.set_trace(False)
+
+
+def test_reorder_matches_reference_goldens(ctx, goldens):
+    """Against the numbers the reference's own GPU code produced."""
+    bad = []
+    for case, key, N, M, s in nm_cases(goldens):
+        nr, r, c, v = nm_input(goldens, key)
+        res, newpos = ctx.nm_reorder(nr, r, c, v, N, M, s)
+        pos = goldens["pos__" + case]
+        m = pos >= 0
+        if not (np.array_equal(res, goldens["res__" + case]) and np.array_equal(newpos[m], pos[m])):
+            bad.append(case)
+    assert not bad, "%d of the reference cases differ, e.g. %s" % (len(bad), bad[:4])
+
+
+def test_search_picks_like_find_best(ctx, goldens):
+    for key in ("c1_512__n2_m8", "rmat_1024__n2_m4", "u256_d05__n1_m4", "GD01_c__n2_m8"):
+        nr, r, c, v = nm_input(goldens, key)
+        N, M = int(key.split("__n")[1].split("_")[0]), int(key.split("_m")[-1])
+        best, res, newpos = ctx.nm_search(nr, r, c, v, N, M)
+        obest, _ = oracle.find_best(nr, r, c, v, N, M)
+        assert best == obest, key
+        for s in range(4):
+            ores, _, _, _ = oracle.nm_run(nr, r, c, v, N, M, s)
+            assert np.array_equal(res[s], ores), (key, s)
+        ores, _, _, opos = oracle.nm_run(nr, r, c, v, N, M, best)
+        assert np.array_equal(newpos, opos), key
+
+
+def test_device_pointers_and_permute(ctx, goldens):
+    import torch
+    nr, r, c, v = nm_input(goldens, "rmat_2048__n2_m4")
+    tr = torch.from_numpy(r.astype(np.int32)).cuda()
+    tc = torch.from_numpy(c.astype(np.int32)).cuda()
+    tv = torch.from_numpy(v.astype(np.float32)).cuda()
+    res, newpos = ctx.nm_reorder(nr, tr, tc, tv, 2, 4, 1)
+    ores, orow, ocol, opos = oracle.nm_run(nr, r, c, v, 2, 4, 1)
+    assert np.array_equal(res, ores) and np.array_equal(newpos, opos)
+    pr, pc = ctx.permute_coo(nr, tr, tc, torch.from_numpy(newpos).cuda())
+    assert np.array_equal(pr.cpu().numpy(), orow) and np.array_equal(pc.cpu().numpy(), ocol)
+    hr, hc = ctx.permute_coo(nr, r, c, newpos)
+    assert np.array_equal(hr, orow) and np.array_equal(hc, ocol)
+
+
+def test_errors_are_reported(ctx):
+    import vnm_gb300
+    r = np.array([1, 0], np.int32)  # not sorted
+    c = np.array([0, 1], np.int32)
+    v = np.ones(2, np.float32)
+    with pytest.raises(vnm_gb300.VnmError) as e:
+        ctx.nm_reorder(8, r, c, v, 2, 4, 0)
+    assert e.value.status == 3
+    with pytest.raises(vnm_gb300.VnmError) as e:
+        ctx.nm_reorder(8, np.array([0], np.int32), np.array([9], np.int32), v[:1], 2, 4, 0)
+    assert e.value.status == 4
+    with pytest.raises(vnm_gb300.VnmError):
+        ctx.nm_reorder(6, r[:0], c[:0], v[:0], 2, 4, 0)  # nrows not a multiple of M
+    res, newpos = ctx.nm_reorder(8, r[:0], c[:0], v[:0], 2, 4, 0)  # empty matrix
+    assert res.tolist() == [0, 0, 0, 0, 0] and newpos.tolist() == list(range(8))

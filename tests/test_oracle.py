@@ -1,0 +1,141 @@
+"""CPU tests: the oracle against the reference's own outputs, the number
+formats of the file round trips, the heap emulation, and the C ABI exports.
+No GPU is used here."""
+import os
+import re
+import warnings
+
+import numpy as np
+import pytest
+
+import oracle
+from golden_cases import nm_cases, nm_input
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def vnm_goldens():
+    return np.load(os.path.join(REPO, "tests", "golden", "vnm_ref_goldens.npz"))
+
+
+def test_oracle_nm_matches_reference_every_case(goldens):
+    """run_onepair* of the reference, run on a GB300 (tests/golden/make_nm_goldens.py)."""
+    bad = []
+    for case, key, N, M, s in nm_cases(goldens):
+        nr, r, c, v = nm_input(goldens, key)
+        res, _, _, newpos = oracle.nm_run(nr, r, c, v, N, M, s)
+        pos = goldens["pos__" + case]
+        m = pos >= 0
+        if not (np.array_equal(res, goldens["res__" + case]) and np.array_equal(newpos[m], pos[m])):
+            bad.append(case)
+    assert not bad, bad
+
+
+def test_oracle_nm_final_coo_hash(goldens):
+    import hashlib
+    for case, key, N, M, s in list(nm_cases(goldens))[::7]:
+        nr, r, c, v = nm_input(goldens, key)
+        _, r2, c2, _ = oracle.nm_run(nr, r, c, v, N, M, s)
+        body = np.stack([r2, c2], 1).astype(np.int32)
+        assert hashlib.sha256(body.tobytes()).digest() == goldens["sha__" + case].tobytes(), case
+
+
+def test_oracle_vnm_matches_reordering_py(vnm_goldens):
+    g = vnm_goldens
+    for case in g["cases"].tolist():
+        name, mv = case.split("__")
+        M, V = int(mv.split("_")[0][1:]), int(mv.split("_")[1][1:])
+        n = int(g["in__%s__n" % name])
+        r, c = g["in__%s__row" % name], g["in__%s__col" % name]
+        assert oracle.vnm_eval(n, n, r, c, M, V).tolist() == g["eval__" + case].tolist(), case
+        out5, r2, c2, newpos = oracle.vnm_run(n, n, r, c, M, V)
+        assert out5.tolist() == g["out__" + case].tolist(), case
+        want = set(zip(g["wrow__" + case].tolist(), g["wcol__" + case].tolist()))
+        assert set(zip(r2.tolist(), c2.tolist())) == want, case
+        # the composed row map explains the written matrix
+        assert np.array_equal(newpos[r], r2) and np.array_equal(newpos[c], c2), case
+
+
+def test_vnm_writer_number_format(vnm_goldens):
+    """scipy mmwrite(precision=1) prints '%.0e' (pinned against scipy itself)."""
+    vals = vnm_goldens["fmt__in"]
+    text = vnm_goldens["fmt__text"]
+    for v, t in zip(vals.tolist(), text.tolist()):
+        assert "%.0e" % v == t, (v, t)
+        f32 = np.float32(v)
+        assert oracle.roundtrip_vnm(f32) == np.float32(float("%.0e" % float(f32)))
+
+
+def test_nm_writer_round_trip():
+    rng = np.random.default_rng(1)
+    for v in np.concatenate([rng.standard_normal(500), [0.004999, 0.005, -0.0049, 0.125, 1e6]]).astype(np.float32):
+        assert oracle.roundtrip_nm(v) == np.float32(float("%.2f" % float(v)))
+
+
+def test_reader_matches_scipy_pattern():
+    """readMtx: mirror symmetric files, drop repeats, sort, pad to M."""
+    from scipy.io import mmread
+    d = os.path.join(REPO, "tests", "golden", "nm_inputs")
+    if not os.path.isdir(d):
+        pytest.skip("golden inputs not generated (tests/golden/make_nm_goldens.py prepare)")
+    for f in sorted(os.listdir(d))[:6]:
+        path = os.path.join(d, f)
+        nr, nc, r, c, v = oracle.read_mtx(path, 8)
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            m = mmread(path).tocoo()
+        assert nr % 8 == 0 and nr >= m.shape[0]
+        key = r.astype(np.int64) * nr + c
+        assert np.all(np.diff(key) > 0)
+        want = set(zip(m.row.tolist(), m.col.tolist()))
+        assert set(zip(r.tolist(), c.tolist())) == want, f
+
+
+def test_heap_emulation_matches_libstdcxx():
+    import vnm_gb300
+    rng = np.random.default_rng(0)
+    for t in range(3000):
+        n = int(rng.choice([1, 2, 5, 16, 36, 64]))
+        lo, hi = [(0, 1), (-1, 2), (-3, 4), (-40, 40)][t % 4]
+        lg = rng.integers(lo, hi, n)
+        rg = rng.integers(lo, hi, n)
+        assert np.array_equal(oracle.swap_heap_order(lg, rg), vnm_gb300.swap_heap_order(lg, rg))
+
+
+def test_library_exports_every_declared_symbol():
+    import ctypes
+    import vnm_gb300
+    lib = ctypes.CDLL(vnm_gb300.LIB_PATH)
+    names = set()
+    for h in os.listdir(os.path.join(REPO, "include")):
+        if h.endswith(".h"):
+            src = open(os.path.join(REPO, "include", h)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names |= set(re.findall(r"\b(vnm_[a-z0-9_]+)\s*\(", src))
+    assert len(names) > 10
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_status_strings_and_cpu_side_errors():
+    import vnm_gb300
+    assert vnm_gb300.status_string(0) == "ok"
+    assert "sorted" in vnm_gb300.status_string(3)
+    assert vnm_gb300.version().endswith("sm_103a")
+    with pytest.raises(vnm_gb300.VnmError):
+        vnm_gb300.swap_heap_order(np.zeros(300), np.zeros(300))
+
+
+def test_oracle_cli_composition_on_fixture():
+    """The whole spmm command on a small file: CSV fields are consistent."""
+    d = os.path.join(REPO, "tests", "golden", "nm_inputs")
+    if not os.path.isdir(d):
+        pytest.skip("golden inputs not generated")
+    path = os.path.join(d, "u256_d05.mtx")
+    csv, best, nr, r, c, v = oracle.spmm_cli(path, 2, 8, 32, 2)
+    nr0, _, r0, c0, v0 = oracle.read_mtx(path, 8)
+    res0, _, _, _ = oracle.nm_run(nr0, r0, c0, v0, 2, 8, best)
+    assert csv[0] == nr0 and csv[1] == len(r0)
+    assert csv[3] == res0[0] and csv[5] == res0[2]
+    assert len(r) == len(r0) and nr == nr0

@@ -1,0 +1,110 @@
+// Shared definitions of libvnm_gb300: status handling, the context object,
+// the device scratch arena and launch accounting.
+#ifndef VNM_COMMON_CUH
+#define VNM_COMMON_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "../../include/vnm_gb300.h"
+
+#define VNM_CUDA_TRY(expr)                    \
+  do {                                        \
+    cudaError_t e_ = (expr);                  \
+    if (e_ != cudaSuccess) {                  \
+      (void)cudaGetLastError();               \
+      return e_ == cudaErrorMemoryAllocation  \
+                 ? VNM_ERR_NOMEM              \
+                 : VNM_ERR_CUDA;              \
+    }                                         \
+  } while (0)
+
+#define VNM_TRY(expr)          \
+  do {                         \
+    vnm_status s_ = (expr);    \
+    if (s_ != VNM_OK) return s_; \
+  } while (0)
+
+// Launch with accounting; the kernel's launch error is checked right away.
+#define VNM_LAUNCH(ctx, kernel, grid, block, smem, ...)                             \
+  do {                                                                              \
+    kernel<<<(grid), (block), (smem), (ctx)->stream>>>(__VA_ARGS__);                \
+    (ctx)->launches++;                                                              \
+    cudaError_t le_ = cudaGetLastError();                                           \
+    if (le_ != cudaSuccess) return VNM_ERR_CUDA;                                    \
+  } while (0)
+
+// Grow-only device arena: one allocation reused by successive calls.
+struct DeviceArena {
+  char* base = nullptr;
+  size_t cap = 0;
+  size_t used = 0;
+};
+
+struct vnm_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+  cudaEvent_t ev_main0 = nullptr, ev_main1 = nullptr;  // around the call's main kernel
+  float last_ms = 0.f;
+  float main_ms = 0.f;
+  long long stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // work counters of the last call
+  int launches = 0;
+  DeviceArena arena;
+  // pinned staging for small results
+  int* h_pinned = nullptr;
+  size_t h_pinned_cap = 0;
+  // swap trace of the last NM call (host copies)
+  bool trace = false;
+  std::vector<int> trace_pairs, trace_round_end;
+};
+
+namespace vnm {
+
+// Reserve `bytes` (256-byte aligned) of the arena; valid until arena_reset.
+vnm_status arena_reserve(vnm_ctx* ctx, size_t total_bytes);
+template <class T>
+inline T* arena_take(vnm_ctx* ctx, size_t count) {
+  size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
+  if (ctx->arena.used + bytes > ctx->arena.cap) return nullptr;
+  T* p = reinterpret_cast<T*>(ctx->arena.base + ctx->arena.used);
+  ctx->arena.used += bytes;
+  return p;
+}
+inline size_t arena_bytes(size_t count, size_t elem) { return (count * elem + 255) & ~size_t(255); }
+
+vnm_status begin_call(vnm_ctx* ctx);
+vnm_status end_call(vnm_ctx* ctx);  // records the stop event and synchronises
+vnm_status pinned_reserve(vnm_ctx* ctx, size_t ints);
+
+// Copy a caller array to the device (or alias it when it already is there).
+template <class T>
+inline vnm_status stage_in(vnm_ctx* ctx, const T* src, size_t count, int mem, const T** dst) {
+  if (mem == VNM_MEM_DEVICE) {
+    *dst = src;
+    return VNM_OK;
+  }
+  T* d = arena_take<T>(ctx, count);
+  if (!d) return VNM_ERR_NOMEM;
+  if (count) VNM_CUDA_TRY(cudaMemcpyAsync(d, src, count * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+  *dst = d;
+  return VNM_OK;
+}
+
+// exclusive prefix sum of n ints (out may alias in); returns the total in
+// *d_total (device).  Uses arena scratch.
+vnm_status exclusive_scan(vnm_ctx* ctx, const int* d_in, int* d_out, int n, int* d_total);
+size_t scan_scratch_bytes(int n);
+
+// stable LSD radix sort of 64-bit keys (low `bits` bits) carrying int payloads
+// (nullptr payload = original positions); see radix_sort.cu
+vnm_status radix_sort_u64(vnm_ctx* ctx, const unsigned long long* keys, const int* vals, int n, int bits,
+                          unsigned long long** out_keys, int** out_vals);
+size_t radix_sort_scratch_bytes(int n);
+
+}  // namespace vnm
+
+#endif

@@ -1,0 +1,1233 @@
+// NM reorder on the GPU: a bit-exact, GB300-native rebuild of the reference's
+// greedy swap search (reorder/reorder.h:1805-2474, reorder/swappair.h).
+//
+// What the reference does per round: recount invalid groups for every
+// (row, segment) with one thread each (LocateinvalidSegment), then for each
+// (primary, target) segment pair it visits, launch GetSegSwapScore over all
+// rows (with cudaMalloc / memset / memcpy / cudaFree around it), push the M*M
+// gains into a std::priority_queue, commit the best unvisited swap, and at
+// the end of the round apply all swaps to the COO, copy it to the host, sort
+// it, copy it back and rebuild BSR with cuSPARSE (Mtx::reset).
+//
+// Facts this design is built on (each is a property of the reference code):
+//   1. A symmetric swap moves a row's groups to another row without changing
+//      them, so invalid counts depend only on which node sits at which column
+//      position.  The state of a job is therefore `orig[pos]` (the original
+//      node at each position) plus per-segment counts; rows keep their
+//      original ids throughout.
+//   2. All gains of a round are computed against the round-start matrix
+//      (swaps are applied only in reorder()), and a primary segment can take
+//      at most M targets before all of its nodes are visited.  After the
+//      first primary, the list is a subset of its <= M targets.  So a round
+//      touches at most M+1 segments -- the first M+1 of the list in the
+//      traversal order of the schedule -- and needs the gains of the
+//      C(M+1, 2) segment pairs among them, all of which are computed up
+//      front, in parallel.
+//   3. For rows that touch only one of the two segments of a pair, the gain
+//      depends on that segment alone: the left gain of swap (i, j) over such
+//      rows is S_p(i) = #rows with bit i set and popcount == N+1.  Only rows
+//      that touch both segments need the per-(i, j) terms.
+//   4. The pop order of the swap-pair heap is fixed once its gains are known;
+//      the visited filter only skips ahead in it.  So each ordered pair's pop
+//      order is computed once per round by one thread (exact libstdc++ sift
+//      steps, swap_heap.h) and the walk reads the first unvisited entry.
+//
+// One thread block runs one job (a matrix and a schedule) for all of its
+// rounds: no host round trips, no atomics on global counters in the loop,
+// no allocation.  Many jobs (four schedules, or a batch of matrices) run in
+// one launch.
+
+#include <cstdio>
+#include <cstring>
+
+#include "common.cuh"
+#include "swap_heap.h"
+
+namespace vnm {
+
+size_t scan_scratch_bytes(int n);
+
+constexpr int NM_THREADS = 512;  // threads per job block
+constexpr unsigned FULL = 0xffffffffu;
+
+// status bits a job reports in res[5]
+constexpr int JOB_OK = 0;
+constexpr int JOB_EMPTY_HEAP = 1;   // reference would call top() on an empty queue
+constexpr int JOB_BAD_STATE = 2;    // a count went out of range
+
+struct NMJob {
+  int R;              // padded rows = columns
+  int nseg;           // R / M
+  int sched;          // 0..3
+  int maxiter;        // reorderUtil MAXITER before it is raised to init_size
+  const int* cptr;    // [R+1] column pointers of the nonzero pattern (original ids)
+  const int* crow;    // rows of each column
+  int* orig;          // [R] original node at each position (identity on entry)
+  int* cnt;           // [nseg] invalid rows per segment
+  int* zc;            // [nseg] all-zero rows per segment
+  uint4* rec;         // [R] per-row scratch, zero on entry and on exit
+  int* touched;       // [R] scratch
+  int* res;           // [16]: init_size, final_size, init_cnt, final_cnt, rounds, status,
+                      //       swaps, gathered entries (lo, hi), touched rows (lo, hi)
+  int* trace_pairs;   // optional: swaps in commit order (v1, v2)
+  int* trace_rounds;  // optional: pairs committed by the end of each round
+  int trace_cap_pairs;
+  int trace_cap_rounds;
+};
+
+// ---------------------------------------------------------------------------
+// Setup kernels
+// ---------------------------------------------------------------------------
+
+// Range and strict (row, col) order check of the caller's COO.
+__global__ void k_validate(const int* row, const int* col, int nnz, int R, int* err) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += gridDim.x * blockDim.x) {
+    int r = row[i], c = col[i];
+    if (r < 0 || r >= R || c < 0 || c >= R) {
+      atomicOr(err, 2);
+      continue;
+    }
+    if (i > 0) {
+      int rp = row[i - 1], cp = col[i - 1];
+      if (rp > r || (rp == r && cp >= c)) atomicOr(err, 1);
+    }
+  }
+}
+
+__global__ void k_nonzero_flags(const float* val, int nnz, int* flags) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += gridDim.x * blockDim.x)
+    flags[i] = val[i] != 0.0f;  // reorder/reorder.h:93: the bitmap bit is (val != 0)
+}
+
+// Keep the entries with nonzero value, in order; count entries per column.
+__global__ void k_compact(const int* row, const int* col, const float* val, const int* pos, int nnz, int* prow,
+                          int* pcol, int* coldeg) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += gridDim.x * blockDim.x) {
+    if (val[i] != 0.0f) {
+      int p = pos[i];
+      prow[p] = row[i];
+      pcol[p] = col[i];
+      atomicAdd(&coldeg[col[i]], 1);
+    }
+  }
+}
+
+__global__ void k_csc_scatter(const int* prow, const int* pcol, int np, const int* cptr, int* cfill, int* crow) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+    int c = pcol[i];
+    int slot = atomicAdd(&cfill[c], 1);
+    crow[cptr[c] + slot] = prow[i];
+  }
+}
+
+// Invalid and non-empty group counts per segment at the identity arrangement.
+// The pattern is sorted by (row, col), so a row's groups are runs of entries
+// with equal col / M; the last entry of each run does the counting.
+template <int M>
+__global__ void k_locate(const int* prow, const int* pcol, int np, int N, int* inv, int* pres) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+    const int r = prow[i], s = pcol[i] / M;
+    const bool last = (i + 1 == np) || prow[i + 1] != r || pcol[i + 1] / M != s;
+    if (!last) continue;
+    int len = 1;
+#pragma unroll
+    for (int b = 1; b < M; ++b) {
+      int k = i - b;
+      if (k >= 0 && prow[k] == r && pcol[k] / M == s) len++;
+    }
+    atomicAdd(&pres[s], 1);
+    if (len > N) atomicAdd(&inv[s], 1);
+  }
+}
+
+__global__ void k_init_job(int* orig, int* cnt, int* zc, const int* inv0, const int* pres0, int R, int nseg) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x) {
+    orig[i] = i;
+    if (i < nseg) {
+      cnt[i] = inv0[i];
+      zc[i] = R - pres0[i];
+    }
+  }
+}
+
+// newpos[orig[p]] = p
+__global__ void k_invert(const int* orig, int R, int* newpos) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x) newpos[orig[i]] = i;
+}
+
+__global__ void k_permute(int* row, int* col, int nnz, const int* newpos) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += gridDim.x * blockDim.x) {
+    row[i] = newpos[row[i]];
+    col[i] = newpos[col[i]];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The round kernel
+// ---------------------------------------------------------------------------
+template <int M>
+struct RoundSmem {
+  static constexpr int K = M + 1;           // segments a round can touch
+  static constexpr int NPAIR = K * (K - 1) / 2;
+  static constexpr int MM = M * M;
+  static constexpr int NW = NM_THREADS / 32;
+  int xseg[K];      // the segments of this round, xseg[0] first
+  int xcnt[K];      // their counts at round start
+  int K_;           // how many
+  int mode;         // 0 = pair walk, 1 = single invalid segment + minseg, 2 = single, minseg is itself
+  int lsize, ltotal;
+  int minseg;
+  int ntouched;
+  int E;            // gathered entries
+  int status;
+  int nswaps;
+  int S[K][M];                 // S_x(k): rows with bit k set and popcount == N+1
+  int CL[NPAIR][MM];           // per unordered pair (a < b): left-side corrections
+  int CR[NPAIR][MM];           //                              right-side corrections
+  uint8_t ord[K * K][MM];      // pop order per ordered pair (a * K + b)
+  int colstart[K * M];
+  int colpre[K * M + 1];
+  uint8_t dest[K][M];          // bit moves of this round's swaps: (xi << 4) | k
+  int newinv[K], newpres[K];
+  int swaps[2 * K * M];        // committed swaps (positions)
+  unsigned long long wtop[2][NW][K];
+  unsigned long long top[2][K];  // [0] Ldesc order (cnt desc, seg asc), [1] reverse
+  unsigned long long red64[NW];
+  int red32[2][NW];
+};
+
+template <int M>
+__device__ __forceinline__ int pair_id(int a, int b) {  // a < b < K
+  constexpr int K = M + 1;
+  return a * (2 * K - a - 1) / 2 + (b - a - 1);
+}
+
+// Gains of swap idx = i*M + j of ordered pair (a = primary side, b = target side).
+template <int M>
+__device__ __forceinline__ void pair_gains(const RoundSmem<M>& sm, int a, int b, int idx, int& l, int& r) {
+  const int i = idx / M, j = idx % M;
+  if (a == b) {  // single segment paired with itself: direct sums kept in CL/CR[0]
+    l = sm.CL[0][idx];
+    r = sm.CR[0][idx];
+  } else if (a < b) {
+    const int p = pair_id<M>(a, b);
+    l = sm.S[a][i] - sm.CL[p][i * M + j];
+    r = sm.S[b][j] - sm.CR[p][i * M + j];
+  } else {
+    const int p = pair_id<M>(b, a);
+    l = sm.S[a][i] - sm.CR[p][j * M + i];
+    r = sm.S[b][j] - sm.CL[p][j * M + i];
+  }
+}
+
+// insert `key` into a register list sorted descending (0 = empty)
+template <int K>
+__device__ __forceinline__ void topk_insert(unsigned long long (&a)[K], unsigned long long key) {
+  if (key <= a[K - 1]) return;
+  a[K - 1] = key;
+#pragma unroll
+  for (int q = K - 1; q > 0; --q) {
+    if (a[q] > a[q - 1]) {
+      unsigned long long t = a[q];
+      a[q] = a[q - 1];
+      a[q - 1] = t;
+    }
+  }
+}
+
+// merge the 32 lanes' sorted lists; lane 0 gets the warp's top K in out[]
+template <int K>
+__device__ __forceinline__ void topk_warp_merge(unsigned long long (&a)[K], unsigned long long* out) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int q = 0; q < K; ++q) {
+    unsigned long long h = a[0], m = h;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long t = __shfl_xor_sync(FULL, m, o);
+      m = t > m ? t : m;
+    }
+    if (lane == 0) out[q] = m;
+    if (h == m && m != 0) {
+#pragma unroll
+      for (int z = 0; z < K - 1; ++z) a[z] = a[z + 1];
+      a[K - 1] = 0;
+    }
+  }
+}
+
+// Scan the segment counts: list size, total, first K in both orders.
+template <int M>
+__device__ void select_phase(RoundSmem<M>& sm, const NMJob& J) {
+  constexpr int K = M + 1;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  unsigned long long kd[K], kr[K];
+#pragma unroll
+  for (int q = 0; q < K; ++q) kd[q] = kr[q] = 0;
+  int lsz = 0, tot = 0;
+  for (int s = tid; s < J.nseg; s += NM_THREADS) {
+    const int c = J.cnt[s];
+    if (c > 0) {
+      lsz++;
+      tot += c;
+      topk_insert<K>(kd, ((unsigned long long)(unsigned)c << 32) | (unsigned)(0xffffffffu - (unsigned)s));
+      topk_insert<K>(kr, ((unsigned long long)(unsigned)(0x7fffffff - c) << 32) | (unsigned)s);
+    }
+  }
+  topk_warp_merge<K>(kd, sm.wtop[0][w]);
+  topk_warp_merge<K>(kr, sm.wtop[1][w]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lsz += __shfl_xor_sync(FULL, lsz, o);
+    tot += __shfl_xor_sync(FULL, tot, o);
+  }
+  if (lane == 0) {
+    sm.red32[0][w] = lsz;
+    sm.red32[1][w] = tot;
+  }
+  __syncthreads();
+  if (w < 2) {  // warp 0 merges the descending lists, warp 1 the reverse ones
+    unsigned long long a[K];
+#pragma unroll
+    for (int q = 0; q < K; ++q) a[q] = lane < RoundSmem<M>::NW ? sm.wtop[w][lane][q] : 0ull;
+    topk_warp_merge<K>(a, sm.top[w]);
+  } else if (w == 2) {
+    int v0 = lane < RoundSmem<M>::NW ? sm.red32[0][lane] : 0;
+    int v1 = lane < RoundSmem<M>::NW ? sm.red32[1][lane] : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      v0 += __shfl_xor_sync(FULL, v0, o);
+      v1 += __shfl_xor_sync(FULL, v1, o);
+    }
+    if (lane == 0) {
+      sm.lsize = v0;
+      sm.ltotal = v1;
+    }
+  }
+  __syncthreads();
+}
+
+// locate_min_outdeg_seg (reorder/reorder.h:767-797): most all-zero rows,
+// ties to the largest segment id.
+template <int M>
+__device__ void minseg_phase(RoundSmem<M>& sm, const NMJob& J) {
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  unsigned long long best = 0;
+  for (int s = tid; s < J.nseg; s += NM_THREADS) {
+    unsigned long long k = ((unsigned long long)(unsigned)J.zc[s] << 32) | (unsigned)s;
+    best = k > best ? k : best;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long t = __shfl_xor_sync(FULL, best, o);
+    best = t > best ? t : best;
+  }
+  if (lane == 0) sm.red64[w] = best;
+  __syncthreads();
+  if (w == 0) {
+    unsigned long long v = lane < RoundSmem<M>::NW ? sm.red64[lane] : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long t = __shfl_xor_sync(FULL, v, o);
+      v = t > v ? t : v;
+    }
+    if (lane == 0) sm.minseg = (int)(unsigned)(v & 0xffffffffu);
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ int seg_of_desc(unsigned long long k) { return (int)(0xffffffffu - (unsigned)k); }
+__device__ __forceinline__ int cnt_of_desc(unsigned long long k) { return (int)(k >> 32); }
+__device__ __forceinline__ int seg_of_rev(unsigned long long k) { return (int)(unsigned)k; }
+__device__ __forceinline__ int cnt_of_rev(unsigned long long k) { return 0x7fffffff - (int)(k >> 32); }
+
+// cmp (reorder/reorder.h:422-427) as "a comes out of the max-heap before b"
+__device__ __forceinline__ bool before_cmp(int sa, int ca, int sb, int cb) {
+  return ca != cb ? ca > cb : sa < sb;
+}
+// cmp_reverse (reorder/reorder.h:429-434)
+__device__ __forceinline__ bool before_rev(int sa, int ca, int sb, int cb) {
+  return ca != cb ? ca < cb : sa > sb;
+}
+
+// Which segments this round can touch (fact 2 above).
+template <int M>
+__device__ void choose_segments(RoundSmem<M>& sm, int sched) {
+  constexpr int K = M + 1;
+  if (threadIdx.x != 0) return;
+  const int L = sm.lsize;
+  int n = 0;
+  if (L == 1) {
+    int s0 = seg_of_desc(sm.top[0][0]);
+    sm.xseg[0] = s0;
+    sm.xcnt[0] = cnt_of_desc(sm.top[0][0]);
+    if (sm.minseg == s0) {
+      sm.mode = 2;
+      n = 1;
+    } else {
+      sm.mode = 1;
+      sm.xseg[1] = sm.minseg;
+      sm.xcnt[1] = 0;
+      n = 2;
+    }
+  } else {
+    sm.mode = 0;
+    const int lim = L < K ? L : K;
+    if (sched == 0 || sched == 2) {  // primary and targets follow one order
+      const int o = sched == 0 ? 0 : 1;
+      for (int q = 0; q < lim; ++q) {
+        unsigned long long k = sm.top[o][q];
+        sm.xseg[n] = o == 0 ? seg_of_desc(k) : seg_of_rev(k);
+        sm.xcnt[n] = o == 0 ? cnt_of_desc(k) : cnt_of_rev(k);
+        ++n;
+      }
+    } else {  // primary from one end, targets from the other
+      const int po = sched == 1 ? 0 : 1, to = 1 - po;
+      unsigned long long pk = sm.top[po][0];
+      const int ps = po == 0 ? seg_of_desc(pk) : seg_of_rev(pk);
+      sm.xseg[0] = ps;
+      sm.xcnt[0] = po == 0 ? cnt_of_desc(pk) : cnt_of_rev(pk);
+      n = 1;
+      for (int q = 0; q < K && n < lim; ++q) {
+        unsigned long long k = sm.top[to][q];
+        int s = to == 0 ? seg_of_desc(k) : seg_of_rev(k);
+        if (s == ps) continue;
+        sm.xseg[n] = s;
+        sm.xcnt[n] = to == 0 ? cnt_of_desc(k) : cnt_of_rev(k);
+        ++n;
+      }
+    }
+  }
+  sm.K_ = n;
+}
+
+template <int M>
+__device__ void clear_round_smem(RoundSmem<M>& sm) {
+  constexpr int K = M + 1;
+  for (int i = threadIdx.x; i < K * M; i += NM_THREADS) (&sm.S[0][0])[i] = 0;
+  for (int i = threadIdx.x; i < RoundSmem<M>::NPAIR * RoundSmem<M>::MM; i += NM_THREADS) {
+    (&sm.CL[0][0])[i] = 0;
+    (&sm.CR[0][0])[i] = 0;
+  }
+  if (threadIdx.x < K) {
+    sm.newinv[threadIdx.x] = 0;
+    sm.newpres[threadIdx.x] = 0;
+  }
+  if (threadIdx.x == 0) {
+    sm.ntouched = 0;
+    sm.nswaps = 0;
+  }
+}
+
+// OR the bitmaps of the round's segments into per-row records.
+template <int M>
+__device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J) {
+  const int tid = threadIdx.x;
+  const int KM = sm.K_ * M;
+  if (tid < KM) {
+    const int xi = tid / M, k = tid % M;
+    const int u = J.orig[sm.xseg[xi] * M + k];
+    const int b = J.cptr[u];
+    sm.colstart[tid] = b;
+    sm.colpre[tid + 1] = J.cptr[u + 1] - b;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    sm.colpre[0] = 0;
+    for (int q = 0; q < KM; ++q) sm.colpre[q + 1] += sm.colpre[q];
+    sm.E = sm.colpre[KM];
+  }
+  __syncthreads();
+  const int E = sm.E;
+  unsigned* recw = reinterpret_cast<unsigned*>(J.rec);
+  for (int e = tid; e < E; e += NM_THREADS) {
+    int lo = 0, hi = KM - 1;  // last q with colpre[q] <= e
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (sm.colpre[mid] <= e) lo = mid;
+      else hi = mid - 1;
+    }
+    const int q = lo, xi = q / M, k = q % M;
+    const int r = J.crow[sm.colstart[q] + (e - sm.colpre[q])];
+    atomicOr(&recw[4 * r + (xi >> 2)], (1u << k) << ((xi & 3) * 8));
+    if (atomicOr(&recw[4 * r + 3], 1u) == 0u) J.touched[atomicAdd(&sm.ntouched, 1)] = r;
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ unsigned rec_byte(const uint4& w, int xi) {
+  const unsigned word = xi < 4 ? w.x : (xi < 8 ? w.y : w.z);
+  return (word >> ((xi & 3) * 8)) & 0xffu;
+}
+
+// Solo terms and pair corrections (fact 3).
+template <int M>
+__device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N) {
+  constexpr int K = M + 1;
+  constexpr unsigned MASK = (1u << M) - 1u;
+  const int nt = sm.ntouched, Kn = sm.K_;
+  const bool self = sm.mode == 2;
+  for (int t = threadIdx.x; t < nt; t += NM_THREADS) {
+    const int r = J.touched[t];
+    const uint4 w = J.rec[r];
+    unsigned b[K];
+    int p[K];
+#pragma unroll
+    for (int xi = 0; xi < K; ++xi) {
+      b[xi] = xi < Kn ? rec_byte(w, xi) : 0u;
+      p[xi] = __popc(b[xi]);
+    }
+    if (self) {
+      // reference kernel lines 108-121 with lval == rval: direct per (i, j)
+      const unsigned L = b[0];
+      const int pl = p[0];
+      if (L == 0) continue;
+      for (int i = 0; i < M; ++i) {
+        const unsigned li = (L >> i) & 1u;
+        for (int j = 0; j < M; ++j) {
+          const unsigned lj = (L >> j) & 1u;
+          int l = (li && !lj && pl == N + 1) - (!li && lj && pl == N);
+          int rr = (lj && !li && pl == N + 1) - (!lj && li && pl == N);
+          if (l) atomicAdd(&sm.CL[0][i * M + j], l);
+          if (rr) atomicAdd(&sm.CR[0][i * M + j], rr);
+        }
+      }
+      continue;
+    }
+#pragma unroll
+    for (int xi = 0; xi < K; ++xi) {
+      if (p[xi] == N + 1) {
+        unsigned bb = b[xi];
+        while (bb) {
+          int k = __ffs(bb) - 1;
+          bb &= bb - 1;
+          atomicAdd(&sm.S[xi][k], 1);
+        }
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < K; ++a) {
+      if (!b[a]) continue;
+#pragma unroll
+      for (int c = a + 1; c < K; ++c) {
+        if (!b[c]) continue;
+        const unsigned L = b[a], Rb = b[c];
+        const int pid = pair_id<M>(a, c);
+        // left corrections: R_j = 1 and (L_i = 1, pL = N+1  or  L_i = 0, pL = N)
+        const unsigned li_set = p[a] == N + 1 ? L : (p[a] == N ? (~L & MASK) : 0u);
+        if (li_set) {
+          unsigned jj = Rb;
+          while (jj) {
+            const int j = __ffs(jj) - 1;
+            jj &= jj - 1;
+            unsigned ii = li_set;
+            while (ii) {
+              const int i = __ffs(ii) - 1;
+              ii &= ii - 1;
+              atomicAdd(&sm.CL[pid][i * M + j], 1);
+            }
+          }
+        }
+        // right corrections: L_i = 1 and (R_j = 1, pR = N+1  or  R_j = 0, pR = N)
+        const unsigned rj_set = p[c] == N + 1 ? Rb : (p[c] == N ? (~Rb & MASK) : 0u);
+        if (rj_set) {
+          unsigned ii = L;
+          while (ii) {
+            const int i = __ffs(ii) - 1;
+            ii &= ii - 1;
+            unsigned jj = rj_set;
+            while (jj) {
+              const int j = __ffs(jj) - 1;
+              jj &= jj - 1;
+              atomicAdd(&sm.CR[pid][i * M + j], 1);
+            }
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// Pop order of every ordered pair's swap heap (fact 4).
+template <int M>
+__device__ void heap_phase(RoundSmem<M>& sm) {
+  constexpr int K = M + 1, MM = M * M;
+  const int Kn = sm.K_;
+  const int t = threadIdx.x;
+  if (t < Kn * Kn) {
+    const int a = t / Kn, b = t % Kn;
+    if (a != b || sm.mode == 2) {
+      int64_t key[MM];
+      uint8_t heap[MM];
+      for (int idx = 0; idx < MM; ++idx) {
+        int l, r;
+        pair_gains<M>(sm, a, b, idx, l, r);
+        key[idx] = swap_key(l, r);
+      }
+      swap_heap_pop_order(MM, key, heap, sm.ord[a * K + b]);
+    }
+  }
+  __syncthreads();
+}
+
+// The greedy walk of run_onepair* over this round's segments (thread 0).
+template <int M>
+__device__ void walk_phase(RoundSmem<M>& sm, int sched) {
+  constexpr int K = M + 1, MM = M * M;
+  constexpr unsigned FULLM = (1u << M) - 1u;
+  if (threadIdx.x != 0) return;
+  unsigned vis[K];
+#pragma unroll
+  for (int q = 0; q < K; ++q) vis[q] = 0;
+  int nsw = 0;
+  auto commit = [&](int a, int b, int idx) {
+    const int i = idx / M, j = idx % M;
+    sm.swaps[2 * nsw] = sm.xseg[a] * M + i;
+    sm.swaps[2 * nsw + 1] = sm.xseg[b] * M + j;
+    ++nsw;
+    vis[a] |= 1u << i;
+    vis[b] |= 1u << j;
+  };
+  if (sm.mode != 0) {
+    // |L| == 1: best pair of (top, minseg) with no visited filter (:1837-1860)
+    const int b = sm.mode == 2 ? 0 : 1;
+    commit(0, b, sm.ord[0 * K + b][0]);
+  } else {
+    const bool rev_list = sched >= 2;                     // inv_seg_list / updatePQ comparator
+    const bool trav_rev = (sched == 1 || sched == 2);     // traversal comparator is cmp_reverse
+    int W[K], Wc[K];
+    int nW = sm.K_;
+    for (int q = 0; q < nW; ++q) {
+      W[q] = q;
+      Wc[q] = sm.xcnt[q];
+    }
+    while (nW >= 2) {
+      // primary = top of the list
+      int bp = 0;
+      for (int q = 1; q < nW; ++q) {
+        const int sa = sm.xseg[W[q]], sb = sm.xseg[W[bp]];
+        const bool bef = rev_list ? before_rev(sa, Wc[q], sb, Wc[bp]) : before_cmp(sa, Wc[q], sb, Wc[bp]);
+        if (bef) bp = q;
+      }
+      const int pxi = W[bp];
+      int pc = Wc[bp];
+      // targets: the rest, in traversal order (selection sort, <= M entries)
+      int T[K], Tc[K], nT = 0;
+      for (int q = 0; q < nW; ++q)
+        if (q != bp) {
+          T[nT] = W[q];
+          Tc[nT] = Wc[q];
+          ++nT;
+        }
+      for (int x = 0; x < nT; ++x) {
+        int best = x;
+        for (int y = x + 1; y < nT; ++y) {
+          const int sa = sm.xseg[T[y]], sb = sm.xseg[T[best]];
+          const bool bef = trav_rev ? before_rev(sa, Tc[y], sb, Tc[best]) : before_cmp(sa, Tc[y], sb, Tc[best]);
+          if (bef) best = y;
+        }
+        int t0 = T[x], t1 = Tc[x];
+        T[x] = T[best];
+        Tc[x] = Tc[best];
+        T[best] = t0;
+        Tc[best] = t1;
+      }
+      int nU = 0;
+      int U[K], Uc[K];
+      for (int x = 0; x < nT; ++x) {
+        if (pc <= 0 || vis[pxi] == FULLM) break;
+        const int txi = T[x];
+        int tc = Tc[x];
+        const uint8_t* ord = sm.ord[pxi * K + txi];
+        int pick = -1;
+        for (int k = 0; k < MM; ++k) {
+          const int idx = ord[k];
+          if (!((vis[pxi] >> (idx / M)) & 1u) && !((vis[txi] >> (idx % M)) & 1u)) {
+            pick = idx;
+            break;
+          }
+        }
+        if (pick < 0) {  // unreachable: a scored target always has an unvisited node
+          sm.status |= JOB_EMPTY_HEAP;
+          pick = ord[MM - 1];
+        }
+        int l, r;
+        pair_gains<M>(sm, pxi, txi, pick, l, r);
+        commit(pxi, txi, pick);
+        pc -= l;
+        tc -= r;
+        if (tc > 0) {
+          U[nU] = txi;
+          Uc[nU] = tc;
+          ++nU;
+        }
+      }
+      for (int q = 0; q < nU; ++q) {
+        W[q] = U[q];
+        Wc[q] = Uc[q];
+      }
+      nW = nU;
+    }
+  }
+  sm.nswaps = nsw;
+  // bit moves of the swaps for the recount (identity elsewhere)
+  for (int xi = 0; xi < K; ++xi)
+    for (int k = 0; k < M; ++k) sm.dest[xi][k] = (uint8_t)((xi << 4) | k);
+  for (int q = 0; q < nsw; ++q) {
+    const int v1 = sm.swaps[2 * q], v2 = sm.swaps[2 * q + 1];
+    int a = -1, b = -1;
+    for (int xi = 0; xi < sm.K_; ++xi) {
+      if (sm.xseg[xi] == v1 / M && a < 0) a = xi;
+      if (sm.xseg[xi] == v2 / M && b < 0) b = xi;
+    }
+    if (a < 0 || b < 0) {  // every swap lies in this round's segments
+      sm.status |= JOB_BAD_STATE;
+      continue;
+    }
+    sm.dest[a][v1 % M] = (uint8_t)((b << 4) | (v2 % M));
+    sm.dest[b][v2 % M] = (uint8_t)((a << 4) | (v1 % M));
+  }
+}
+
+// Apply the swaps to orig[] and recount the touched segments.
+template <int M>
+__device__ void apply_phase(RoundSmem<M>& sm, const NMJob& J, int N, int round) {
+  constexpr int K = M + 1;
+  const int tid = threadIdx.x;
+  (void)round;
+  if (tid == 0) {
+    for (int q = 0; q < sm.nswaps; ++q) {
+      const int v1 = sm.swaps[2 * q], v2 = sm.swaps[2 * q + 1];
+      const int o1 = J.orig[v1], o2 = J.orig[v2];
+      J.orig[v1] = o2;
+      J.orig[v2] = o1;
+    }
+  }
+  const int nt = sm.ntouched, Kn = sm.K_;
+  for (int t = tid; t < nt; t += NM_THREADS) {
+    const int r = J.touched[t];
+    const uint4 w = J.rec[r];
+    unsigned nb[K];
+#pragma unroll
+    for (int xi = 0; xi < K; ++xi) nb[xi] = 0;
+#pragma unroll
+    for (int xi = 0; xi < K; ++xi) {
+      if (xi >= Kn) break;
+      unsigned bb = rec_byte(w, xi);
+      while (bb) {
+        const int k = __ffs(bb) - 1;
+        bb &= bb - 1;
+        const int d = sm.dest[xi][k];
+        const int dx = d >> 4, dk = d & 15;
+#pragma unroll
+        for (int z = 0; z < K; ++z)
+          if (z == dx) nb[z] |= 1u << dk;
+      }
+    }
+#pragma unroll
+    for (int xi = 0; xi < K; ++xi) {
+      if (xi < Kn && nb[xi]) {
+        atomicAdd(&sm.newpres[xi], 1);
+        if (__popc(nb[xi]) > N) atomicAdd(&sm.newinv[xi], 1);
+      }
+    }
+    J.rec[r] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  __syncthreads();
+  if (tid < Kn) {
+    J.cnt[sm.xseg[tid]] = sm.newinv[tid];
+    J.zc[sm.xseg[tid]] = J.R - sm.newpres[tid];
+  }
+  __syncthreads();
+}
+
+template <int M>
+__global__ void __launch_bounds__(NM_THREADS) k_nm_rounds(const NMJob* __restrict__ jobs, int N) {
+  __shared__ RoundSmem<M> sm;
+  const NMJob J = jobs[blockIdx.x];
+  const int tid = threadIdx.x;
+  if (tid == 0) sm.status = JOB_OK;
+  clear_round_smem<M>(sm);
+  __syncthreads();
+  select_phase<M>(sm, J);
+  const int init_size = sm.lsize, init_cnt = sm.ltotal;
+  const int MAXITER = J.maxiter > init_size ? J.maxiter : init_size;  // reorder.h:1819
+  int round = 1;
+  int committed = 0;
+  unsigned long long sumE = 0, sumT = 0;
+  while (round <= MAXITER && sm.lsize >= 1) {
+    if (sm.lsize == 1) minseg_phase<M>(sm, J);
+    choose_segments<M>(sm, J.sched);
+    __syncthreads();
+    gather_phase<M>(sm, J);
+    process_phase<M>(sm, J, N);
+    heap_phase<M>(sm);
+    walk_phase<M>(sm, J.sched);
+    __syncthreads();
+    if (tid == 0 && J.trace_pairs) {
+      for (int q = 0; q < sm.nswaps; ++q) {
+        if (committed < J.trace_cap_pairs) {
+          J.trace_pairs[2 * committed] = sm.swaps[2 * q];
+          J.trace_pairs[2 * committed + 1] = sm.swaps[2 * q + 1];
+        }
+        ++committed;
+      }
+      if (round - 1 < J.trace_cap_rounds) J.trace_rounds[round - 1] = committed;
+    }
+    sumE += (unsigned)sm.E;
+    sumT += (unsigned)sm.ntouched;
+    apply_phase<M>(sm, J, N, round);
+    clear_round_smem<M>(sm);
+    __syncthreads();
+    select_phase<M>(sm, J);
+    round += 1;
+    if (sm.status != JOB_OK) break;
+  }
+  if (tid == 0) {
+    J.res[0] = init_size;
+    J.res[1] = sm.lsize;
+    J.res[2] = init_cnt;
+    J.res[3] = sm.ltotal;
+    J.res[4] = round - 1;
+    J.res[5] = sm.status;
+    J.res[6] = committed;
+    J.res[7] = (int)(sumE & 0x7fffffffull);
+    J.res[8] = (int)(sumE >> 31);
+    J.res[9] = (int)(sumT & 0x7fffffffull);
+    J.res[10] = (int)(sumT >> 31);
+  }
+}
+
+// One segment pair's full gain table (GetSegSwapScore) through the same
+// phases the round kernel uses; orig is the identity here.
+template <int M>
+__global__ void __launch_bounds__(NM_THREADS) k_pair_score(NMJob J, int N, int s1, int s2, int* score) {
+  __shared__ RoundSmem<M> sm;
+  clear_round_smem<M>(sm);
+  if (threadIdx.x == 0) {
+    sm.xseg[0] = s1;
+    sm.xcnt[0] = 0;
+    if (s1 == s2) {
+      sm.mode = 2;
+      sm.K_ = 1;
+    } else {
+      sm.mode = 1;
+      sm.xseg[1] = s2;
+      sm.xcnt[1] = 0;
+      sm.K_ = 2;
+    }
+  }
+  __syncthreads();
+  gather_phase<M>(sm, J);
+  process_phase<M>(sm, J, N);
+  const int b = s1 == s2 ? 0 : 1;
+  for (int idx = threadIdx.x; idx < M * M; idx += NM_THREADS) {
+    int l, r;
+    pair_gains<M>(sm, 0, b, idx, l, r);
+    score[2 * idx] = l;
+    score[2 * idx + 1] = r;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < sm.ntouched; t += NM_THREADS) J.rec[J.touched[t]] = make_uint4(0u, 0u, 0u, 0u);
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+struct Pattern {  // the nonzero-valued pattern of one matrix on the device
+  int R = 0, nseg = 0, np = 0;
+  int* prow = nullptr;
+  int* pcol = nullptr;
+  int* cptr = nullptr;
+  int* crow = nullptr;
+  int* inv0 = nullptr;
+  int* pres0 = nullptr;
+};
+
+static inline int grid_for(const vnm_ctx* ctx, long long n, int nt = 256) {
+  long long g = (n + nt - 1) / nt;
+  long long cap = (long long)ctx->num_sms * 8;
+  if (g > cap) g = cap;
+  return g < 1 ? 1 : (int)g;
+}
+
+size_t pattern_bytes(int R, int nnz) {
+  size_t b = 0;
+  b += arena_bytes(1, sizeof(int));              // error word
+  b += arena_bytes(nnz, sizeof(int));            // flags / positions
+  b += 2 * arena_bytes(nnz, sizeof(int));        // prow, pcol
+  b += arena_bytes(R + 1, sizeof(int)) * 2;      // coldeg->cptr, cfill
+  b += arena_bytes(nnz, sizeof(int));            // crow
+  b += 2 * arena_bytes(R / 2 + 1, sizeof(int));  // inv0, pres0 (nseg <= R/2)
+  b += arena_bytes(1, sizeof(int)) * 2;          // totals
+  b += scan_scratch_bytes(nnz > R + 1 ? nnz : R + 1) * 2;
+  return b;
+}
+
+template <int M>
+static vnm_status build_pattern_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, const int* d_col,
+                                  const float* d_val, int N, Pattern& P, int* h_scratch) {
+  P.R = R;
+  P.nseg = R / M;
+  int* err = arena_take<int>(ctx, 1);
+  int* pos = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
+  P.prow = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
+  P.pcol = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
+  P.cptr = arena_take<int>(ctx, R + 1);
+  int* cfill = arena_take<int>(ctx, R + 1);
+  P.crow = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
+  P.inv0 = arena_take<int>(ctx, R / 2 + 1);
+  P.pres0 = arena_take<int>(ctx, R / 2 + 1);
+  int* d_np = arena_take<int>(ctx, 1);
+  int* d_tot = arena_take<int>(ctx, 1);
+  if (!err || !pos || !P.prow || !P.pcol || !P.cptr || !cfill || !P.crow || !P.inv0 || !P.pres0 || !d_np ||
+      !d_tot)
+    return VNM_ERR_NOMEM;
+  VNM_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  VNM_CUDA_TRY(cudaMemsetAsync(P.cptr, 0, sizeof(int) * (R + 1), ctx->stream));
+  VNM_CUDA_TRY(cudaMemsetAsync(cfill, 0, sizeof(int) * (R + 1), ctx->stream));
+  VNM_CUDA_TRY(cudaMemsetAsync(P.inv0, 0, sizeof(int) * (P.nseg + 1), ctx->stream));
+  VNM_CUDA_TRY(cudaMemsetAsync(P.pres0, 0, sizeof(int) * (P.nseg + 1), ctx->stream));
+  if (nnz > 0) {
+    // indices are checked before any kernel uses them as addresses
+    VNM_LAUNCH(ctx, k_validate, grid_for(ctx, nnz), 256, 0, d_row, d_col, nnz, R, err);
+    VNM_CUDA_TRY(cudaMemcpyAsync(h_scratch, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    VNM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    if (h_scratch[0] & 2) return VNM_ERR_RANGE;
+    if (h_scratch[0] & 1) return VNM_ERR_UNSORTED;
+    VNM_LAUNCH(ctx, k_nonzero_flags, grid_for(ctx, nnz), 256, 0, d_val, nnz, pos);
+    VNM_TRY(exclusive_scan(ctx, pos, pos, nnz, d_np));
+    VNM_LAUNCH(ctx, k_compact, grid_for(ctx, nnz), 256, 0, d_row, d_col, d_val, pos, nnz, P.prow, P.pcol, P.cptr);
+  } else {
+    VNM_CUDA_TRY(cudaMemsetAsync(d_np, 0, sizeof(int), ctx->stream));
+  }
+  VNM_TRY(exclusive_scan(ctx, P.cptr, P.cptr, R + 1, d_tot));
+  VNM_CUDA_TRY(cudaMemcpyAsync(h_scratch + 1, d_np, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  VNM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  P.np = h_scratch[1];
+  if (P.np > 0) {
+    VNM_LAUNCH(ctx, k_csc_scatter, grid_for(ctx, P.np), 256, 0, P.prow, P.pcol, P.np, P.cptr, cfill, P.crow);
+    VNM_LAUNCH(ctx, k_locate<M>, grid_for(ctx, P.np), 256, 0, P.prow, P.pcol, P.np, N, P.inv0, P.pres0);
+  }
+  return VNM_OK;
+}
+
+static vnm_status build_pattern(vnm_ctx* ctx, int R, int nnz, const int* d_row, const int* d_col,
+                                const float* d_val, int N, int M, Pattern& P, int* h_scratch) {
+  switch (M) {
+    case 2: return build_pattern_t<2>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch);
+    case 3: return build_pattern_t<3>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch);
+    case 4: return build_pattern_t<4>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch);
+    case 5: return build_pattern_t<5>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch);
+    case 6: return build_pattern_t<6>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch);
+    case 7: return build_pattern_t<7>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch);
+    case 8: return build_pattern_t<8>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch);
+  }
+  return VNM_ERR_ARG;
+}
+
+size_t job_bytes(int R) {
+  const int nseg = R / 2 + 1;
+  return arena_bytes(R, sizeof(int)) + 2 * arena_bytes(nseg, sizeof(int)) + arena_bytes(R, sizeof(uint4)) +
+         arena_bytes(R, sizeof(int)) + arena_bytes(16, sizeof(int));
+}
+
+// Carve one job's state out of the arena and initialise it.
+static vnm_status make_job(vnm_ctx* ctx, const Pattern& P, int sched, int maxiter, NMJob& J) {
+  J.R = P.R;
+  J.nseg = P.nseg;
+  J.sched = sched;
+  J.maxiter = maxiter;
+  J.cptr = P.cptr;
+  J.crow = P.crow;
+  J.orig = arena_take<int>(ctx, P.R > 0 ? P.R : 1);
+  J.cnt = arena_take<int>(ctx, P.nseg + 1);
+  J.zc = arena_take<int>(ctx, P.nseg + 1);
+  J.rec = arena_take<uint4>(ctx, P.R > 0 ? P.R : 1);
+  J.touched = arena_take<int>(ctx, P.R > 0 ? P.R : 1);
+  J.res = arena_take<int>(ctx, 16);
+  J.trace_pairs = nullptr;
+  J.trace_rounds = nullptr;
+  J.trace_cap_pairs = 0;
+  J.trace_cap_rounds = 0;
+  if (!J.orig || !J.cnt || !J.zc || !J.rec || !J.touched || !J.res) return VNM_ERR_NOMEM;
+  VNM_CUDA_TRY(cudaMemsetAsync(J.rec, 0, sizeof(uint4) * (P.R > 0 ? P.R : 1), ctx->stream));
+  VNM_CUDA_TRY(cudaMemsetAsync(J.res, 0, sizeof(int) * 16, ctx->stream));
+  if (P.R > 0)
+    VNM_LAUNCH(ctx, k_init_job, grid_for(ctx, P.R), 256, 0, J.orig, J.cnt, J.zc, P.inv0, P.pres0, P.R, P.nseg);
+  return VNM_OK;
+}
+
+template <int M>
+static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, int N) {
+  VNM_LAUNCH(ctx, k_nm_rounds<M>, njobs, NM_THREADS, 0, d_jobs, N);
+  return VNM_OK;
+}
+
+static vnm_status launch_rounds(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, int N, int M) {
+  switch (M) {
+    case 2: return launch_rounds_t<2>(ctx, d_jobs, njobs, N);
+    case 3: return launch_rounds_t<3>(ctx, d_jobs, njobs, N);
+    case 4: return launch_rounds_t<4>(ctx, d_jobs, njobs, N);
+    case 5: return launch_rounds_t<5>(ctx, d_jobs, njobs, N);
+    case 6: return launch_rounds_t<6>(ctx, d_jobs, njobs, N);
+    case 7: return launch_rounds_t<7>(ctx, d_jobs, njobs, N);
+    case 8: return launch_rounds_t<8>(ctx, d_jobs, njobs, N);
+  }
+  return VNM_ERR_ARG;
+}
+
+static vnm_status check_nm_args(int nrows, int nnz, const int* row, const int* col, const float* val, int mem, int N,
+                                int M) {
+  if (M < 2 || M > 8 || N < 1 || N >= M) return VNM_ERR_ARG;
+  if (nrows < 0 || nnz < 0 || (nrows % M) != 0) return VNM_ERR_ARG;
+  if (mem != VNM_MEM_HOST && mem != VNM_MEM_DEVICE) return VNM_ERR_ARG;
+  if (nnz > 0 && (!row || !col || !val)) return VNM_ERR_ARG;
+  if (nrows > (1 << 28)) return VNM_ERR_LIMIT;
+  return VNM_OK;
+}
+
+// find_best_2toX's choice (main.cu:80-113) from the four result vectors:
+// largest improve rate, ties to the lower schedule id; 0 when the matrix is
+// empty or has no invalid segment (main.cu:85).
+static int pick_best(const int* res, int nsched, int nnz) {
+  float max_imprv = 0.0f;
+  int best = 0;
+  for (int s = 0; s < nsched; ++s) {
+    const int* r = res + 5 * s;
+    if (nnz == 0 || r[0] == 0) return 0;
+    const float imp = (r[2] != 0) ? ((r[2] - r[3]) * 1.0f / r[2]) : 0;
+    if (imp > max_imprv) {
+      max_imprv = imp;
+      best = s;
+    }
+  }
+  return best;
+}
+
+// Run `nsched` jobs on one matrix (schedules sched0 .. sched0+nsched-1).
+// newpos_job >= 0 selects the job whose permutation goes to newpos_out;
+// -1 selects the find_best_2toX winner (reported in *picked).
+static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, const int* col, const float* val,
+                             int mem, int N, int M, int sched0, int nsched, int maxiter, int* res5_out,
+                             int* newpos_out, int newpos_job, bool trace, int* picked = nullptr) {
+  const int R = nrows;
+  const int trace_pairs_cap = trace ? 2 * (M + 1) * M * 4096 : 0;
+  const int trace_rounds_cap = trace ? 65536 : 0;
+  size_t need = pattern_bytes(R, nnz) + (size_t)nsched * job_bytes(R) + arena_bytes(nsched, sizeof(NMJob)) +
+                arena_bytes(R, sizeof(int)) + 3 * arena_bytes(nnz, sizeof(int)) +
+                arena_bytes(trace_pairs_cap * 2, sizeof(int)) + arena_bytes(trace_rounds_cap, sizeof(int)) + 4096;
+  VNM_TRY(arena_reserve(ctx, need));
+  VNM_TRY(pinned_reserve(ctx, 64 + (size_t)trace_pairs_cap * 2 + trace_rounds_cap));
+  VNM_TRY(begin_call(ctx));
+  const int *d_row, *d_col;
+  const float* d_val;
+  VNM_TRY(stage_in(ctx, row, nnz, mem, &d_row));
+  VNM_TRY(stage_in(ctx, col, nnz, mem, &d_col));
+  VNM_TRY(stage_in(ctx, val, nnz, mem, &d_val));
+  Pattern P;
+  VNM_TRY(build_pattern(ctx, R, nnz, d_row, d_col, d_val, N, M, P, ctx->h_pinned));
+  NMJob hj[4];
+  for (int s = 0; s < nsched; ++s) VNM_TRY(make_job(ctx, P, sched0 + s, maxiter, hj[s]));
+  int* d_tp = nullptr;
+  int* d_tr = nullptr;
+  if (trace) {
+    d_tp = arena_take<int>(ctx, trace_pairs_cap * 2);
+    d_tr = arena_take<int>(ctx, trace_rounds_cap);
+    if (!d_tp || !d_tr) return VNM_ERR_NOMEM;
+    hj[0].trace_pairs = d_tp;
+    hj[0].trace_rounds = d_tr;
+    hj[0].trace_cap_pairs = trace_pairs_cap;
+    hj[0].trace_cap_rounds = trace_rounds_cap;
+  }
+  NMJob* d_jobs = arena_take<NMJob>(ctx, nsched);
+  if (!d_jobs) return VNM_ERR_NOMEM;
+  VNM_CUDA_TRY(cudaMemcpyAsync(d_jobs, hj, sizeof(NMJob) * nsched, cudaMemcpyHostToDevice, ctx->stream));
+  VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main0, ctx->stream));
+  VNM_TRY(launch_rounds(ctx, d_jobs, nsched, N, M));
+  VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main1, ctx->stream));
+  int* hres = ctx->h_pinned;
+  for (int s = 0; s < nsched; ++s)
+    VNM_CUDA_TRY(cudaMemcpyAsync(hres + 16 * s, hj[s].res, sizeof(int) * 16, cudaMemcpyDeviceToHost, ctx->stream));
+  VNM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  VNM_CUDA_TRY(cudaEventElapsedTime(&ctx->main_ms, ctx->ev_main0, ctx->ev_main1));
+  int hres_copy[64];
+  memcpy(hres_copy, hres, sizeof(int) * 16 * nsched);
+  for (int q = 0; q < 8; ++q) ctx->stats[q] = 0;
+  ctx->stats[3] = P.nseg;
+  ctx->stats[4] = nsched;
+  ctx->stats[5] = P.np;
+  for (int s = 0; s < nsched; ++s) {
+    const int* h = hres_copy + 16 * s;
+    if (h[5] != 0) return VNM_ERR_INTERNAL;
+    for (int q = 0; q < 5; ++q) res5_out[5 * s + q] = h[q];
+    ctx->stats[0] += h[4];
+    ctx->stats[1] += (long long)h[7] + ((long long)h[8] << 31);
+    ctx->stats[2] += (long long)h[9] + ((long long)h[10] << 31);
+  }
+  if (trace) {
+    const int committed = hres_copy[6];
+    const int rounds = hres_copy[4];
+    const int np = committed < trace_pairs_cap ? committed : trace_pairs_cap;
+    const int nr = rounds < trace_rounds_cap ? rounds : trace_rounds_cap;
+    int* hp = ctx->h_pinned + 64;
+    if (np) VNM_CUDA_TRY(cudaMemcpyAsync(hp, d_tp, sizeof(int) * 2 * np, cudaMemcpyDeviceToHost, ctx->stream));
+    if (nr)
+      VNM_CUDA_TRY(cudaMemcpyAsync(hp + 2 * np, d_tr, sizeof(int) * nr, cudaMemcpyDeviceToHost, ctx->stream));
+    VNM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    ctx->trace_pairs.assign(hp, hp + 2 * np);
+    ctx->trace_round_end.assign(hp + 2 * np, hp + 2 * np + nr);
+  }
+  if (newpos_job < 0) newpos_job = pick_best(res5_out, nsched, nnz);
+  if (picked) *picked = newpos_job;
+  if (newpos_out && R > 0) {
+    int* d_np = arena_take<int>(ctx, R);
+    if (!d_np) return VNM_ERR_NOMEM;
+    VNM_LAUNCH(ctx, k_invert, grid_for(ctx, R), 256, 0, hj[newpos_job].orig, R, d_np);
+    VNM_CUDA_TRY(cudaMemcpyAsync(newpos_out, d_np, sizeof(int) * R, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  VNM_TRY(end_call(ctx));
+  return VNM_OK;
+}
+
+}  // namespace vnm
+
+using namespace vnm;
+
+extern "C" {
+
+vnm_status vnm_nm_reorder(vnm_ctx* ctx, int nrows, int nnz, const int* row, const int* col, const float* val,
+                          int mem, int N, int M, int sched, int nm_maxiter, int* res5, int* newpos) {
+  if (!ctx || !res5) return VNM_ERR_ARG;
+  VNM_TRY(check_nm_args(nrows, nnz, row, col, val, mem, N, M));
+  if (sched < 0 || sched > 3) return VNM_ERR_ARG;
+  return run_matrix(ctx, nrows, nnz, row, col, val, mem, N, M, sched, 1, nm_maxiter, res5, newpos, 0, ctx->trace);
+}
+
+vnm_status vnm_nm_search(vnm_ctx* ctx, int nrows, int nnz, const int* row, const int* col, const float* val,
+                         int mem, int N, int M, int nm_maxiter, int* best_sched, int* res5x4, int* newpos_best) {
+  if (!ctx || !best_sched) return VNM_ERR_ARG;
+  VNM_TRY(check_nm_args(nrows, nnz, row, col, val, mem, N, M));
+  int res[20];
+  // the four schedules run as four blocks of one launch; the winner's final
+  // arrangement is already on the device, so its permutation is read back
+  // without a second run
+  VNM_TRY(run_matrix(ctx, nrows, nnz, row, col, val, mem, N, M, 0, 4, nm_maxiter, res, newpos_best, -1, false,
+                     best_sched));
+  if (res5x4) memcpy(res5x4, res, sizeof res);
+  return VNM_OK;
+}
+
+vnm_status vnm_nm_set_trace(vnm_ctx* ctx, int enable) {
+  if (!ctx) return VNM_ERR_ARG;
+  ctx->trace = enable != 0;
+  return VNM_OK;
+}
+
+vnm_status vnm_nm_get_trace(vnm_ctx* ctx, int* pairs, int cap_pairs, int* npairs, int* round_end, int cap_rounds,
+                            int* nrounds) {
+  if (!ctx || !npairs || !nrounds) return VNM_ERR_ARG;
+  const int np = (int)ctx->trace_pairs.size() / 2, nr = (int)ctx->trace_round_end.size();
+  *npairs = np;
+  *nrounds = nr;
+  if (pairs)
+    for (int i = 0; i < 2 * np && i < 2 * cap_pairs; ++i) pairs[i] = ctx->trace_pairs[i];
+  if (round_end)
+    for (int i = 0; i < nr && i < cap_rounds; ++i) round_end[i] = ctx->trace_round_end[i];
+  return VNM_OK;
+}
+
+vnm_status vnm_permute_coo(vnm_ctx* ctx, int nrows, int nnz, int* row, int* col, int mem, const int* newpos) {
+  if (!ctx || nrows < 0 || nnz < 0 || !newpos || (nnz > 0 && (!row || !col))) return VNM_ERR_ARG;
+  if (mem != VNM_MEM_HOST && mem != VNM_MEM_DEVICE) return VNM_ERR_ARG;
+  VNM_TRY(arena_reserve(ctx, 3 * arena_bytes(nnz, sizeof(int)) + arena_bytes(nrows, sizeof(int)) + 1024));
+  VNM_TRY(begin_call(ctx));
+  int *d_row = row, *d_col = col;
+  const int* d_np = newpos;
+  if (mem == VNM_MEM_HOST) {
+    d_row = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
+    d_col = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
+    int* t = arena_take<int>(ctx, nrows > 0 ? nrows : 1);
+    if (!d_row || !d_col || !t) return VNM_ERR_NOMEM;
+    if (nnz) {
+      VNM_CUDA_TRY(cudaMemcpyAsync(d_row, row, sizeof(int) * nnz, cudaMemcpyHostToDevice, ctx->stream));
+      VNM_CUDA_TRY(cudaMemcpyAsync(d_col, col, sizeof(int) * nnz, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    if (nrows) VNM_CUDA_TRY(cudaMemcpyAsync(t, newpos, sizeof(int) * nrows, cudaMemcpyHostToDevice, ctx->stream));
+    d_np = t;
+  }
+  if (nnz) VNM_LAUNCH(ctx, k_permute, grid_for(ctx, nnz), 256, 0, d_row, d_col, nnz, d_np);
+  if (mem == VNM_MEM_HOST && nnz) {
+    VNM_CUDA_TRY(cudaMemcpyAsync(row, d_row, sizeof(int) * nnz, cudaMemcpyDeviceToHost, ctx->stream));
+    VNM_CUDA_TRY(cudaMemcpyAsync(col, d_col, sizeof(int) * nnz, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  return end_call(ctx);
+}
+
+vnm_status vnm_nm_segment_counts(vnm_ctx* ctx, int nrows, int nnz, const int* row, const int* col,
+                                 const float* val, int mem, int N, int M, int* invalid, int* allzero) {
+  if (!ctx || !invalid || !allzero) return VNM_ERR_ARG;
+  VNM_TRY(check_nm_args(nrows, nnz, row, col, val, mem, N, M));
+  VNM_TRY(arena_reserve(ctx, pattern_bytes(nrows, nnz) + 3 * arena_bytes(nnz, sizeof(int)) + 4096));
+  VNM_TRY(pinned_reserve(ctx, 64));
+  VNM_TRY(begin_call(ctx));
+  const int *d_row, *d_col;
+  const float* d_val;
+  VNM_TRY(stage_in(ctx, row, nnz, mem, &d_row));
+  VNM_TRY(stage_in(ctx, col, nnz, mem, &d_col));
+  VNM_TRY(stage_in(ctx, val, nnz, mem, &d_val));
+  Pattern P;
+  VNM_TRY(build_pattern(ctx, nrows, nnz, d_row, d_col, d_val, N, M, P, ctx->h_pinned));
+  const int nseg = nrows / M;
+  if (nseg) {
+    VNM_CUDA_TRY(cudaMemcpyAsync(invalid, P.inv0, sizeof(int) * nseg, cudaMemcpyDeviceToHost, ctx->stream));
+    VNM_CUDA_TRY(cudaMemcpyAsync(allzero, P.pres0, sizeof(int) * nseg, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  VNM_TRY(end_call(ctx));
+  for (int s = 0; s < nseg; ++s) allzero[s] = nrows - allzero[s];
+  return VNM_OK;
+}
+
+vnm_status vnm_nm_pair_score(vnm_ctx* ctx, int nrows, int nnz, const int* row, const int* col, const float* val,
+                             int mem, int N, int M, int seg1, int seg2, int* score) {
+  if (!ctx || !score) return VNM_ERR_ARG;
+  VNM_TRY(check_nm_args(nrows, nnz, row, col, val, mem, N, M));
+  const int nseg = nrows / M;
+  if (seg1 < 0 || seg2 < 0 || seg1 >= nseg || seg2 >= nseg) return VNM_ERR_ARG;
+  VNM_TRY(arena_reserve(ctx, pattern_bytes(nrows, nnz) + job_bytes(nrows) + 3 * arena_bytes(nnz, sizeof(int)) +
+                                 arena_bytes(2 * M * M, sizeof(int)) + 4096));
+  VNM_TRY(pinned_reserve(ctx, 64));
+  VNM_TRY(begin_call(ctx));
+  const int *d_row, *d_col;
+  const float* d_val;
+  VNM_TRY(stage_in(ctx, row, nnz, mem, &d_row));
+  VNM_TRY(stage_in(ctx, col, nnz, mem, &d_col));
+  VNM_TRY(stage_in(ctx, val, nnz, mem, &d_val));
+  Pattern P;
+  VNM_TRY(build_pattern(ctx, nrows, nnz, d_row, d_col, d_val, N, M, P, ctx->h_pinned));
+  NMJob J;
+  VNM_TRY(make_job(ctx, P, 0, 10, J));
+  int* d_score = arena_take<int>(ctx, 2 * M * M);
+  if (!d_score) return VNM_ERR_NOMEM;
+  switch (M) {
+#define VNM_PS(MM)                                                                          \
+  case MM:                                                                                  \
+    VNM_LAUNCH(ctx, k_pair_score<MM>, 1, NM_THREADS, 0, J, N, seg1, seg2, d_score);         \
+    break;
+    VNM_PS(2) VNM_PS(3) VNM_PS(4) VNM_PS(5) VNM_PS(6) VNM_PS(7) VNM_PS(8)
+#undef VNM_PS
+  }
+  VNM_CUDA_TRY(cudaMemcpyAsync(score, d_score, sizeof(int) * 2 * M * M, cudaMemcpyDeviceToHost, ctx->stream));
+  return end_call(ctx);
+}
+
+vnm_status vnm_nm_reorder_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int64_t* nnz_offset,
+                                const int* row, const int* col, const float* val, int N, int M, int sched,
+                                int nm_maxiter, int* res5, int* newpos) {
+  (void)ctx; (void)nmat; (void)nrows; (void)nnz_offset; (void)row; (void)col; (void)val; (void)N; (void)M;
+  (void)sched; (void)nm_maxiter; (void)res5; (void)newpos;
+  return VNM_ERR_ARG;  // filled in by batch.cu
+}
+
+}  // extern "C"

@@ -1,0 +1,234 @@
+"""Python binding of libvnm_gb300 (ctypes over the C ABI in include/vnm_gb300.h).
+
+This module is a thin host-side mirror of the library's C entry points; all
+work happens in the CUDA library.  It refuses to run without the library:
+there is no CPU fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG, "libvnm_gb300.so")
+
+MEM_HOST = 0
+MEM_DEVICE = 1
+
+_i32p = ctypes.POINTER(ctypes.c_int)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_f32p = ctypes.POINTER(ctypes.c_float)
+_vp = ctypes.c_void_p
+
+
+class VnmError(RuntimeError):
+    def __init__(self, status, what):
+        self.status = status
+        super().__init__("%s failed: %s (status %d)" % (what, status_string(status), status))
+
+
+_lib = None
+
+
+def build():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("vnm_gb300_build", os.path.join(PKG, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build()
+
+
+def lib():
+    """Load libvnm_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libvnm_gb300.so is missing at %s: build it first (python __graft_entry__.py build "
+                           "or vnm-graph-reordering_gb300/build.py)" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    L.vnm_status_string.restype = ctypes.c_char_p
+    L.vnm_status_string.argtypes = [ctypes.c_int]
+    L.vnm_version.restype = ctypes.c_char_p
+    L.vnm_create.argtypes = [ctypes.POINTER(_vp), ctypes.c_int]
+    L.vnm_destroy.argtypes = [_vp]
+    L.vnm_last_kernel_ms.argtypes = [_vp]
+    L.vnm_last_kernel_ms.restype = ctypes.c_float
+    L.vnm_last_launch_count.argtypes = [_vp]
+    L.vnm_last_main_kernel_ms.argtypes = [_vp]
+    L.vnm_last_main_kernel_ms.restype = ctypes.c_float
+    L.vnm_last_stats.argtypes = [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]
+    L.vnm_nm_reorder.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                                 ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p, _i32p]
+    L.vnm_nm_search.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                                ctypes.c_int, ctypes.c_int, _i32p, _i32p, _i32p]
+    L.vnm_nm_reorder_batch.argtypes = [_vp, ctypes.c_int, _i32p, _i64p, _i32p, _i32p, _f32p, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p, _i32p]
+    L.vnm_nm_set_trace.argtypes = [_vp, ctypes.c_int]
+    L.vnm_nm_get_trace.argtypes = [_vp, _i32p, ctypes.c_int, _i32p, _i32p, ctypes.c_int, _i32p]
+    L.vnm_permute_coo.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, ctypes.c_int, _vp]
+    L.vnm_nm_segment_counts.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, _i32p, _i32p]
+    L.vnm_nm_pair_score.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p]
+    L.vnm_swap_heap_order.argtypes = [ctypes.c_int, _i32p, _i32p, _i32p]
+    _lib = L
+    return L
+
+
+def status_string(s):
+    return lib().vnm_status_string(int(s)).decode()
+
+
+def version():
+    return lib().vnm_version().decode()
+
+
+def _check(st, what):
+    if st != 0:
+        raise VnmError(st, what)
+
+
+def _ptr(a, dtype):
+    if a is None:
+        return None
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def _host(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+def swap_heap_order(lg, rg):
+    lg = _host(lg, np.int32)
+    rg = _host(rg, np.int32)
+    out = np.zeros(len(lg), np.int32)
+    _check(lib().vnm_swap_heap_order(len(lg), lg.ctypes.data_as(_i32p), rg.ctypes.data_as(_i32p),
+                                     out.ctypes.data_as(_i32p)), "vnm_swap_heap_order")
+    return out
+
+
+class Context:
+    """One CUDA context handle (own stream and scratch) of the library."""
+
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        _check(lib().vnm_create(ctypes.byref(h), int(device)), "vnm_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().vnm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def last_kernel_ms(self):
+        return lib().vnm_last_kernel_ms(self.h)
+
+    @property
+    def last_launch_count(self):
+        return lib().vnm_last_launch_count(self.h)
+
+    @property
+    def last_main_kernel_ms(self):
+        return lib().vnm_last_main_kernel_ms(self.h)
+
+    def last_stats(self):
+        out = (ctypes.c_longlong * 8)()
+        _check(lib().vnm_last_stats(self.h, out, 8), "vnm_last_stats")
+        keys = ("rounds", "gathered", "touched", "nseg", "jobs", "pattern_nnz")
+        return dict(zip(keys, list(out)[:6]))
+
+    # ---- array plumbing: numpy arrays (host) or torch CUDA tensors (device)
+    @staticmethod
+    def _arrays(row, col, val):
+        if hasattr(row, "is_cuda") and row.is_cuda:
+            import torch
+            assert row.dtype == torch.int32 and col.dtype == torch.int32 and val.dtype == torch.float32
+            return (ctypes.c_void_p(row.data_ptr()), ctypes.c_void_p(col.data_ptr()),
+                    ctypes.c_void_p(val.data_ptr()), MEM_DEVICE, int(row.numel()), (row, col, val))
+        r = _host(row, np.int32)
+        c = _host(col, np.int32)
+        v = _host(val, np.float32)
+        return _ptr(r, np.int32), _ptr(c, np.int32), _ptr(v, np.float32), MEM_HOST, len(r), (r, c, v)
+
+    def nm_reorder(self, nrows, row, col, val, N, M, sched, nm_maxiter=10, want_newpos=True):
+        """One NM job; returns (res5, newpos or None)."""
+        pr, pc, pv, mem, nnz, keep = self._arrays(row, col, val)
+        res = np.zeros(5, np.int32)
+        newpos = np.zeros(nrows, np.int32) if want_newpos else None
+        _check(lib().vnm_nm_reorder(self.h, nrows, nnz, pr, pc, pv, mem, N, M, sched, nm_maxiter,
+                                    res.ctypes.data_as(_i32p),
+                                    newpos.ctypes.data_as(_i32p) if newpos is not None else None),
+               "vnm_nm_reorder")
+        return res, newpos
+
+    def nm_search(self, nrows, row, col, val, N, M, nm_maxiter=10, want_newpos=True):
+        """find_best_2toX over schedules 0..3: returns (best, res5x4, newpos)."""
+        pr, pc, pv, mem, nnz, keep = self._arrays(row, col, val)
+        res = np.zeros(20, np.int32)
+        best = ctypes.c_int()
+        newpos = np.zeros(nrows, np.int32) if want_newpos else None
+        _check(lib().vnm_nm_search(self.h, nrows, nnz, pr, pc, pv, mem, N, M, nm_maxiter, ctypes.byref(best),
+                                   res.ctypes.data_as(_i32p),
+                                   newpos.ctypes.data_as(_i32p) if newpos is not None else None), "vnm_nm_search")
+        return best.value, res.reshape(4, 5), newpos
+
+    def set_trace(self, on):
+        _check(lib().vnm_nm_set_trace(self.h, 1 if on else 0), "vnm_nm_set_trace")
+
+    def get_trace(self):
+        """Swaps of the last traced job: list of per-round (k, 2) arrays."""
+        np_, nr = ctypes.c_int(), ctypes.c_int()
+        _check(lib().vnm_nm_get_trace(self.h, None, 0, ctypes.byref(np_), None, 0, ctypes.byref(nr)), "trace")
+        pairs = np.zeros(2 * max(np_.value, 1), np.int32)
+        ends = np.zeros(max(nr.value, 1), np.int32)
+        _check(lib().vnm_nm_get_trace(self.h, pairs.ctypes.data_as(_i32p), np_.value, ctypes.byref(np_),
+                                      ends.ctypes.data_as(_i32p), nr.value, ctypes.byref(nr)), "trace")
+        pairs = pairs[:2 * np_.value].reshape(-1, 2)
+        out, start = [], 0
+        for e in ends[:nr.value].tolist():
+            out.append(pairs[start:e])
+            start = e
+        return out
+
+    def permute_coo(self, nrows, row, col, newpos):
+        if hasattr(row, "is_cuda") and row.is_cuda:
+            _check(lib().vnm_permute_coo(self.h, nrows, int(row.numel()), ctypes.c_void_p(row.data_ptr()),
+                                         ctypes.c_void_p(col.data_ptr()), MEM_DEVICE,
+                                         ctypes.c_void_p(newpos.data_ptr())), "vnm_permute_coo")
+            return row, col
+        r = np.array(row, np.int32)
+        c = np.array(col, np.int32)
+        p = _host(newpos, np.int32)
+        _check(lib().vnm_permute_coo(self.h, nrows, len(r), _ptr(r, None), _ptr(c, None), MEM_HOST,
+                                     _ptr(p, None)), "vnm_permute_coo")
+        return r, c
+
+    def nm_segment_counts(self, nrows, row, col, val, N, M):
+        pr, pc, pv, mem, nnz, keep = self._arrays(row, col, val)
+        inv = np.zeros(nrows // M, np.int32)
+        az = np.zeros(nrows // M, np.int32)
+        _check(lib().vnm_nm_segment_counts(self.h, nrows, nnz, pr, pc, pv, mem, N, M, inv.ctypes.data_as(_i32p),
+                                           az.ctypes.data_as(_i32p)), "vnm_nm_segment_counts")
+        return inv, az
+
+    def nm_pair_score(self, nrows, row, col, val, N, M, s1, s2):
+        pr, pc, pv, mem, nnz, keep = self._arrays(row, col, val)
+        sc = np.zeros(2 * M * M, np.int32)
+        _check(lib().vnm_nm_pair_score(self.h, nrows, nnz, pr, pc, pv, mem, N, M, s1, s2,
+                                       sc.ctypes.data_as(_i32p)), "vnm_nm_pair_score")
+        return sc
