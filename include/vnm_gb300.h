@@ -142,6 +142,29 @@ vnm_status vnm_nm_segment_counts(vnm_ctx* ctx, int nrows, int nnz, const int* ro
 vnm_status vnm_nm_pair_score(vnm_ctx* ctx, int nrows, int nnz, const int* row, const int* col, const float* val,
                              int mem, int N, int M, int seg1, int seg2, int* score);
 
+/* ---------------------------------------------------------------------------
+ * VNM stage (the row sort of reordering.py)
+ * ------------------------------------------------------------------------- */
+
+/* `python3 reordering.py --evalonly --m M --v V` (reordering.py:187-198):
+ * out2 = {V-blocks whose OR over V rows has more than 4 ones, the same
+ * count also flagging blocks with a row of more than 2 ones}.  m, n are the
+ * matrix shape (padded to multiples of M inside, reordering.py:50-51); the
+ * pattern is every stored entry (values are not read).  COO in any order. */
+vnm_status vnm_vnm_eval(vnm_ctx* ctx, int m, int n, int nnz, const int* row, const int* col, int mem, int M, int V,
+                        int* out2);
+
+/* `python3 reordering.py --m M --v V` (reordering.py:200-265): repeated
+ * stable sorts of the rows by their Gray-code hashed segment strings, each
+ * applied to rows and columns, stopping when the V-block count grows or
+ * reaches 0 or after max(maxiter, initial count) rounds.  row/col are
+ * replaced by the matrix the script writes back (entries keep their order).
+ *   out5   = the five integers of output.txt:
+ *            {init, init_strict, final, final_strict, rounds}
+ *   newpos = optional, length m padded to M: final position of each row. */
+vnm_status vnm_vnm_reorder(vnm_ctx* ctx, int m, int n, int nnz, int* row, int* col, int mem, int M, int V,
+                           int maxiter, int* out5, int* newpos);
+
 /* Host helper: the pop order of the SwapPair priority queue of
  * reorder/reorder.h:521-532 (Comparator, reorder/swappair.h:112-120) for n
  * pairs pushed in index order -- the exact emulation the kernels use. */

@@ -1231,3 +1231,4 @@ vnm_status vnm_nm_reorder_batch(vnm_ctx* ctx, int nmat, const int* nrows, const 
 }
 
 }  // extern "C"
+

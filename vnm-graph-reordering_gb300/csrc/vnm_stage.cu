@@ -427,7 +427,8 @@ vnm_status vnm_vnm_reorder(vnm_ctx* ctx, int m, int n, int nnz, int* row, int* c
     VNM_CUDA_TRY(cudaMemcpyAsync(prev_c, col, sizeof(int) * nnz, kind, ctx->stream));
   }
   VNM_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
-  if (nnz) VNM_LAUNCH(ctx, k_vs_check, vs_grid(ctx, nnz), VS_NT, 0, prev_r, prev_c, nnz, mp, np, err);
+  // columns index new_id[] (m entries), as in reordering.py:175-176
+  if (nnz) VNM_LAUNCH(ctx, k_vs_check, vs_grid(ctx, nnz), VS_NT, 0, prev_r, prev_c, nnz, mp, mp < np ? mp : np, err);
   VNM_CUDA_TRY(cudaMemcpyAsync(h, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   VNM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   if (h[0]) return VNM_ERR_RANGE;

@@ -73,6 +73,10 @@ def lib():
     L.vnm_nm_pair_score.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
                                     ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p]
     L.vnm_swap_heap_order.argtypes = [ctypes.c_int, _i32p, _i32p, _i32p]
+    L.vnm_vnm_eval.argtypes = [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                               ctypes.c_int, _i32p]
+    L.vnm_vnm_reorder.argtypes = [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, ctypes.c_int,
+                                  ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p, _i32p]
     _lib = L
     return L
 
@@ -232,3 +236,23 @@ class Context:
         _check(lib().vnm_nm_pair_score(self.h, nrows, nnz, pr, pc, pv, mem, N, M, s1, s2,
                                        sc.ctypes.data_as(_i32p)), "vnm_nm_pair_score")
         return sc
+
+    # ---- VNM stage (reordering.py)
+    def vnm_eval(self, m, n, row, col, M, V):
+        r = _host(row, np.int32)
+        c = _host(col, np.int32)
+        out = np.zeros(2, np.int32)
+        _check(lib().vnm_vnm_eval(self.h, m, n, len(r), _ptr(r, None), _ptr(c, None), MEM_HOST, M, V,
+                                  out.ctypes.data_as(_i32p)), "vnm_vnm_eval")
+        return out
+
+    def vnm_reorder(self, m, n, row, col, M, V, maxiter=10):
+        """reordering.py's loop: returns (out5, row', col', newpos)."""
+        r = np.array(row, np.int32)
+        c = np.array(col, np.int32)
+        out = np.zeros(5, np.int32)
+        mp = (m + M - 1) // M * M
+        newpos = np.zeros(mp, np.int32)
+        _check(lib().vnm_vnm_reorder(self.h, m, n, len(r), _ptr(r, None), _ptr(c, None), MEM_HOST, M, V, maxiter,
+                                     out.ctypes.data_as(_i32p), newpos.ctypes.data_as(_i32p)), "vnm_vnm_reorder")
+        return out, r, c, newpos
