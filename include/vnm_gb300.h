@@ -125,6 +125,30 @@ vnm_status vnm_nm_set_trace(vnm_ctx* ctx, int enable);
 vnm_status vnm_nm_get_trace(vnm_ctx* ctx, int* pairs, int cap_pairs, int* npairs, int* round_end, int cap_rounds,
                             int* nrounds);
 
+/* vnm_nm_reorder for callers that cannot allocate device memory.  No
+ * counterpart in the reference.  Some callers cannot call cudaMalloc:
+ * services whose device memory is all handed out up front by their own
+ * allocator, and latency-critical loops where an allocation (which can
+ * synchronise the device) is not allowed.  This entry point allocates
+ * nothing and needs no context: its scratch is one fixed array in device
+ * memory of VNM_NOALLOC_SCRATCH_BYTES, which every GPU that loads the
+ * library keeps until the process exits.
+ *   - row, col, val: device memory of the current device, sorted COO as for
+ *     vnm_nm_reorder; res5 (5 ints) and newpos (nrows ints): device memory
+ *     the caller owns; work is issued on `stream` (a cudaStream_t, NULL for
+ *     the default stream) and the call returns when it is done.
+ *   - nrows <= VNM_NOALLOC_MAX_ROWS and nnz <= VNM_NOALLOC_MAX_NNZ, else
+ *     VNM_ERR_LIMIT.
+ *   - The first call on a device looks up the array's device address with
+ *     that device current; make that first call before any stream capture.
+ *   - All calls share the array.  Calls that overlap on the GPU (from other
+ *     streams or host threads) race; serialise them. */
+#define VNM_NOALLOC_MAX_ROWS 32768
+#define VNM_NOALLOC_MAX_NNZ 524288
+#define VNM_NOALLOC_SCRATCH_BYTES (10u << 20)
+vnm_status vnm_nm_reorder_noalloc(int nrows, int nnz, const int* row, const int* col, const float* val, int N, int M,
+                                  int sched, int nm_maxiter, int* res5, int* newpos, void* stream);
+
 /* Apply a node permutation to a COO in place: row = newpos[row],
  * col = newpos[col] -- the Reorder kernel of reorder/reorder.h:23-35 with all
  * rounds composed.  The order of the entries does not change. */

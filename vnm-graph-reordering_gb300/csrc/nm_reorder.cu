@@ -1232,3 +1232,95 @@ vnm_status vnm_nm_reorder_batch(vnm_ctx* ctx, int nmat, const int* nrows, const 
 
 }  // extern "C"
 
+// ---------------------------------------------------------------------------
+// NM reorder without allocation
+//
+// Some callers cannot call cudaMalloc: services whose device memory is all
+// handed out up front by their own allocator (a foreign allocation would
+// break its accounting or fail), and latency-critical loops where an
+// allocation -- which can synchronise the device -- is not allowed.  For
+// them, vnm_nm_reorder_noalloc runs the same kernels as vnm_nm_reorder with
+// its scratch taken from one fixed array in device memory instead of the
+// context's allocator, and with no context at all.
+//
+// Limits: nrows <= VNM_NOALLOC_MAX_ROWS, nnz <= VNM_NOALLOC_MAX_NNZ; the
+// array is VNM_NOALLOC_SCRATCH_BYTES and every GPU that loads this library
+// keeps it until the process exits.  All calls share it: calls that overlap
+// on the GPU (other streams, other host threads) race and must not be made.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace vnm {
+
+constexpr int NOALLOC_MAX_ROWS = 32768;
+constexpr int NOALLOC_MAX_NNZ = 1 << 19;
+constexpr size_t NOALLOC_BYTES = size_t(10) << 20;  // 10 MiB
+
+// The scratch itself.  Host code must not use this symbol as an address
+// (in host code it names a host-side shadow); it asks the runtime for the
+// device address instead (noalloc_scratch below).
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+// Device address of g_noalloc_scratch on `device`, looked up once per device
+// with that device current.
+static vnm_status noalloc_scratch(int device, unsigned char** out) {
+  constexpr int MAXDEV = 64;
+  static unsigned char* addr[MAXDEV] = {nullptr};
+  static std::mutex mu;
+  if (device < 0 || device >= MAXDEV) return VNM_ERR_ARG;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      (void)cudaGetLastError();
+      return VNM_ERR_CUDA;
+    }
+    addr[device] = static_cast<unsigned char*>(p);
+  }
+  *out = addr[device];
+  return VNM_OK;
+}
+
+}  // namespace vnm
+
+extern "C" vnm_status vnm_nm_reorder_noalloc(int nrows, int nnz, const int* row, const int* col, const float* val,
+                                             int N, int M, int sched, int nm_maxiter, int* res5, int* newpos,
+                                             void* stream) {
+  using namespace vnm;
+  VNM_TRY(check_nm_args(nrows, nnz, row, col, val, VNM_MEM_DEVICE, N, M));
+  if (sched < 0 || sched > 3 || !res5 || !newpos) return VNM_ERR_ARG;
+  if (nrows > NOALLOC_MAX_ROWS || nnz > NOALLOC_MAX_NNZ) return VNM_ERR_LIMIT;
+  const size_t need = pattern_bytes(nrows, nnz) + job_bytes(nrows) + arena_bytes(1, sizeof(NMJob)) + 4096;
+  if (need > NOALLOC_BYTES) return VNM_ERR_LIMIT;
+  int device = 0;
+  VNM_CUDA_TRY(cudaGetDevice(&device));
+  unsigned char* scratch = nullptr;
+  VNM_TRY(noalloc_scratch(device, &scratch));
+  // a context on the stack: its "arena" is the fixed array, its stream the
+  // caller's; no event, stream or memory is created
+  vnm_ctx c;
+  c.device = device;
+  c.num_sms = 1;
+  VNM_CUDA_TRY(cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, device));
+  c.stream = static_cast<cudaStream_t>(stream);
+  c.arena.base = reinterpret_cast<char*>(scratch);
+  c.arena.cap = NOALLOC_BYTES;
+  c.arena.used = 0;
+  int hs[16] = {0};  // host readback (pageable)
+  Pattern P;
+  VNM_TRY(build_pattern(&c, nrows, nnz, row, col, val, N, M, P, hs));
+  NMJob hj;
+  VNM_TRY(make_job(&c, P, sched, nm_maxiter, hj));  // clears the job's scratch
+  NMJob* d_job = arena_take<NMJob>(&c, 1);
+  if (!d_job) return VNM_ERR_LIMIT;
+  VNM_CUDA_TRY(cudaMemcpyAsync(d_job, &hj, sizeof(NMJob), cudaMemcpyHostToDevice, c.stream));
+  VNM_TRY(launch_rounds(&c, d_job, 1, N, M));
+  VNM_CUDA_TRY(cudaMemcpyAsync(hs, hj.res, sizeof(int) * 16, cudaMemcpyDeviceToHost, c.stream));
+  VNM_CUDA_TRY(cudaStreamSynchronize(c.stream));
+  if (hs[5] != 0) return VNM_ERR_INTERNAL;
+  VNM_CUDA_TRY(cudaMemcpyAsync(res5, hj.res, sizeof(int) * 5, cudaMemcpyDeviceToDevice, c.stream));
+  if (nrows > 0) VNM_LAUNCH(&c, k_invert, grid_for(&c, nrows), 256, 0, hj.orig, nrows, newpos);
+  VNM_CUDA_TRY(cudaStreamSynchronize(c.stream));
+  return VNM_OK;
+}
