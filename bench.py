@@ -206,6 +206,7 @@ def run_ours(args, rank, world, local):
     barrier()
     dev_ms, main_ms, launches, wall = 0.0, 0.0, 0, 0.0
     stats_sum = None
+    phase_sum = None
     for _ in range(args.steps):
         t0 = time.perf_counter()
         best, res, newpos = step(True)
@@ -214,7 +215,9 @@ def run_ours(args, rank, world, local):
         main_ms += ctx.last_main_kernel_ms
         launches += ctx.last_launch_count
         st = ctx.last_stats()
+        ph = st.pop("phase_kcycles")
         stats_sum = st if stats_sum is None else {k: stats_sum[k] + st[k] for k in st}
+        phase_sum = ph if stats_sum is st else {k: phase_sum[k] + ph[k] for k in ph}
     barrier()
     clk = clocks.stop()
     # the search launches the four jobs and then a second single job for the
@@ -263,7 +266,10 @@ def run_ours(args, rank, world, local):
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
                      "alg_bytes_per_step": alg_bytes / args.steps,
                      "kernel_ms_per_step": main_ms / args.steps,
-                     "note": "latency-bound sequential greedy; see profiles/"},
+                     "note": "latency-bound sequential greedy; see profiles/",
+                     "round_phase_share": {k: round(v / max(1, sum(phase_sum.values())), 4)
+                                           for k, v in phase_sum.items()},
+                     "us_per_round": 1000.0 * main_ms / max(1, st["rounds"] / max(1, st["jobs"]))},
         "gpu_launches": launches,
         "clocks": clk,
         "wall_ms_per_step": 1000.0 * wall / args.steps,

@@ -71,7 +71,9 @@ float vnm_last_main_kernel_ms(const vnm_ctx* ctx);
 /* Work counters of the last NM call (for roofline accounting):
  * out[0] rounds summed over jobs, out[1] column entries gathered,
  * out[2] row records touched, out[3] segments per job, out[4] jobs,
- * out[5] nonzero-valued entries of the pattern.  n <= 8 values. */
+ * out[5] nonzero-valued entries of the pattern, out[8..14] kilocycles
+ * spent per round phase (select, choose, gather, process, heap, walk,
+ * apply) summed over jobs.  n <= 16 values. */
 vnm_status vnm_last_stats(const vnm_ctx* ctx, long long* out, int n);
 
 /* ---------------------------------------------------------------------------

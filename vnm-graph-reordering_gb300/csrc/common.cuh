@@ -51,7 +51,7 @@ struct vnm_ctx {
   cudaEvent_t ev_main0 = nullptr, ev_main1 = nullptr;  // around the call's main kernel
   float last_ms = 0.f;
   float main_ms = 0.f;
-  long long stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // work counters of the last call
+  long long stats[16] = {0};  // work counters of the last call
   int launches = 0;
   DeviceArena arena;
   // pinned staging for small results

@@ -67,8 +67,9 @@ struct NMJob {
   int* zc;            // [nseg] all-zero rows per segment
   uint4* rec;         // [R] per-row scratch, zero on entry and on exit
   int* touched;       // [R] scratch
-  int* res;           // [16]: init_size, final_size, init_cnt, final_cnt, rounds, status,
-                      //       swaps, gathered entries (lo, hi), touched rows (lo, hi)
+  int* res;           // [24]: init_size, final_size, init_cnt, final_cnt, rounds, status,
+                      //       swaps, gathered entries (lo, hi), touched rows (lo, hi),
+                      //       [16..22] kilocycles per round phase
   int* trace_pairs;   // optional: swaps in commit order (v1, v2)
   int* trace_rounds;  // optional: pairs committed by the end of each round
   int trace_cap_pairs;
@@ -756,15 +757,32 @@ __global__ void __launch_bounds__(NM_THREADS) k_nm_rounds(const NMJob* __restric
   int round = 1;
   int committed = 0;
   unsigned long long sumE = 0, sumT = 0;
+  // cycles spent in each phase of a round, measured by thread 0 at the
+  // barriers that end the phases: select, choose, gather, process, heap,
+  // walk, apply
+  unsigned long long tph[7] = {0, 0, 0, 0, 0, 0, 0};
+  long long t0 = clock64(), t1;
+#define VNM_PHASE(i)                     \
+  if (tid == 0) {                        \
+    t1 = clock64();                      \
+    tph[i] += (unsigned long long)(t1 - t0); \
+    t0 = t1;                             \
+  }
   while (round <= MAXITER && sm.lsize >= 1) {
     if (sm.lsize == 1) minseg_phase<M>(sm, J);
+    VNM_PHASE(0);
     choose_segments<M>(sm, J.sched);
     __syncthreads();
+    VNM_PHASE(1);
     gather_phase<M>(sm, J);
+    VNM_PHASE(2);
     process_phase<M>(sm, J, N);
+    VNM_PHASE(3);
     heap_phase<M>(sm);
+    VNM_PHASE(4);
     walk_phase<M>(sm, J.sched);
     __syncthreads();
+    VNM_PHASE(5);
     if (tid == 0 && J.trace_pairs) {
       for (int q = 0; q < sm.nswaps; ++q) {
         if (committed < J.trace_cap_pairs) {
@@ -780,10 +798,12 @@ __global__ void __launch_bounds__(NM_THREADS) k_nm_rounds(const NMJob* __restric
     apply_phase<M>(sm, J, N, round);
     clear_round_smem<M>(sm);
     __syncthreads();
+    VNM_PHASE(6);
     select_phase<M>(sm, J);
     round += 1;
     if (sm.status != JOB_OK) break;
   }
+#undef VNM_PHASE
   if (tid == 0) {
     J.res[0] = init_size;
     J.res[1] = sm.lsize;
@@ -796,6 +816,7 @@ __global__ void __launch_bounds__(NM_THREADS) k_nm_rounds(const NMJob* __restric
     J.res[8] = (int)(sumE >> 31);
     J.res[9] = (int)(sumT & 0x7fffffffull);
     J.res[10] = (int)(sumT >> 31);
+    for (int q = 0; q < 7; ++q) J.res[16 + q] = (int)(tph[q] >> 10);  // kilocycles
   }
 }
 
@@ -930,7 +951,7 @@ static vnm_status build_pattern(vnm_ctx* ctx, int R, int nnz, const int* d_row, 
 size_t job_bytes(int R) {
   const int nseg = R / 2 + 1;
   return arena_bytes(R, sizeof(int)) + 2 * arena_bytes(nseg, sizeof(int)) + arena_bytes(R, sizeof(uint4)) +
-         arena_bytes(R, sizeof(int)) + arena_bytes(16, sizeof(int));
+         arena_bytes(R, sizeof(int)) + arena_bytes(24, sizeof(int));
 }
 
 // Carve one job's state out of the arena and initialise it.
@@ -946,14 +967,14 @@ static vnm_status make_job(vnm_ctx* ctx, const Pattern& P, int sched, int maxite
   J.zc = arena_take<int>(ctx, P.nseg + 1);
   J.rec = arena_take<uint4>(ctx, P.R > 0 ? P.R : 1);
   J.touched = arena_take<int>(ctx, P.R > 0 ? P.R : 1);
-  J.res = arena_take<int>(ctx, 16);
+  J.res = arena_take<int>(ctx, 24);
   J.trace_pairs = nullptr;
   J.trace_rounds = nullptr;
   J.trace_cap_pairs = 0;
   J.trace_cap_rounds = 0;
   if (!J.orig || !J.cnt || !J.zc || !J.rec || !J.touched || !J.res) return VNM_ERR_NOMEM;
   VNM_CUDA_TRY(cudaMemsetAsync(J.rec, 0, sizeof(uint4) * (P.R > 0 ? P.R : 1), ctx->stream));
-  VNM_CUDA_TRY(cudaMemsetAsync(J.res, 0, sizeof(int) * 16, ctx->stream));
+  VNM_CUDA_TRY(cudaMemsetAsync(J.res, 0, sizeof(int) * 24, ctx->stream));
   if (P.R > 0)
     VNM_LAUNCH(ctx, k_init_job, grid_for(ctx, P.R), 256, 0, J.orig, J.cnt, J.zc, P.inv0, P.pres0, P.R, P.nseg);
   return VNM_OK;
@@ -1049,22 +1070,23 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
   VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main1, ctx->stream));
   int* hres = ctx->h_pinned;
   for (int s = 0; s < nsched; ++s)
-    VNM_CUDA_TRY(cudaMemcpyAsync(hres + 16 * s, hj[s].res, sizeof(int) * 16, cudaMemcpyDeviceToHost, ctx->stream));
+    VNM_CUDA_TRY(cudaMemcpyAsync(hres + 24 * s, hj[s].res, sizeof(int) * 24, cudaMemcpyDeviceToHost, ctx->stream));
   VNM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   VNM_CUDA_TRY(cudaEventElapsedTime(&ctx->main_ms, ctx->ev_main0, ctx->ev_main1));
-  int hres_copy[64];
-  memcpy(hres_copy, hres, sizeof(int) * 16 * nsched);
-  for (int q = 0; q < 8; ++q) ctx->stats[q] = 0;
+  int hres_copy[96];
+  memcpy(hres_copy, hres, sizeof(int) * 24 * nsched);
+  for (int q = 0; q < 16; ++q) ctx->stats[q] = 0;
   ctx->stats[3] = P.nseg;
   ctx->stats[4] = nsched;
   ctx->stats[5] = P.np;
   for (int s = 0; s < nsched; ++s) {
-    const int* h = hres_copy + 16 * s;
+    const int* h = hres_copy + 24 * s;
     if (h[5] != 0) return VNM_ERR_INTERNAL;
     for (int q = 0; q < 5; ++q) res5_out[5 * s + q] = h[q];
     ctx->stats[0] += h[4];
     ctx->stats[1] += (long long)h[7] + ((long long)h[8] << 31);
     ctx->stats[2] += (long long)h[9] + ((long long)h[10] << 31);
+    for (int q = 0; q < 7; ++q) ctx->stats[8 + q] += h[16 + q];
   }
   if (trace) {
     const int committed = hres_copy[6];

@@ -151,10 +151,13 @@ class Context:
         return lib().vnm_last_main_kernel_ms(self.h)
 
     def last_stats(self):
-        out = (ctypes.c_longlong * 8)()
-        _check(lib().vnm_last_stats(self.h, out, 8), "vnm_last_stats")
+        out = (ctypes.c_longlong * 16)()
+        _check(lib().vnm_last_stats(self.h, out, 16), "vnm_last_stats")
         keys = ("rounds", "gathered", "touched", "nseg", "jobs", "pattern_nnz")
-        return dict(zip(keys, list(out)[:6]))
+        d = dict(zip(keys, list(out)[:6]))
+        d["phase_kcycles"] = dict(zip(("select", "choose", "gather", "process", "heap", "walk", "apply"),
+                                      list(out)[8:15]))
+        return d
 
     # ---- array plumbing: numpy arrays (host) or torch CUDA tensors (device)
     @staticmethod
