@@ -1040,7 +1040,7 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
                 arena_bytes(R, sizeof(int)) + 3 * arena_bytes(nnz, sizeof(int)) +
                 arena_bytes(trace_pairs_cap * 2, sizeof(int)) + arena_bytes(trace_rounds_cap, sizeof(int)) + 4096;
   VNM_TRY(arena_reserve(ctx, need));
-  VNM_TRY(pinned_reserve(ctx, 64 + (size_t)trace_pairs_cap * 2 + trace_rounds_cap));
+  VNM_TRY(pinned_reserve(ctx, 256 + (size_t)trace_pairs_cap * 2 + trace_rounds_cap));
   VNM_TRY(begin_call(ctx));
   const int *d_row, *d_col;
   const float* d_val;
@@ -1093,7 +1093,7 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
     const int rounds = hres_copy[4];
     const int np = committed < trace_pairs_cap ? committed : trace_pairs_cap;
     const int nr = rounds < trace_rounds_cap ? rounds : trace_rounds_cap;
-    int* hp = ctx->h_pinned + 64;
+    int* hp = ctx->h_pinned + 128;  // after the per-job results (24 ints each)
     if (np) VNM_CUDA_TRY(cudaMemcpyAsync(hp, d_tp, sizeof(int) * 2 * np, cudaMemcpyDeviceToHost, ctx->stream));
     if (nr)
       VNM_CUDA_TRY(cudaMemcpyAsync(hp + 2 * np, d_tr, sizeof(int) * nr, cudaMemcpyDeviceToHost, ctx->stream));
