@@ -259,7 +259,7 @@ __device__ __forceinline__ void topk_warp_merge(unsigned long long (&a)[K], unsi
 
 // Scan the segment counts: list size, total, first K in both orders.
 template <int M>
-__device__ void select_phase(RoundSmem<M>& sm, const NMJob& J) {
+__device__ void select_phase(RoundSmem<M>& sm, const NMJob& J, const int* cnt) {
   constexpr int K = M + 1;
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   unsigned long long kd[K], kr[K];
@@ -267,7 +267,7 @@ __device__ void select_phase(RoundSmem<M>& sm, const NMJob& J) {
   for (int q = 0; q < K; ++q) kd[q] = kr[q] = 0;
   int lsz = 0, tot = 0;
   for (int s = tid; s < J.nseg; s += NM_THREADS) {
-    const int c = J.cnt[s];
+    const int c = cnt[s];
     if (c > 0) {
       lsz++;
       tot += c;
@@ -441,17 +441,41 @@ __device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J) {
   __syncthreads();
   const int E = sm.E;
   unsigned* recw = reinterpret_cast<unsigned*>(J.rec);
-  for (int e = tid; e < E; e += NM_THREADS) {
-    int lo = 0, hi = KM - 1;  // last q with colpre[q] <= e
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (sm.colpre[mid] <= e) lo = mid;
-      else hi = mid - 1;
+  // GATHER_U entries per thread per step: their row loads, their bitmap ORs
+  // (no result used, so they issue as reductions) and their first-touch
+  // atomics are all in flight together instead of one chain at a time.
+  constexpr int GATHER_U = 4;
+  for (int base = tid; base < E; base += NM_THREADS * GATHER_U) {
+    int rr[GATHER_U];
+    unsigned word[GATHER_U], bit[GATHER_U];
+#pragma unroll
+    for (int u = 0; u < GATHER_U; ++u) {
+      const int e = base + u * NM_THREADS;
+      rr[u] = -1;
+      word[u] = 0;
+      bit[u] = 0;
+      if (e < E) {
+        int lo = 0, hi = KM - 1;  // last q with colpre[q] <= e
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (sm.colpre[mid] <= e) lo = mid;
+          else hi = mid - 1;
+        }
+        const int q = lo, xi = q / M, k = q % M;
+        rr[u] = J.crow[sm.colstart[q] + (e - sm.colpre[q])];
+        word[u] = (unsigned)(xi >> 2);
+        bit[u] = (1u << k) << ((xi & 3) * 8);
+      }
     }
-    const int q = lo, xi = q / M, k = q % M;
-    const int r = J.crow[sm.colstart[q] + (e - sm.colpre[q])];
-    atomicOr(&recw[4 * r + (xi >> 2)], (1u << k) << ((xi & 3) * 8));
-    if (atomicOr(&recw[4 * r + 3], 1u) == 0u) J.touched[atomicAdd(&sm.ntouched, 1)] = r;
+#pragma unroll
+    for (int u = 0; u < GATHER_U; ++u)
+      if (rr[u] >= 0) atomicOr(&recw[4 * rr[u] + word[u]], bit[u]);
+    unsigned first[GATHER_U];
+#pragma unroll
+    for (int u = 0; u < GATHER_U; ++u) first[u] = rr[u] >= 0 ? atomicOr(&recw[4 * rr[u] + 3], 1u) : 1u;
+#pragma unroll
+    for (int u = 0; u < GATHER_U; ++u)
+      if (first[u] == 0u) J.touched[atomicAdd(&sm.ntouched, 1)] = rr[u];
   }
   __syncthreads();
 }
@@ -461,28 +485,62 @@ __device__ __forceinline__ unsigned rec_byte(const uint4& w, int xi) {
   return (word >> ((xi & 3) * 8)) & 0xffu;
 }
 
-// Solo terms and pair corrections (fact 3).
+// Run f(row, record, valid) over the touched rows, one row per lane, with
+// every lane of a warp calling f the same number of times (lanes past the
+// end get valid = false and a zero record) so f may use warp votes.  Each
+// lane first loads the records of TOUCH_U rows so their L2 round trips
+// overlap.
+template <int M, class F>
+__device__ __forceinline__ void for_touched_warp(const RoundSmem<M>& sm, const NMJob& J, F&& f) {
+  constexpr int TOUCH_U = 4;
+  constexpr int NW = NM_THREADS / 32;
+  const int nt = sm.ntouched;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int base = w * 32 * TOUCH_U; base < nt; base += NW * 32 * TOUCH_U) {
+    int rv[TOUCH_U];
+    uint4 wv[TOUCH_U];
+#pragma unroll
+    for (int u = 0; u < TOUCH_U; ++u) {
+      const int t = base + u * 32 + lane;
+      rv[u] = t < nt ? J.touched[t] : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < TOUCH_U; ++u) wv[u] = rv[u] >= 0 ? J.rec[rv[u]] : make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll 1
+    for (int u = 0; u < TOUCH_U; ++u) f(rv[u], wv[u], rv[u] >= 0);
+  }
+}
+
+// Solo terms and pair corrections (fact 3), accumulated with warp votes:
+// for 32 rows at a time, a count over rows of a product of two per-row bit
+// conditions is popc(ballot(first) & ballot(second)), and one lane adds it
+// to shared memory.  For the pair (a, c) with L = bits in a, R = bits in c,
+// over rows where both are non-empty:
+//   CL(i, j) = sum  R_j * eL_i,   eL = L if pL == N+1, ~L if pL == N, else 0
+//   CR(i, j) = sum  L_i * eR_j,   eR = R if pR == N+1, ~R if pR == N, else 0
+//   S_a(k)   = sum over all rows of [L_k and pL == N+1]
 template <int M>
 __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N) {
   constexpr int K = M + 1;
+  constexpr int MM = M * M;
   constexpr unsigned MASK = (1u << M) - 1u;
-  const int nt = sm.ntouched, Kn = sm.K_;
+  const int Kn = sm.K_;
   const bool self = sm.mode == 2;
-  for (int t = threadIdx.x; t < nt; t += NM_THREADS) {
-    const int r = J.touched[t];
-    const uint4 w = J.rec[r];
+  const int lane = threadIdx.x & 31;
+  for_touched_warp<M>(sm, J, [&](int r, const uint4& w, bool valid) {
+    (void)r;
     unsigned b[K];
     int p[K];
 #pragma unroll
     for (int xi = 0; xi < K; ++xi) {
-      b[xi] = xi < Kn ? rec_byte(w, xi) : 0u;
+      b[xi] = (valid && xi < Kn) ? rec_byte(w, xi) : 0u;
       p[xi] = __popc(b[xi]);
     }
     if (self) {
       // reference kernel lines 108-121 with lval == rval: direct per (i, j)
       const unsigned L = b[0];
       const int pl = p[0];
-      if (L == 0) continue;
+      if (L == 0) return;
       for (int i = 0; i < M; ++i) {
         const unsigned li = (L >> i) & 1u;
         for (int j = 0; j < M; ++j) {
@@ -493,60 +551,63 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N) {
           if (rr) atomicAdd(&sm.CR[0][i * M + j], rr);
         }
       }
-      continue;
+      return;
     }
+    // solo terms
 #pragma unroll
     for (int xi = 0; xi < K; ++xi) {
-      if (p[xi] == N + 1) {
-        unsigned bb = b[xi];
-        while (bb) {
-          int k = __ffs(bb) - 1;
-          bb &= bb - 1;
-          atomicAdd(&sm.S[xi][k], 1);
-        }
+      const unsigned s = p[xi] == N + 1 ? b[xi] : 0u;
+      if (__ballot_sync(FULL, s != 0u) == 0u) continue;
+#pragma unroll
+      for (int k = 0; k < M; ++k) {
+        const unsigned v = __ballot_sync(FULL, (s >> k) & 1u);
+        if (lane == k && v) atomicAdd(&sm.S[xi][k], __popc(v));
       }
     }
+    // pair corrections
 #pragma unroll
     for (int a = 0; a < K; ++a) {
-      if (!b[a]) continue;
 #pragma unroll
       for (int c = a + 1; c < K; ++c) {
-        if (!b[c]) continue;
-        const unsigned L = b[a], Rb = b[c];
-        const int pid = pair_id<M>(a, c);
-        // left corrections: R_j = 1 and (L_i = 1, pL = N+1  or  L_i = 0, pL = N)
-        const unsigned li_set = p[a] == N + 1 ? L : (p[a] == N ? (~L & MASK) : 0u);
-        if (li_set) {
-          unsigned jj = Rb;
-          while (jj) {
-            const int j = __ffs(jj) - 1;
-            jj &= jj - 1;
-            unsigned ii = li_set;
-            while (ii) {
-              const int i = __ffs(ii) - 1;
-              ii &= ii - 1;
-              atomicAdd(&sm.CL[pid][i * M + j], 1);
-            }
-          }
+        const bool both = b[a] != 0u && b[c] != 0u;
+        if (__ballot_sync(FULL, both) == 0u) continue;
+        const unsigned L = both ? b[a] : 0u, Rb = both ? b[c] : 0u;
+        const unsigned eL = p[a] == N + 1 ? L : (p[a] == N ? (~L & MASK) : 0u);
+        const unsigned eR = p[c] == N + 1 ? Rb : (p[c] == N ? (~Rb & MASK) : 0u);
+        unsigned vL[M], vR[M], vE[M], vF[M];  // ballots of L_i, R_j, eL_i, eR_j
+#pragma unroll
+        for (int k = 0; k < M; ++k) {
+          vL[k] = __ballot_sync(FULL, (L >> k) & 1u);
+          vR[k] = __ballot_sync(FULL, (Rb >> k) & 1u);
+          vE[k] = __ballot_sync(FULL, both && ((eL >> k) & 1u));
+          vF[k] = __ballot_sync(FULL, both && ((eR >> k) & 1u));
         }
-        // right corrections: L_i = 1 and (R_j = 1, pR = N+1  or  R_j = 0, pR = N)
-        const unsigned rj_set = p[c] == N + 1 ? Rb : (p[c] == N ? (~Rb & MASK) : 0u);
-        if (rj_set) {
-          unsigned ii = L;
-          while (ii) {
-            const int i = __ffs(ii) - 1;
-            ii &= ii - 1;
-            unsigned jj = rj_set;
-            while (jj) {
-              const int j = __ffs(jj) - 1;
-              jj &= jj - 1;
-              atomicAdd(&sm.CR[pid][i * M + j], 1);
+        const int pid = pair_id<M>(a, c);
+#pragma unroll
+        for (int idx0 = 0; idx0 < MM; idx0 += 32) {
+          const int idx = idx0 + lane;
+          if (idx < MM) {
+            const int i = idx / M, j = idx % M;
+            unsigned e_i = 0, l_i = 0, r_j = 0, f_j = 0;
+#pragma unroll
+            for (int k = 0; k < M; ++k) {
+              if (k == i) {
+                e_i = vE[k];
+                l_i = vL[k];
+              }
+              if (k == j) {
+                r_j = vR[k];
+                f_j = vF[k];
+              }
             }
+            const int cl = __popc(e_i & r_j), cr = __popc(l_i & f_j);
+            if (cl) atomicAdd(&sm.CL[pid][idx], cl);
+            if (cr) atomicAdd(&sm.CR[pid][idx], cr);
           }
         }
       }
     }
-  }
+  });
   __syncthreads();
 }
 
@@ -693,7 +754,7 @@ __device__ void walk_phase(RoundSmem<M>& sm, int sched) {
 
 // Apply the swaps to orig[] and recount the touched segments.
 template <int M>
-__device__ void apply_phase(RoundSmem<M>& sm, const NMJob& J, int N, int round) {
+__device__ void apply_phase(RoundSmem<M>& sm, const NMJob& J, int N, int round, int* cnt) {
   constexpr int K = M + 1;
   const int tid = threadIdx.x;
   (void)round;
@@ -705,17 +766,16 @@ __device__ void apply_phase(RoundSmem<M>& sm, const NMJob& J, int N, int round) 
       J.orig[v2] = o1;
     }
   }
-  const int nt = sm.ntouched, Kn = sm.K_;
-  for (int t = tid; t < nt; t += NM_THREADS) {
-    const int r = J.touched[t];
-    const uint4 w = J.rec[r];
+  const int Kn = sm.K_;
+  const int lane = tid & 31;
+  for_touched_warp<M>(sm, J, [&](int r, const uint4& w, bool valid) {
     unsigned nb[K];
 #pragma unroll
     for (int xi = 0; xi < K; ++xi) nb[xi] = 0;
 #pragma unroll
     for (int xi = 0; xi < K; ++xi) {
       if (xi >= Kn) break;
-      unsigned bb = rec_byte(w, xi);
+      unsigned bb = valid ? rec_byte(w, xi) : 0u;
       while (bb) {
         const int k = __ffs(bb) - 1;
         bb &= bb - 1;
@@ -726,32 +786,39 @@ __device__ void apply_phase(RoundSmem<M>& sm, const NMJob& J, int N, int round) 
           if (z == dx) nb[z] |= 1u << dk;
       }
     }
+    // non-empty and invalid groups per segment, one shared add per warp
 #pragma unroll
     for (int xi = 0; xi < K; ++xi) {
-      if (xi < Kn && nb[xi]) {
-        atomicAdd(&sm.newpres[xi], 1);
-        if (__popc(nb[xi]) > N) atomicAdd(&sm.newinv[xi], 1);
-      }
+      if (xi >= Kn) break;
+      const unsigned pres = __ballot_sync(FULL, nb[xi] != 0u);
+      const unsigned inv = __ballot_sync(FULL, __popc(nb[xi]) > N);
+      if (lane == 0 && pres) atomicAdd(&sm.newpres[xi], __popc(pres));
+      if (lane == 0 && inv) atomicAdd(&sm.newinv[xi], __popc(inv));
     }
-    J.rec[r] = make_uint4(0u, 0u, 0u, 0u);
-  }
+    if (valid) J.rec[r] = make_uint4(0u, 0u, 0u, 0u);
+  });
   __syncthreads();
   if (tid < Kn) {
-    J.cnt[sm.xseg[tid]] = sm.newinv[tid];
+    cnt[sm.xseg[tid]] = sm.newinv[tid];
     J.zc[sm.xseg[tid]] = J.R - sm.newpres[tid];
   }
   __syncthreads();
 }
 
 template <int M>
-__global__ void __launch_bounds__(NM_THREADS) k_nm_rounds(const NMJob* __restrict__ jobs, int N) {
+__global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __restrict__ jobs, int N,
+                                                              int cnt_in_smem) {
   __shared__ RoundSmem<M> sm;
+  extern __shared__ int smem_cnt[];  // the job's segment counts, when they fit
   const NMJob J = jobs[blockIdx.x];
   const int tid = threadIdx.x;
+  int* cnt = cnt_in_smem ? smem_cnt : J.cnt;
+  if (cnt_in_smem)
+    for (int s = tid; s < J.nseg; s += NM_THREADS) smem_cnt[s] = J.cnt[s];
   if (tid == 0) sm.status = JOB_OK;
   clear_round_smem<M>(sm);
   __syncthreads();
-  select_phase<M>(sm, J);
+  select_phase<M>(sm, J, cnt);
   const int init_size = sm.lsize, init_cnt = sm.ltotal;
   const int MAXITER = J.maxiter > init_size ? J.maxiter : init_size;  // reorder.h:1819
   int round = 1;
@@ -795,15 +862,17 @@ __global__ void __launch_bounds__(NM_THREADS) k_nm_rounds(const NMJob* __restric
     }
     sumE += (unsigned)sm.E;
     sumT += (unsigned)sm.ntouched;
-    apply_phase<M>(sm, J, N, round);
+    apply_phase<M>(sm, J, N, round, cnt);
     clear_round_smem<M>(sm);
     __syncthreads();
     VNM_PHASE(6);
-    select_phase<M>(sm, J);
+    select_phase<M>(sm, J, cnt);
     round += 1;
     if (sm.status != JOB_OK) break;
   }
 #undef VNM_PHASE
+  if (cnt_in_smem)
+    for (int s = tid; s < J.nseg; s += NM_THREADS) J.cnt[s] = smem_cnt[s];
   if (tid == 0) {
     J.res[0] = init_size;
     J.res[1] = sm.lsize;
@@ -980,21 +1049,29 @@ static vnm_status make_job(vnm_ctx* ctx, const Pattern& P, int sched, int maxite
   return VNM_OK;
 }
 
+// Segment counts live in shared memory when they fit beside RoundSmem.
+constexpr size_t CNT_SMEM_MAX = 160u << 10;
+
 template <int M>
-static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, int N) {
-  VNM_LAUNCH(ctx, k_nm_rounds<M>, njobs, NM_THREADS, 0, d_jobs, N);
+static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, int N, int max_nseg) {
+  const size_t bytes = (size_t)max_nseg * sizeof(int);
+  const int in_smem = bytes <= CNT_SMEM_MAX ? 1 : 0;
+  const size_t dyn = in_smem ? bytes : 0;
+  if (dyn > 48u * 1024u)
+    VNM_CUDA_TRY(cudaFuncSetAttribute(k_nm_rounds<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+  VNM_LAUNCH(ctx, k_nm_rounds<M>, njobs, NM_THREADS, dyn, d_jobs, N, in_smem);
   return VNM_OK;
 }
 
-static vnm_status launch_rounds(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, int N, int M) {
+static vnm_status launch_rounds(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, int N, int M, int max_nseg) {
   switch (M) {
-    case 2: return launch_rounds_t<2>(ctx, d_jobs, njobs, N);
-    case 3: return launch_rounds_t<3>(ctx, d_jobs, njobs, N);
-    case 4: return launch_rounds_t<4>(ctx, d_jobs, njobs, N);
-    case 5: return launch_rounds_t<5>(ctx, d_jobs, njobs, N);
-    case 6: return launch_rounds_t<6>(ctx, d_jobs, njobs, N);
-    case 7: return launch_rounds_t<7>(ctx, d_jobs, njobs, N);
-    case 8: return launch_rounds_t<8>(ctx, d_jobs, njobs, N);
+    case 2: return launch_rounds_t<2>(ctx, d_jobs, njobs, N, max_nseg);
+    case 3: return launch_rounds_t<3>(ctx, d_jobs, njobs, N, max_nseg);
+    case 4: return launch_rounds_t<4>(ctx, d_jobs, njobs, N, max_nseg);
+    case 5: return launch_rounds_t<5>(ctx, d_jobs, njobs, N, max_nseg);
+    case 6: return launch_rounds_t<6>(ctx, d_jobs, njobs, N, max_nseg);
+    case 7: return launch_rounds_t<7>(ctx, d_jobs, njobs, N, max_nseg);
+    case 8: return launch_rounds_t<8>(ctx, d_jobs, njobs, N, max_nseg);
   }
   return VNM_ERR_ARG;
 }
@@ -1066,7 +1143,7 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
   if (!d_jobs) return VNM_ERR_NOMEM;
   VNM_CUDA_TRY(cudaMemcpyAsync(d_jobs, hj, sizeof(NMJob) * nsched, cudaMemcpyHostToDevice, ctx->stream));
   VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main0, ctx->stream));
-  VNM_TRY(launch_rounds(ctx, d_jobs, nsched, N, M));
+  VNM_TRY(launch_rounds(ctx, d_jobs, nsched, N, M, P.nseg));
   VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main1, ctx->stream));
   int* hres = ctx->h_pinned;
   for (int s = 0; s < nsched; ++s)
@@ -1337,7 +1414,7 @@ extern "C" vnm_status vnm_nm_reorder_noalloc(int nrows, int nnz, const int* row,
   NMJob* d_job = arena_take<NMJob>(&c, 1);
   if (!d_job) return VNM_ERR_LIMIT;
   VNM_CUDA_TRY(cudaMemcpyAsync(d_job, &hj, sizeof(NMJob), cudaMemcpyHostToDevice, c.stream));
-  VNM_TRY(launch_rounds(&c, d_job, 1, N, M));
+  VNM_TRY(launch_rounds(&c, d_job, 1, N, M, P.nseg));
   VNM_CUDA_TRY(cudaMemcpyAsync(hs, hj.res, sizeof(int) * 16, cudaMemcpyDeviceToHost, c.stream));
   VNM_CUDA_TRY(cudaStreamSynchronize(c.stream));
   if (hs[5] != 0) return VNM_ERR_INTERNAL;
