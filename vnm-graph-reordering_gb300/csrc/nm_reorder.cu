@@ -39,6 +39,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <vector>
 
 #include "common.cuh"
 #include "swap_heap.h"
@@ -1190,6 +1191,178 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
   return VNM_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// Batches: many matrices as one block-diagonal matrix.  Matrix b's ids are
+// shifted by its row offset, so one pattern build covers the whole batch;
+// job b sees the columns of its own diagonal block and the rows it reaches
+// are its own (global ids), so the jobs share the row-record array without
+// overlapping.  All jobs run as the blocks of one persistent launch.
+// ---------------------------------------------------------------------------
+__global__ void k_batch_offset(const int* row, const int* col, const long long* nnz_off, const int* row_off,
+                               const int* nrows, int nmat, long long nnz, int* grow, int* gcol, int* err) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nnz;
+       i += (long long)gridDim.x * blockDim.x) {
+    int lo = 0, hi = nmat - 1;  // last b with nnz_off[b] <= i
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (nnz_off[mid] <= i) lo = mid;
+      else hi = mid - 1;
+    }
+    const int b = lo, R = nrows[b];
+    const int r = row[i], c = col[i];
+    if (r < 0 || r >= R || c < 0 || c >= R) {
+      atomicOr(err, 2);
+      grow[i] = gcol[i] = 0;
+      continue;
+    }
+    if (i > nnz_off[b]) {
+      const int rp = row[i - 1], cp = col[i - 1];
+      if (rp > r || (rp == r && cp >= c)) atomicOr(err, 1);
+    }
+    grow[i] = r + row_off[b];
+    gcol[i] = c + row_off[b];
+  }
+}
+
+__global__ void k_batch_init(const NMJob* jobs, const int* inv0, const int* pres0, const int* seg_off) {
+  const NMJob J = jobs[blockIdx.x];
+  const int so = seg_off[blockIdx.x];
+  for (int i = threadIdx.x; i < J.R; i += blockDim.x) {
+    J.orig[i] = i;
+    if (i < J.nseg) {
+      J.cnt[i] = inv0[so + i];
+      J.zc[i] = J.R - pres0[so + i];
+    }
+  }
+}
+
+__global__ void k_batch_invert(const NMJob* jobs, const int* row_off, int* newpos) {
+  const NMJob J = jobs[blockIdx.x];
+  int* out = newpos + row_off[blockIdx.x];
+  for (int i = threadIdx.x; i < J.R; i += blockDim.x) out[J.orig[i]] = i;
+}
+
+static vnm_status run_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int64_t* nnz_offset, const int* row,
+                            const int* col, const float* val, int N, int M, int sched, int maxiter, int* res5,
+                            int* newpos) {
+  if (!ctx || nmat < 0 || !nrows || !nnz_offset || !res5) return VNM_ERR_ARG;
+  if (M < 2 || M > 8 || N < 1 || N >= M || sched < 0 || sched > 3) return VNM_ERR_ARG;
+  if (nmat == 0) return VNM_OK;
+  std::vector<int> row_off(nmat + 1), seg_off(nmat);
+  long long totR = 0;
+  for (int b = 0; b < nmat; ++b) {
+    if (nrows[b] < 0 || nrows[b] % M != 0 || nnz_offset[b + 1] < nnz_offset[b]) return VNM_ERR_ARG;
+    row_off[b] = (int)totR;
+    seg_off[b] = (int)(totR / M);
+    totR += nrows[b];
+  }
+  row_off[nmat] = (int)totR;
+  const long long nnz = nnz_offset[nmat] - nnz_offset[0];
+  if (nnz_offset[0] != 0 || totR > (1 << 28) || nnz > (1ll << 31) - 1) return VNM_ERR_LIMIT;
+  if (nnz > 0 && (!row || !col || !val)) return VNM_ERR_ARG;
+  const int R = (int)totR, n = (int)nnz;
+  size_t need = pattern_bytes(R, n) + 5 * arena_bytes(n, sizeof(int)) + arena_bytes(nmat + 1, 8) +
+                3 * arena_bytes(nmat + 1, sizeof(int)) + arena_bytes(nmat, sizeof(NMJob)) +
+                2 * arena_bytes(R, sizeof(int)) + arena_bytes(R, sizeof(uint4)) +
+                2 * arena_bytes(R / M + nmat, sizeof(int)) + arena_bytes((size_t)24 * nmat, sizeof(int)) +
+                arena_bytes(R, sizeof(int)) + 8192;
+  VNM_TRY(arena_reserve(ctx, need));
+  VNM_TRY(pinned_reserve(ctx, 256 + (size_t)24 * nmat));
+  VNM_TRY(begin_call(ctx));
+  const int *d_row, *d_col;
+  const float* d_val;
+  VNM_TRY(stage_in(ctx, row, n, VNM_MEM_HOST, &d_row));
+  VNM_TRY(stage_in(ctx, col, n, VNM_MEM_HOST, &d_col));
+  VNM_TRY(stage_in(ctx, val, n, VNM_MEM_HOST, &d_val));
+  long long* d_noff = arena_take<long long>(ctx, nmat + 1);
+  int* d_roff = arena_take<int>(ctx, nmat + 1);
+  int* d_soff = arena_take<int>(ctx, nmat + 1);
+  int* d_nrows = arena_take<int>(ctx, nmat + 1);
+  int* grow = arena_take<int>(ctx, n > 0 ? n : 1);
+  int* gcol = arena_take<int>(ctx, n > 0 ? n : 1);
+  int* err = arena_take<int>(ctx, 1);
+  if (!d_noff || !d_roff || !d_soff || !d_nrows || !grow || !gcol || !err) return VNM_ERR_NOMEM;
+  VNM_CUDA_TRY(cudaMemcpyAsync(d_noff, nnz_offset, sizeof(long long) * (nmat + 1), cudaMemcpyHostToDevice,
+                               ctx->stream));
+  VNM_CUDA_TRY(cudaMemcpyAsync(d_roff, row_off.data(), sizeof(int) * (nmat + 1), cudaMemcpyHostToDevice,
+                               ctx->stream));
+  VNM_CUDA_TRY(cudaMemcpyAsync(d_soff, seg_off.data(), sizeof(int) * nmat, cudaMemcpyHostToDevice, ctx->stream));
+  VNM_CUDA_TRY(cudaMemcpyAsync(d_nrows, nrows, sizeof(int) * nmat, cudaMemcpyHostToDevice, ctx->stream));
+  VNM_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  if (n > 0)
+    VNM_LAUNCH(ctx, k_batch_offset, grid_for(ctx, n), 256, 0, d_row, d_col, d_noff, d_roff, d_nrows, nmat,
+               (long long)n, grow, gcol, err);
+  VNM_CUDA_TRY(cudaMemcpyAsync(ctx->h_pinned, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  VNM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  if (ctx->h_pinned[0] & 2) return VNM_ERR_RANGE;
+  if (ctx->h_pinned[0] & 1) return VNM_ERR_UNSORTED;
+  Pattern P;
+  VNM_TRY(build_pattern(ctx, R, n, grow, gcol, d_val, N, M, P, ctx->h_pinned));
+  // per-job state, one allocation per field for the whole batch
+  int* orig = arena_take<int>(ctx, R > 0 ? R : 1);
+  int* touched = arena_take<int>(ctx, R > 0 ? R : 1);
+  uint4* rec = arena_take<uint4>(ctx, R > 0 ? R : 1);
+  int* cnt = arena_take<int>(ctx, R / M + nmat);
+  int* zc = arena_take<int>(ctx, R / M + nmat);
+  int* res = arena_take<int>(ctx, (size_t)24 * nmat);
+  NMJob* d_jobs = arena_take<NMJob>(ctx, nmat);
+  if (!orig || !touched || !rec || !cnt || !zc || !res || !d_jobs) return VNM_ERR_NOMEM;
+  VNM_CUDA_TRY(cudaMemsetAsync(rec, 0, sizeof(uint4) * (R > 0 ? R : 1), ctx->stream));
+  VNM_CUDA_TRY(cudaMemsetAsync(res, 0, sizeof(int) * 24 * nmat, ctx->stream));
+  std::vector<NMJob> hj(nmat);
+  int max_nseg = 0;
+  for (int b = 0; b < nmat; ++b) {
+    NMJob& J = hj[b];
+    J.R = nrows[b];
+    J.nseg = nrows[b] / M;
+    J.sched = sched;
+    J.maxiter = maxiter;
+    J.cptr = P.cptr + row_off[b];
+    J.crow = P.crow;
+    J.orig = orig + row_off[b];
+    J.cnt = cnt + seg_off[b] + b;
+    J.zc = zc + seg_off[b] + b;
+    J.rec = rec;
+    J.touched = touched + row_off[b];
+    J.res = res + 24 * b;
+    J.trace_pairs = nullptr;
+    J.trace_rounds = nullptr;
+    J.trace_cap_pairs = 0;
+    J.trace_cap_rounds = 0;
+    if (J.nseg > max_nseg) max_nseg = J.nseg;
+  }
+  VNM_CUDA_TRY(cudaMemcpyAsync(d_jobs, hj.data(), sizeof(NMJob) * nmat, cudaMemcpyHostToDevice, ctx->stream));
+  VNM_LAUNCH(ctx, k_batch_init, nmat, 256, 0, d_jobs, P.inv0, P.pres0, d_soff);
+  VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main0, ctx->stream));
+  VNM_TRY(launch_rounds(ctx, d_jobs, nmat, N, M, max_nseg));
+  VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main1, ctx->stream));
+  int* hres = ctx->h_pinned + 256;
+  VNM_CUDA_TRY(cudaMemcpyAsync(hres, res, sizeof(int) * 24 * nmat, cudaMemcpyDeviceToHost, ctx->stream));
+  if (newpos && R > 0) {
+    int* d_np = arena_take<int>(ctx, R);
+    if (!d_np) return VNM_ERR_NOMEM;
+    VNM_LAUNCH(ctx, k_batch_invert, nmat, 256, 0, d_jobs, d_roff, d_np);
+    VNM_CUDA_TRY(cudaMemcpyAsync(newpos, d_np, sizeof(int) * R, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  VNM_TRY(end_call(ctx));
+  VNM_CUDA_TRY(cudaEventElapsedTime(&ctx->main_ms, ctx->ev_main0, ctx->ev_main1));
+  for (int q = 0; q < 16; ++q) ctx->stats[q] = 0;
+  ctx->stats[3] = max_nseg;
+  ctx->stats[4] = nmat;
+  ctx->stats[5] = P.np;
+  for (int b = 0; b < nmat; ++b) {
+    const int* h = hres + 24 * b;
+    if (h[5] != 0) return VNM_ERR_INTERNAL;
+    for (int q = 0; q < 5; ++q) res5[5 * b + q] = h[q];
+    ctx->stats[0] += h[4];
+    ctx->stats[1] += (long long)h[7] + ((long long)h[8] << 31);
+    ctx->stats[2] += (long long)h[9] + ((long long)h[10] << 31);
+    for (int q = 0; q < 7; ++q) ctx->stats[8 + q] += h[16 + q];
+  }
+  return VNM_OK;
+}
+
 }  // namespace vnm
 
 using namespace vnm;
@@ -1324,9 +1497,7 @@ vnm_status vnm_nm_pair_score(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
 vnm_status vnm_nm_reorder_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int64_t* nnz_offset,
                                 const int* row, const int* col, const float* val, int N, int M, int sched,
                                 int nm_maxiter, int* res5, int* newpos) {
-  (void)ctx; (void)nmat; (void)nrows; (void)nnz_offset; (void)row; (void)col; (void)val; (void)N; (void)M;
-  (void)sched; (void)nm_maxiter; (void)res5; (void)newpos;
-  return VNM_ERR_ARG;  // filled in by batch.cu
+  return run_batch(ctx, nmat, nrows, nnz_offset, row, col, val, N, M, sched, nm_maxiter, res5, newpos);
 }
 
 }  // extern "C"

@@ -259,3 +259,29 @@ class Context:
         _check(lib().vnm_vnm_reorder(self.h, m, n, len(r), _ptr(r, None), _ptr(c, None), MEM_HOST, M, V, maxiter,
                                      out.ctypes.data_as(_i32p), newpos.ctypes.data_as(_i32p)), "vnm_vnm_reorder")
         return out, r, c, newpos
+
+    # ---- batches
+    def nm_reorder_batch(self, mats, N, M, sched, nm_maxiter=10, want_newpos=True):
+        """Reorder many matrices [(nrows, row, col, val), ...] in one launch.
+        Returns (res5 [nmat, 5], list of newpos arrays or None)."""
+        nmat = len(mats)
+        nrows = np.array([m[0] for m in mats], np.int32)
+        off = np.zeros(nmat + 1, np.int64)
+        off[1:] = np.cumsum([len(m[1]) for m in mats])
+        row = np.ascontiguousarray(np.concatenate([m[1] for m in mats]) if nmat else np.zeros(0), np.int32)
+        col = np.ascontiguousarray(np.concatenate([m[2] for m in mats]) if nmat else np.zeros(0), np.int32)
+        val = np.ascontiguousarray(np.concatenate([m[3] for m in mats]) if nmat else np.zeros(0), np.float32)
+        res = np.zeros(5 * max(nmat, 1), np.int32)
+        tot = int(nrows.sum()) if nmat else 0
+        newpos = np.zeros(max(tot, 1), np.int32) if want_newpos else None
+        _check(lib().vnm_nm_reorder_batch(self.h, nmat, nrows.ctypes.data_as(_i32p), off.ctypes.data_as(_i64p),
+                                          row.ctypes.data_as(_i32p), col.ctypes.data_as(_i32p),
+                                          val.ctypes.data_as(_f32p), N, M, sched, nm_maxiter,
+                                          res.ctypes.data_as(_i32p),
+                                          newpos.ctypes.data_as(_i32p) if newpos is not None else None),
+               "vnm_nm_reorder_batch")
+        outs = None
+        if want_newpos:
+            ro = np.concatenate([[0], np.cumsum(nrows)])
+            outs = [newpos[ro[b]:ro[b + 1]].copy() for b in range(nmat)]
+        return res[:5 * nmat].reshape(nmat, 5), outs
