@@ -181,6 +181,10 @@ struct RoundSmem {
   int minseg;
   int ntouched;
   int E;            // gathered entries
+  uint4* table;     // shared-memory row records (x, y, z: bitmaps; w: row + 1), or null
+  int ts_max;       // slots of `table` (a power of two) or 0
+  int ts_shift;     // 32 - log2(ts_max)
+  int use_table;    // this round's records are in `table` (else in J.rec)
   int status;
   int nswaps;
   int S[K][M];                 // S_x(k): rows with bit k set and popcount == N+1
@@ -440,7 +444,36 @@ __device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J) {
     sm.E = sm.colpre[KM];
   }
   __syncthreads();
+  if (tid == 0) sm.use_table = sm.ts_max > 0 && sm.E <= (sm.ts_max >> 2) * 3;
+  __syncthreads();
   const int E = sm.E;
+  if (sm.use_table) {
+    // open addressing, linear probing; a slot is claimed by CAS on its row key
+    unsigned* tw = reinterpret_cast<unsigned*>(sm.table);
+    const unsigned mask = (unsigned)sm.ts_max - 1u;
+    for (int e = tid; e < E; e += NM_THREADS) {
+      int lo = 0, hi = KM - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sm.colpre[mid] <= e) lo = mid;
+        else hi = mid - 1;
+      }
+      const int q = lo, xi = q / M, k = q % M;
+      const unsigned key = (unsigned)J.crow[sm.colstart[q] + (e - sm.colpre[q])] + 1u;
+      unsigned h = (key * 2654435761u) >> sm.ts_shift;
+      for (int probe = 0; probe <= (int)mask; ++probe) {
+        const unsigned cur = atomicCAS(&tw[4 * h + 3], 0u, key);
+        if (cur == 0u || cur == key) {
+          atomicOr(&tw[4 * h + (xi >> 2)], (1u << k) << ((xi & 3) * 8));
+          if (cur == 0u) atomicAdd(&sm.ntouched, 1);
+          break;
+        }
+        h = (h + 1u) & mask;
+      }
+    }
+    __syncthreads();
+    return;
+  }
   unsigned* recw = reinterpret_cast<unsigned*>(J.rec);
   // GATHER_U entries per thread per step: their row loads, their bitmap ORs
   // (no result used, so they issue as reductions) and their first-touch
@@ -512,6 +545,24 @@ __device__ __forceinline__ void for_touched_warp(const RoundSmem<M>& sm, const N
   }
 }
 
+// Run f(index, record, valid) over this round's row records: the table
+// slots (index = slot) when the records are in shared memory, else the
+// touched rows (index = row).  Warp-uniform like for_touched_warp.
+template <int M, class F>
+__device__ __forceinline__ void for_rows_warp(const RoundSmem<M>& sm, const NMJob& J, F&& f) {
+  if (sm.use_table) {
+    constexpr int NW = NM_THREADS / 32;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int base = w * 32; base < sm.ts_max; base += NW * 32) {
+      const int slot = base + lane;
+      const uint4 v = sm.table[slot];
+      f(slot, v, v.w != 0u);
+    }
+  } else {
+    for_touched_warp<M>(sm, J, f);
+  }
+}
+
 // Solo terms and pair corrections (fact 3), accumulated with warp votes:
 // for 32 rows at a time, a count over rows of a product of two per-row bit
 // conditions is popc(ballot(first) & ballot(second)), and one lane adds it
@@ -528,7 +579,7 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N) {
   const int Kn = sm.K_;
   const bool self = sm.mode == 2;
   const int lane = threadIdx.x & 31;
-  for_touched_warp<M>(sm, J, [&](int r, const uint4& w, bool valid) {
+  for_rows_warp<M>(sm, J, [&](int r, const uint4& w, bool valid) {
     (void)r;
     unsigned b[K];
     int p[K];
@@ -769,7 +820,7 @@ __device__ void apply_phase(RoundSmem<M>& sm, const NMJob& J, int N, int round, 
   }
   const int Kn = sm.K_;
   const int lane = tid & 31;
-  for_touched_warp<M>(sm, J, [&](int r, const uint4& w, bool valid) {
+  for_rows_warp<M>(sm, J, [&](int r, const uint4& w, bool valid) {
     unsigned nb[K];
 #pragma unroll
     for (int xi = 0; xi < K; ++xi) nb[xi] = 0;
@@ -796,7 +847,10 @@ __device__ void apply_phase(RoundSmem<M>& sm, const NMJob& J, int N, int round, 
       if (lane == 0 && pres) atomicAdd(&sm.newpres[xi], __popc(pres));
       if (lane == 0 && inv) atomicAdd(&sm.newinv[xi], __popc(inv));
     }
-    if (valid) J.rec[r] = make_uint4(0u, 0u, 0u, 0u);
+    if (valid) {
+      if (sm.use_table) sm.table[r] = make_uint4(0u, 0u, 0u, 0u);
+      else J.rec[r] = make_uint4(0u, 0u, 0u, 0u);
+    }
   });
   __syncthreads();
   if (tid < Kn) {
@@ -808,15 +862,24 @@ __device__ void apply_phase(RoundSmem<M>& sm, const NMJob& J, int N, int round, 
 
 template <int M>
 __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __restrict__ jobs, int N,
-                                                              int cnt_in_smem) {
+                                                              int cnt_in_smem, int ts_max) {
   __shared__ RoundSmem<M> sm;
-  extern __shared__ int smem_cnt[];  // the job's segment counts, when they fit
+  // dynamic shared memory: [row-record table: ts_max x 16 B][segment counts]
+  extern __shared__ uint4 smem_dyn[];
+  int* smem_cnt = reinterpret_cast<int*>(smem_dyn + ts_max);
   const NMJob J = jobs[blockIdx.x];
   const int tid = threadIdx.x;
   int* cnt = cnt_in_smem ? smem_cnt : J.cnt;
   if (cnt_in_smem)
     for (int s = tid; s < J.nseg; s += NM_THREADS) smem_cnt[s] = J.cnt[s];
-  if (tid == 0) sm.status = JOB_OK;
+  for (int i = tid; i < ts_max; i += NM_THREADS) smem_dyn[i] = make_uint4(0u, 0u, 0u, 0u);
+  if (tid == 0) {
+    sm.status = JOB_OK;
+    sm.table = ts_max > 0 ? smem_dyn : nullptr;
+    sm.ts_max = ts_max;
+    sm.ts_shift = 32 - (31 - __clz(ts_max > 0 ? ts_max : 1));
+    sm.use_table = 0;
+  }
   clear_round_smem<M>(sm);
   __syncthreads();
   select_phase<M>(sm, J, cnt);
@@ -897,6 +960,9 @@ __global__ void __launch_bounds__(NM_THREADS) k_pair_score(NMJob J, int N, int s
   __shared__ RoundSmem<M> sm;
   clear_round_smem<M>(sm);
   if (threadIdx.x == 0) {
+    sm.table = nullptr;
+    sm.ts_max = 0;
+    sm.use_table = 0;
     sm.xseg[0] = s1;
     sm.xcnt[0] = 0;
     if (s1 == s2) {
@@ -1050,17 +1116,23 @@ static vnm_status make_job(vnm_ctx* ctx, const Pattern& P, int sched, int maxite
   return VNM_OK;
 }
 
-// Segment counts live in shared memory when they fit beside RoundSmem.
-constexpr size_t CNT_SMEM_MAX = 160u << 10;
+// Shared memory beyond RoundSmem: the segment counts when they are small
+// (<= 64 KB), and a row-record table of up to 8192 16-byte slots in what is
+// left of a 200 KB budget.
+constexpr size_t NM_SMEM_BUDGET = 200u << 10;
 
 template <int M>
 static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, int N, int max_nseg) {
-  const size_t bytes = (size_t)max_nseg * sizeof(int);
-  const int in_smem = bytes <= CNT_SMEM_MAX ? 1 : 0;
-  const size_t dyn = in_smem ? bytes : 0;
+  const size_t cbytes = (size_t)max_nseg * sizeof(int);
+  const int in_smem = cbytes <= (64u << 10) ? 1 : 0;
+  const size_t fixed = sizeof(RoundSmem<M>) + (in_smem ? cbytes : 0);
+  int ts = 8192;
+  while (ts >= 1024 && fixed + (size_t)ts * sizeof(uint4) > NM_SMEM_BUDGET) ts >>= 1;
+  if (ts < 1024) ts = 0;
+  const size_t dyn = (size_t)ts * sizeof(uint4) + (in_smem ? cbytes : 0);
   if (dyn > 48u * 1024u)
     VNM_CUDA_TRY(cudaFuncSetAttribute(k_nm_rounds<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-  VNM_LAUNCH(ctx, k_nm_rounds<M>, njobs, NM_THREADS, dyn, d_jobs, N, in_smem);
+  VNM_LAUNCH(ctx, k_nm_rounds<M>, njobs, NM_THREADS, dyn, d_jobs, N, in_smem, ts);
   return VNM_OK;
 }
 
