@@ -191,6 +191,34 @@ vnm_status vnm_vnm_eval(vnm_ctx* ctx, int m, int n, int nnz, const int* row, con
 vnm_status vnm_vnm_reorder(vnm_ctx* ctx, int m, int n, int nnz, int* row, int* col, int mem, int M, int V,
                            int maxiter, int* out5, int* newpos);
 
+/* ---------------------------------------------------------------------------
+ * V:N:M SpMM (replaces the BSR WMMA kernel of kernel/spmm.cu:44-161)
+ * ------------------------------------------------------------------------- */
+
+typedef struct vnm_spmm_matrix vnm_spmm_matrix;
+
+/* Compress a (reordered) sparse matrix into the V:N:M layout the SpMM
+ * kernel reads: 128-row tiles; every non-empty V x M block is cut into
+ * slices of 4 columns with at most 2 nonzeros per row (one slice when the
+ * block satisfies V:N:M, more when it does not, so nothing is dropped);
+ * values are divided by their V-block row's largest magnitude and stored
+ * as `dtype` (1 = BF16, 0 = FP16).  Requires 128 % V == 0, 2 <= M <= 8.
+ * COO in any order.  The result lives in device memory of the context's
+ * GPU until vnm_spmm_free. */
+vnm_status vnm_spmm_compress(vnm_ctx* ctx, int nrows, int nnz, const int* row, const int* col, const float* val,
+                             int mem, int M, int V, int dtype, vnm_spmm_matrix** out);
+
+/* info[0..7] = {nnz, non-empty blocks, blocks that satisfy V:N:M, slices,
+ * slices after padding tiles to K-steps of 4, K-steps, tiles, bytes of A}. */
+vnm_status vnm_spmm_info(const vnm_spmm_matrix* A, long long* info, int n);
+
+/* C (nrows x n, FP32, row-major) = A * B with B (nrows x n, row-major, the
+ * compressed dtype).  n must be a multiple of 64.  mem = where B and C are
+ * (device: 16-byte aligned). */
+vnm_status vnm_spmm_run(vnm_ctx* ctx, const vnm_spmm_matrix* A, const void* B, int n, float* C, int mem);
+
+vnm_status vnm_spmm_free(vnm_spmm_matrix* A);
+
 /* Host helper: the pop order of the SwapPair priority queue of
  * reorder/reorder.h:521-532 (Comparator, reorder/swappair.h:112-120) for n
  * pairs pushed in index order -- the exact emulation the kernels use. */

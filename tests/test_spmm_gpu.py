@@ -1,0 +1,58 @@
+"""V:N:M SpMM on tcgen05 against the FP64 oracle (orc_spmm_f64).
+
+Error measure: max |C - C64| / max |C64| (normwise), tolerance 1e-2 as the
+north star states for BF16/FP16 operands with FP32 accumulation."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-2
+
+
+def _run(ctx, nr, r, c, v, M, V, n, dtype, seed=0):
+    import torch
+    import vnm_gb300
+    tdt = torch.bfloat16 if dtype == "bf16" else torch.float16
+    g = torch.Generator().manual_seed(seed)
+    B = torch.randn((nr, n), generator=g).to(tdt)
+    A = vnm_gb300.SpmmMatrix(ctx, nr, r, c, v, M, V, dtype)
+    C = A.run(B.cuda()).cpu().numpy().astype(np.float64)
+    ref = oracle.spmm_f64(nr, r, c, v.astype(np.float64), B.float().numpy().astype(np.float64))
+    err = np.abs(C - ref).max() / max(np.abs(ref).max(), 1e-30)
+    return err, A.info()
+
+
+def test_spmm_identity_is_exact(ctx):
+    nr = 256
+    idx = np.arange(nr, dtype=np.int32)
+    err, info = _run(ctx, nr, idx, idx, np.ones(nr, np.float32), 4, 64, 128, "bf16")
+    assert err < 1e-6, err
+    assert info["slices"] == info["blocks"] == info["valid_blocks"]
+
+
+@pytest.mark.parametrize("dtype", ["bf16", "fp16"])
+@pytest.mark.parametrize("n", [64, 128, 256])
+def test_spmm_random_matches_fp64(ctx, dtype, n):
+    from vnm_gb300 import synth
+    nr, r, c, v = synth.uniform(384, 0.03, 5)
+    err, info = _run(ctx, nr, r, c, v, 8, 32, n, dtype)
+    assert err < TOL, (err, info)
+
+
+def test_spmm_rmat_blocks_that_violate_vnm(ctx):
+    from vnm_gb300 import synth
+    nr, r, c, v = synth.rmat(11, 12000, 9, "normal")   # dense hubs: many blocks need extra slices
+    err, info = _run(ctx, nr, r, c, v, 4, 64, 128, "bf16")
+    assert info["slices"] > info["valid_blocks"]
+    assert err < TOL, (err, info)
+
+
+def test_spmm_partial_last_tile_and_empty_tiles(ctx):
+    nr = 328   # 3 tiles, the last one partly outside the matrix
+    r = np.array([0, 5, 130, 300, 327], np.int32)
+    c = np.array([3, 320, 9, 4, 327], np.int32)
+    v = np.array([1.5, -2.0, 0.25, 3.0, -1.0], np.float32)
+    err, info = _run(ctx, nr, r, c, v, 8, 64, 64, "bf16")
+    assert err < TOL

@@ -1,0 +1,632 @@
+// V:N:M SpMM on tcgen05 tensor cores: C = A * B with A sparse (the reordered
+// matrix) and B dense, BF16 or FP16 operands, FP32 accumulation.
+//
+// Replaces the reference's BSR WMMA kernel (kernel/spmm.cu:44-161), which
+// runs one warp per 16x16 output tile with wmma m16n16k16 over 16x16 BSR
+// blocks.  Here A is first compressed into its V:N:M layout and the dense
+// products run as tcgen05.mma with the accumulator in tensor memory.
+//
+// Layout (the compressor below builds it on the device):
+//   - rows are cut into tiles of 128 (the MMA's M); V must divide 128, so a
+//     tile holds 128 / V block rows of V rows each.
+//   - every non-empty (block row, segment) block -- V rows x M columns -- is
+//     cut into slices: 4 of its columns, and per row at most 2 nonzeros
+//     among them (2:4 inside the slice).  A block that satisfies V:N:M (at
+//     most 4 nonzero columns, at most 2 nonzeros per row) is one slice;
+//     a block that does not spills into more slices, so no nonzero is
+//     dropped and the product is exact up to the operand rounding.
+//   - 4 slices make one K-step of 16: the A operand of a K-step (128 rows x
+//     16) is stored ready for the MMA (K-major, core matrices of 8 rows x 16
+//     bytes), and the 16 B rows it multiplies are listed by index.
+//   - values are stored divided by their block row's scale (max |a| of the
+//     V rows), and the epilogue multiplies each output row back by it.
+// Kernel: one CTA per (tile, column block of C).  A producer thread streams
+// each K-step's A tile (one bulk copy) and gathers its 16 B rows with TMA
+// tile::gather4 (rows in 128-byte swizzled layout); one thread issues the
+// MMA per K-step; two stages overlap copies with MMAs.  Four warps then read
+// the FP32 accumulator out of tensor memory, scale and store it.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "sm100_ptx.cuh"
+
+struct vnm_spmm_matrix {
+  int device = 0;
+  int R = 0, M = 0, V = 0, dtype = 1;  // dtype: 1 bf16, 0 f16
+  int ntiles = 0, nsteps = 0;
+  long long nnz = 0, groups = 0, slices = 0, slices_padded = 0, valid_blocks = 0;
+  int* tile_step = nullptr;  // [ntiles + 1]
+  int* cols = nullptr;       // [nsteps * 16]
+  unsigned char* a = nullptr;  // [nsteps * 4096]
+  float* rscale = nullptr;   // [ntiles * 128]
+  void* base = nullptr;      // one allocation for all of the above
+};
+
+namespace vnm {
+
+constexpr int SP_TM = 128;        // rows per tile (MMA M)
+constexpr int SP_KSTEP_BYTES = 4096;
+constexpr int SP_THREADS = 128;
+constexpr uint32_t SP_WAIT_LIMIT = 1u << 22;  // polls before a wait gives up
+
+static inline int sp_grid(const vnm_ctx* ctx, long long n, int nt = 256) {
+  long long g = (n + nt - 1) / nt, cap = (long long)ctx->num_sms * 16;
+  if (g > cap) g = cap;
+  return g < 1 ? 1 : (int)g;
+}
+
+static inline int sp_bits(long long v) {
+  int b = 1;
+  while ((1ll << b) <= v) ++b;
+  return b;
+}
+
+// ---------------------------------------------------------------------------
+// Compressor
+// ---------------------------------------------------------------------------
+__global__ void k_cmp_keys(const int* row, const int* col, int nnz, int M, int V, int nseg,
+                           unsigned long long* keys) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += gridDim.x * blockDim.x) {
+    const int r = row[i], c = col[i];
+    const unsigned long long blk = (unsigned long long)(r / V) * nseg + (unsigned)(c / M);
+    keys[i] = (blk * V + (unsigned)(r % V)) * M + (unsigned)(c % M);
+  }
+}
+
+__global__ void k_cmp_heads(const unsigned long long* keys, int nnz, int VM, int* flag) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += gridDim.x * blockDim.x)
+    flag[i] = (i == 0) || (keys[i] / VM != keys[i - 1] / VM);
+}
+
+__global__ void k_cmp_group_start(const int* flag_scan, const unsigned long long* keys, int nnz, int VM,
+                                  int* gstart) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += gridDim.x * blockDim.x)
+    if (i == 0 || keys[i] / VM != keys[i - 1] / VM) gstart[flag_scan[i]] = i;
+}
+
+__global__ void k_cmp_scale(const int* row, const float* val, int nnz, int V, unsigned* bmax) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += gridDim.x * blockDim.x) {
+    const float a = fabsf(val[i]);
+    if (a > 0.f) atomicMax(&bmax[row[i] / V], __float_as_uint(a));
+  }
+}
+
+// The slices of one block, formed greedily: take the (up to) 4 columns with
+// the most remaining nonzeros (ties to the lower offset), give each row at
+// most 2 of its remaining nonzeros among them (lowest offsets first), repeat
+// until the block is empty.  `emit(sel, nsel, chosen)` is called once per
+// slice with the chosen offsets and must remove what each row takes (the
+// lowest two bits of mask & chosen).  Row masks: bit o = column offset o.
+template <class Emit>
+__device__ __forceinline__ int block_slices(unsigned char* mask, int nr, int M, Emit&& emit) {
+  int ns = 0;
+  for (int guard = 0; guard < 64; ++guard) {
+    int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    bool any = false;
+    for (int r = 0; r < nr; ++r)
+      for (int o = 0; o < M; ++o)
+        if ((mask[r] >> o) & 1u) {
+          cnt[o]++;
+          any = true;
+        }
+    if (!any) break;
+    int sel[4], nsel = 0;
+    unsigned chosen = 0;
+    for (int pick = 0; pick < 4; ++pick) {
+      int best = -1;
+      for (int o = 0; o < M; ++o)
+        if (!((chosen >> o) & 1u) && cnt[o] > 0 && (best < 0 || cnt[o] > cnt[best])) best = o;
+      if (best < 0) break;
+      chosen |= 1u << best;
+    }
+    for (int o = 0; o < M; ++o)
+      if ((chosen >> o) & 1u) sel[nsel++] = o;
+    emit(sel, nsel, chosen);
+    ++ns;
+  }
+  return ns;
+}
+
+__device__ __forceinline__ unsigned low2(unsigned m) {  // the lowest two set bits of m
+  const unsigned a = m & (0u - m);
+  const unsigned rest = m & ~a;
+  return a | (rest & (0u - rest));
+}
+
+// Count slices per block and per tile.
+__global__ void k_cmp_count(const unsigned long long* skeys, const int* gstart, int ngroups, int nnz, int M, int V,
+                            int nseg, int* gsl, int* tile_raw, int* valid_blocks) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += gridDim.x * blockDim.x) {
+    const int b0 = gstart[g], b1 = g + 1 < ngroups ? gstart[g + 1] : nnz;
+    unsigned char mask[128];
+    int nr = 0, lastr = -1;
+    for (int i = b0; i < b1; ++i) {
+      const unsigned long long k = skeys[i];
+      const int rr = (int)((k / M) % V), o = (int)(k % M);
+      if (rr != lastr) {
+        mask[nr++] = 0;
+        lastr = rr;
+      }
+      mask[nr - 1] |= (unsigned char)(1u << o);
+    }
+    int valid = 1;
+    unsigned orb = 0;
+    for (int r = 0; r < nr; ++r) {
+      orb |= mask[r];
+      if (__popc(mask[r]) > 2) valid = 0;
+    }
+    if (__popc(orb) > 4) valid = 0;
+    const int ns = block_slices(mask, nr, M, [&](const int*, int, unsigned chosen) {
+      for (int r = 0; r < nr; ++r) mask[r] &= ~(unsigned char)low2(mask[r] & chosen);
+    });
+    gsl[g] = ns;
+    const long long blk = (long long)(skeys[b0] / ((unsigned long long)V * M));
+    const int brow = (int)(blk / nseg);
+    atomicAdd(&tile_raw[(brow * V) / SP_TM], ns);
+    if (valid) atomicAdd(valid_blocks, 1);
+  }
+}
+
+__global__ void k_cmp_pad(const int* tile_raw, int ntiles, int* tile_pad) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x)
+    tile_pad[t] = (tile_raw[t] + 3) & ~3;
+}
+
+template <class T>
+__device__ __forceinline__ T to_t(float x);
+template <>
+__device__ __forceinline__ __nv_bfloat16 to_t<__nv_bfloat16>(float x) {
+  return __float2bfloat16_rn(x);
+}
+template <>
+__device__ __forceinline__ __half to_t<__half>(float x) {
+  return __float2half_rn(x);
+}
+
+// Write every block's slices: B-row indices and A values in MMA layout.
+template <class T>
+__global__ void k_cmp_fill(const unsigned long long* skeys, const int* spos, const float* val, const int* gstart,
+                           int ngroups, int nnz, int M, int V, int nseg, const int* gofs, const int* tile_base,
+                           const int* tile_rawbase, const unsigned* bmax, int* cols, unsigned char* a) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += gridDim.x * blockDim.x) {
+    const int b0 = gstart[g], b1 = g + 1 < ngroups ? gstart[g + 1] : nnz;
+    const long long blk = (long long)(skeys[b0] / ((unsigned long long)V * M));
+    const int brow = (int)(blk / nseg), seg = (int)(blk % nseg);
+    const int t = (brow * V) / SP_TM;
+    const float scale = bmax[brow] ? __uint_as_float(bmax[brow]) : 1.0f;
+    const float inv = 1.0f / scale;
+    unsigned char mask[128], orig[128];
+    int rowin[128], first[128];
+    int nr = 0, lastr = -1;
+    for (int i = b0; i < b1; ++i) {
+      const unsigned long long k = skeys[i];
+      const int rr = (int)((k / M) % V), o = (int)(k % M);
+      if (rr != lastr) {
+        rowin[nr] = rr;
+        first[nr] = i;
+        mask[nr] = 0;
+        ++nr;
+        lastr = rr;
+      }
+      mask[nr - 1] |= (unsigned char)(1u << o);
+    }
+    for (int r = 0; r < nr; ++r) orig[r] = mask[r];
+    int si = tile_base[t] + (gofs[g] - tile_rawbase[t]);  // this block's first slice
+    block_slices(mask, nr, M, [&](const int* sel, int nsel, unsigned chosen) {
+      const int ks = si >> 2, j = si & 3;
+      for (int q = 0; q < 4; ++q) cols[ks * 16 + 4 * j + q] = seg * M + sel[q < nsel ? q : 0];
+      unsigned char* tile = a + (size_t)ks * SP_KSTEP_BYTES;
+      for (int r = 0; r < nr; ++r) {
+        const unsigned take = low2(mask[r] & chosen);
+        if (!take) continue;
+        mask[r] &= ~(unsigned char)take;
+        const int rt = (brow * V - t * SP_TM) + rowin[r];  // row inside the tile
+        unsigned tt = take;
+        while (tt) {
+          const int o = __ffs(tt) - 1;
+          tt &= tt - 1;
+          int kk = 0;
+          while (sel[kk] != o) ++kk;
+          const int e = spos[first[r] + __popc(orig[r] & ((1u << o) - 1u))];
+          const int k = 4 * j + kk;
+          const int off = (rt >> 3) * 256 + (k >> 3) * 128 + (rt & 7) * 16 + (k & 7) * 2;
+          *reinterpret_cast<T*>(tile + off) = to_t<T>(val[e] * inv);
+        }
+      }
+      ++si;
+    });
+  }
+}
+
+__global__ void k_cmp_rscale(const unsigned* bmax, int ntiles, int R, int V, float* rscale, const int* tile_base,
+                             int* tile_step) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ntiles * SP_TM; i += gridDim.x * blockDim.x) {
+    const unsigned m = i < R ? bmax[i / V] : 0u;
+    rscale[i] = m ? __uint_as_float(m) : 1.0f;
+    if (i <= ntiles) tile_step[i] = tile_base[i] >> 2;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// SpMM kernel
+// ---------------------------------------------------------------------------
+struct SpmmArgs {
+  const int* tile_step;
+  const int* cols;
+  const unsigned char* a;
+  const float* rscale;
+  float* C;
+  int R, n, ldc;
+  uint32_t idesc;
+  int* err;
+};
+
+constexpr int SP_STAGES = 2;
+
+template <int NT>
+struct SpmmSmem {
+  static constexpr int B_BYTES = 16 * NT * 2;  // K=16 rows x NT columns, 16-bit
+  alignas(1024) unsigned char b[SP_STAGES][B_BYTES];
+  alignas(1024) unsigned char a[SP_STAGES][SP_KSTEP_BYTES];
+  alignas(8) uint64_t full[SP_STAGES];
+  alignas(8) uint64_t empty[SP_STAGES];
+  alignas(8) uint64_t done;
+  uint32_t tmem_base;
+  int abort;
+};
+
+template <int NT>
+__global__ void __launch_bounds__(SP_THREADS, 1)
+    k_spmm_vnm(const __grid_constant__ CUtensorMap tmap, SpmmArgs p) {
+  extern __shared__ unsigned char sp_raw[];
+  SpmmSmem<NT>& sm = *reinterpret_cast<SpmmSmem<NT>*>(
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(sp_raw) + 1023) & ~uintptr_t(1023)));
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int t = blockIdx.x;
+  const int n0 = blockIdx.y * NT;
+  const int s0 = p.tile_step[t], nsteps = p.tile_step[t + 1] - s0;
+
+  if (tid == 0) {
+    for (int s = 0; s < SP_STAGES; ++s) {
+      ptx::mbar_init(&sm.full[s], 1);
+      ptx::mbar_init(&sm.empty[s], 1);
+    }
+    ptx::mbar_init(&sm.done, 1);
+    sm.abort = 0;
+    ptx::fence_mbar_init();
+    ptx::prefetch_tmap(&tmap);
+  }
+  if (warp == 0) {
+    ptx::tmem_alloc(&sm.tmem_base, NT);
+    ptx::tmem_relinquish();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = sm.tmem_base;
+
+  int issued = 0;  // K-steps whose copies were issued (producer thread)
+  if (nsteps > 0) {
+    if (tid == 0) {
+      // producer: A tile by bulk copy, 16 B rows by gather4 (64 columns each)
+      for (int i = 0; i < nsteps; ++i) {
+        const int s = i % SP_STAGES;
+        if (i >= SP_STAGES && !ptx::mbar_wait(&sm.empty[s], ((i / SP_STAGES) - 1) & 1, SP_WAIT_LIMIT)) {
+          atomicOr(p.err, 1);
+          sm.abort = 1;
+          break;
+        }
+        ptx::mbar_arrive_expect_tx(&sm.full[s], SP_KSTEP_BYTES + 16 * NT * 2);
+        ptx::bulk_g2s(sm.a[s], p.a + (size_t)(s0 + i) * SP_KSTEP_BYTES, SP_KSTEP_BYTES, &sm.full[s]);
+        const int* c = p.cols + (size_t)(s0 + i) * 16;
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+          const int y0 = c[4 * g], y1 = c[4 * g + 1], y2 = c[4 * g + 2], y3 = c[4 * g + 3];
+#pragma unroll
+          for (int h = 0; h < NT / 64; ++h) {
+            // atom (k block g/2, n block h): 8 k-rows x 128 bytes; rows 4(g%2)..
+            unsigned char* dst = sm.b[s] + h * 2048 + (g >> 1) * 1024 + (g & 1) * 512;
+            ptx::tma_gather4(dst, &tmap, n0 + 64 * h, y0, y1, y2, y3, &sm.full[s]);
+          }
+        }
+        issued = i + 1;
+      }
+    } else if (tid == 32) {
+      // MMA issuer
+      for (int i = 0; i < nsteps; ++i) {
+        const int s = i % SP_STAGES;
+        if (!ptx::mbar_wait(&sm.full[s], (i / SP_STAGES) & 1, SP_WAIT_LIMIT)) {
+          atomicOr(p.err, 2);
+          sm.abort = 1;
+          break;
+        }
+        ptx::tc_fence_after();
+        const uint64_t adesc = ptx::smem_desc(ptx::smem_addr(sm.a[s]), 128, 256, 0);
+        const uint64_t bdesc = ptx::smem_desc(ptx::smem_addr(sm.b[s]), 2048, 1024, 2);
+        ptx::mma_f16(tmem, adesc, bdesc, p.idesc, i > 0 ? 1u : 0u);
+        ptx::mma_commit(&sm.empty[s]);
+      }
+      ptx::mma_commit(&sm.done);
+    }
+    __syncwarp();
+    // everybody waits for the last MMA
+    bool ok = ptx::mbar_wait(&sm.done, 0, SP_WAIT_LIMIT);
+    if (!ok && tid == 0) atomicOr(p.err, 4);
+    if (tid == 0 && issued < nsteps && issued > 0) {
+      // the producer stopped early: let its last copies land before exit
+      for (int i = (issued > SP_STAGES ? issued - SP_STAGES : 0); i < issued; ++i)
+        ptx::mbar_wait(&sm.full[i % SP_STAGES], (i / SP_STAGES) & 1, SP_WAIT_LIMIT);
+    }
+    __syncthreads();
+    ptx::tc_fence_after();
+    if (ok && !sm.abort) {
+      const int row = t * SP_TM + warp * 32 + lane;
+      const float sc = row < p.R ? p.rscale[row] : 0.f;
+#pragma unroll 1
+      for (int c0 = 0; c0 < NT; c0 += 32) {
+        uint32_t v[32];
+        ptx::tmem_ld_32x32b_x32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+        ptx::tmem_ld_wait();
+        if (row < p.R) {
+          float4* dst = reinterpret_cast<float4*>(p.C + (size_t)row * p.ldc + n0 + c0);
+#pragma unroll
+          for (int q = 0; q < 8; ++q)
+            dst[q] = make_float4(__uint_as_float(v[4 * q]) * sc, __uint_as_float(v[4 * q + 1]) * sc,
+                                 __uint_as_float(v[4 * q + 2]) * sc, __uint_as_float(v[4 * q + 3]) * sc);
+        }
+      }
+    }
+  } else {
+    // an empty tile: C rows are zero
+    const int row = t * SP_TM + warp * 32 + lane;
+    if (row < p.R)
+      for (int c = 0; c < NT; c += 4)
+        *reinterpret_cast<float4*>(p.C + (size_t)row * p.ldc + n0 + c) = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) ptx::tmem_dealloc(tmem, NT);
+}
+
+// ---------------------------------------------------------------------------
+// Host
+// ---------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+    else
+      (void)cudaGetLastError();
+  }
+  return fn;
+}
+
+template <class T>
+static vnm_status compress_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, const int* d_col, const float* d_val,
+                             int M, int V, vnm_spmm_matrix* out) {
+  const int nseg = (R + M - 1) / M;
+  const int nbrow = (R + V - 1) / V;
+  const int ntiles = (R + SP_TM - 1) / SP_TM;
+  int* h = ctx->h_pinned;
+  unsigned long long* keys = arena_take<unsigned long long>(ctx, nnz > 0 ? nnz : 1);
+  int* flag = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
+  int* gstart = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
+  int* gsl = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
+  int* gofs = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
+  int* tile_raw = arena_take<int>(ctx, ntiles + 1);
+  int* tile_pad = arena_take<int>(ctx, ntiles + 1);
+  int* tile_base = arena_take<int>(ctx, ntiles + 1);
+  int* tile_rawbase = arena_take<int>(ctx, ntiles + 1);
+  unsigned* bmax = arena_take<unsigned>(ctx, nbrow + 1);
+  int* counters = arena_take<int>(ctx, 4);
+  if (!keys || !flag || !gstart || !gsl || !gofs || !tile_raw || !tile_pad || !tile_base || !tile_rawbase ||
+      !bmax || !counters)
+    return VNM_ERR_NOMEM;
+  VNM_CUDA_TRY(cudaMemsetAsync(tile_raw, 0, sizeof(int) * (ntiles + 1), ctx->stream));
+  VNM_CUDA_TRY(cudaMemsetAsync(tile_pad, 0, sizeof(int) * (ntiles + 1), ctx->stream));
+  VNM_CUDA_TRY(cudaMemsetAsync(bmax, 0, sizeof(unsigned) * (nbrow + 1), ctx->stream));
+  VNM_CUDA_TRY(cudaMemsetAsync(counters, 0, sizeof(int) * 4, ctx->stream));
+  int ngroups = 0;
+  unsigned long long* skeys = keys;
+  int* spos = nullptr;
+  if (nnz > 0) {
+    VNM_LAUNCH(ctx, k_cmp_keys, sp_grid(ctx, nnz), 256, 0, d_row, d_col, nnz, M, V, nseg, keys);
+    const long long maxkey = ((long long)nbrow * nseg) * V * M;
+    VNM_TRY(radix_sort_u64(ctx, keys, nullptr, nnz, sp_bits(maxkey), &skeys, &spos));
+    VNM_LAUNCH(ctx, k_cmp_heads, sp_grid(ctx, nnz), 256, 0, skeys, nnz, V * M, flag);
+    VNM_TRY(exclusive_scan(ctx, flag, flag, nnz, counters));
+    VNM_LAUNCH(ctx, k_cmp_group_start, sp_grid(ctx, nnz), 256, 0, flag, skeys, nnz, V * M, gstart);
+    VNM_LAUNCH(ctx, k_cmp_scale, sp_grid(ctx, nnz), 256, 0, d_row, d_val, nnz, V, bmax);
+    VNM_CUDA_TRY(cudaMemcpyAsync(h, counters, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    VNM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    ngroups = h[0];
+  }
+  if (ngroups > 0) {
+    VNM_LAUNCH(ctx, k_cmp_count, sp_grid(ctx, ngroups, 128), 128, 0, skeys, gstart, ngroups, nnz, M, V, nseg, gsl,
+               tile_raw, counters + 1);
+    VNM_TRY(exclusive_scan(ctx, gsl, gofs, ngroups, counters + 2));
+  }
+  VNM_LAUNCH(ctx, k_cmp_pad, sp_grid(ctx, ntiles), 256, 0, tile_raw, ntiles, tile_pad);
+  VNM_TRY(exclusive_scan(ctx, tile_pad, tile_base, ntiles + 1, nullptr));
+  VNM_TRY(exclusive_scan(ctx, tile_raw, tile_rawbase, ntiles + 1, nullptr));
+  VNM_CUDA_TRY(cudaMemcpyAsync(h, tile_base + ntiles, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  VNM_CUDA_TRY(cudaMemcpyAsync(h + 1, counters + 1, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  VNM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  const int padded = h[0];
+  out->valid_blocks = h[1];
+  out->slices = ngroups > 0 ? h[2] : 0;
+  out->slices_padded = padded;
+  out->groups = ngroups;
+  out->nsteps = padded / 4;
+  out->ntiles = ntiles;
+  // the matrix's own storage (kept across calls)
+  const size_t b_step = arena_bytes(ntiles + 1, 4), b_cols = arena_bytes((size_t)out->nsteps * 16 + 1, 4),
+               b_a = arena_bytes((size_t)out->nsteps * SP_KSTEP_BYTES + 16, 1),
+               b_sc = arena_bytes((size_t)ntiles * SP_TM, 4);
+  void* base = nullptr;
+  VNM_CUDA_TRY(cudaMalloc(&base, b_step + b_cols + b_a + b_sc));
+  out->base = base;
+  char* pb = static_cast<char*>(base);
+  out->tile_step = reinterpret_cast<int*>(pb);
+  out->cols = reinterpret_cast<int*>(pb + b_step);
+  out->a = reinterpret_cast<unsigned char*>(pb + b_step + b_cols);
+  out->rscale = reinterpret_cast<float*>(pb + b_step + b_cols + b_a);
+  VNM_CUDA_TRY(cudaMemsetAsync(out->cols, 0, b_cols, ctx->stream));
+  VNM_CUDA_TRY(cudaMemsetAsync(out->a, 0, b_a, ctx->stream));
+  if (ngroups > 0)
+    VNM_LAUNCH(ctx, k_cmp_fill<T>, sp_grid(ctx, ngroups, 128), 128, 0, skeys, spos, d_val, gstart, ngroups, nnz, M,
+               V, nseg, gofs, tile_base, tile_rawbase, bmax, out->cols, out->a);
+  VNM_LAUNCH(ctx, k_cmp_rscale, sp_grid(ctx, (long long)ntiles * SP_TM), 256, 0, bmax, ntiles, R, V, out->rscale,
+             tile_base, out->tile_step);
+  return VNM_OK;
+}
+
+template <int NT>
+static vnm_status launch_spmm(vnm_ctx* ctx, const vnm_spmm_matrix* A, const CUtensorMap& tmap, SpmmArgs& p) {
+  // at least 100 KB so that at most two CTAs share an SM: two NT <= 256
+  // column accumulators fit the SM's 512 tensor-memory columns, so the
+  // allocation never has to wait for another CTA
+  size_t smem = sizeof(SpmmSmem<NT>) + 1024;
+  if (smem < (100u << 10)) smem = 100u << 10;
+  VNM_CUDA_TRY(cudaFuncSetAttribute(k_spmm_vnm<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  p.idesc = ptx::idesc_f16(A->dtype == 1 ? 1u : 0u, 0u, 1u, SP_TM, NT);
+  dim3 grid(A->ntiles, p.n / NT);
+  VNM_LAUNCH(ctx, k_spmm_vnm<NT>, grid, SP_THREADS, smem, tmap, p);
+  return VNM_OK;
+}
+
+}  // namespace vnm
+
+using namespace vnm;
+
+extern "C" {
+
+vnm_status vnm_spmm_compress(vnm_ctx* ctx, int nrows, int nnz, const int* row, const int* col, const float* val,
+                             int mem, int M, int V, int dtype, vnm_spmm_matrix** out) {
+  if (!ctx || !out || nrows <= 0 || nnz < 0 || M < 2 || M > 8 || V < 1 || (SP_TM % V) != 0) return VNM_ERR_ARG;
+  if (dtype != 0 && dtype != 1) return VNM_ERR_ARG;
+  if (mem != VNM_MEM_HOST && mem != VNM_MEM_DEVICE) return VNM_ERR_ARG;
+  if (nnz > 0 && (!row || !col || !val)) return VNM_ERR_ARG;
+  *out = nullptr;
+  const int ntiles = (nrows + SP_TM - 1) / SP_TM;
+  size_t need = 3 * arena_bytes(nnz, 4) + 8 * arena_bytes(nnz, 8) + 6 * arena_bytes(nnz, 4) +
+                4 * arena_bytes(ntiles + 1, 4) + arena_bytes(nrows / V + 2, 4) + radix_sort_scratch_bytes(nnz) +
+                4 * scan_scratch_bytes(nnz > ntiles ? nnz + 1 : ntiles + 1) + 8192;
+  VNM_TRY(arena_reserve(ctx, need));
+  VNM_TRY(pinned_reserve(ctx, 64));
+  VNM_TRY(begin_call(ctx));
+  const int *d_row, *d_col;
+  const float* d_val;
+  VNM_TRY(stage_in(ctx, row, nnz, mem, &d_row));
+  VNM_TRY(stage_in(ctx, col, nnz, mem, &d_col));
+  VNM_TRY(stage_in(ctx, val, nnz, mem, &d_val));
+  vnm_spmm_matrix* A = new vnm_spmm_matrix();
+  A->device = ctx->device;
+  A->R = nrows;
+  A->M = M;
+  A->V = V;
+  A->dtype = dtype;
+  A->nnz = nnz;
+  vnm_status st = dtype == 1 ? compress_t<__nv_bfloat16>(ctx, nrows, nnz, d_row, d_col, d_val, M, V, A)
+                             : compress_t<__half>(ctx, nrows, nnz, d_row, d_col, d_val, M, V, A);
+  if (st == VNM_OK) st = end_call(ctx);
+  if (st != VNM_OK) {
+    if (A->base) cudaFree(A->base);
+    delete A;
+    return st;
+  }
+  *out = A;
+  return VNM_OK;
+}
+
+vnm_status vnm_spmm_info(const vnm_spmm_matrix* A, long long* info, int n) {
+  if (!A || !info) return VNM_ERR_ARG;
+  const long long v[8] = {A->nnz, A->groups, A->valid_blocks, A->slices, A->slices_padded, A->nsteps, A->ntiles,
+                          (long long)A->nsteps * SP_KSTEP_BYTES};
+  for (int i = 0; i < n && i < 8; ++i) info[i] = v[i];
+  return VNM_OK;
+}
+
+vnm_status vnm_spmm_free(vnm_spmm_matrix* A) {
+  if (!A) return VNM_ERR_ARG;
+  if (A->base) {
+    cudaSetDevice(A->device);
+    cudaFree(A->base);
+  }
+  delete A;
+  return VNM_OK;
+}
+
+vnm_status vnm_spmm_run(vnm_ctx* ctx, const vnm_spmm_matrix* A, const void* B, int n, float* C, int mem) {
+  if (!ctx || !A || !B || !C || n <= 0 || (n % 64) != 0) return VNM_ERR_ARG;
+  if (mem != VNM_MEM_HOST && mem != VNM_MEM_DEVICE) return VNM_ERR_ARG;
+  if (A->device != ctx->device) return VNM_ERR_ARG;
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return VNM_ERR_CUDA;
+  const size_t bbytes = (size_t)A->R * n * 2, cbytes = (size_t)A->R * n * sizeof(float);
+  VNM_TRY(arena_reserve(ctx, (mem == VNM_MEM_HOST ? bbytes + cbytes : 0) + 4096));
+  VNM_TRY(pinned_reserve(ctx, 64));
+  VNM_TRY(begin_call(ctx));
+  const void* dB = B;
+  float* dC = C;
+  if (mem == VNM_MEM_HOST) {
+    void* tb = arena_take<unsigned char>(ctx, bbytes);
+    dC = arena_take<float>(ctx, (size_t)A->R * n);
+    if (!tb || !dC) return VNM_ERR_NOMEM;
+    VNM_CUDA_TRY(cudaMemcpyAsync(tb, B, bbytes, cudaMemcpyHostToDevice, ctx->stream));
+    dB = tb;
+  }
+  if ((reinterpret_cast<uintptr_t>(dB) & 15) != 0 || (reinterpret_cast<uintptr_t>(dC) & 15) != 0)
+    return VNM_ERR_ARG;
+  CUtensorMap tmap;
+  const cuuint64_t gdim[2] = {(cuuint64_t)n, (cuuint64_t)A->R};
+  const cuuint64_t gstride[1] = {(cuuint64_t)n * 2};
+  const cuuint32_t box[2] = {64, 1};
+  const cuuint32_t estr[2] = {1, 1};
+  CUresult cr = enc(&tmap, A->dtype == 1 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2,
+                    const_cast<void*>(dB), gdim, gstride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (cr != CUDA_SUCCESS) return VNM_ERR_ARG;
+  int* err = arena_take<int>(ctx, 1);
+  if (!err) return VNM_ERR_NOMEM;
+  VNM_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  SpmmArgs p;
+  p.tile_step = A->tile_step;
+  p.cols = A->cols;
+  p.a = A->a;
+  p.rscale = A->rscale;
+  p.C = dC;
+  p.R = A->R;
+  p.n = n;
+  p.ldc = n;
+  p.err = err;
+  VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main0, ctx->stream));
+  if (n % 256 == 0) VNM_TRY(launch_spmm<256>(ctx, A, tmap, p));
+  else if (n % 128 == 0) VNM_TRY(launch_spmm<128>(ctx, A, tmap, p));
+  else VNM_TRY(launch_spmm<64>(ctx, A, tmap, p));
+  VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main1, ctx->stream));
+  VNM_CUDA_TRY(cudaMemcpyAsync(ctx->h_pinned, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  if (mem == VNM_MEM_HOST)
+    VNM_CUDA_TRY(cudaMemcpyAsync(C, dC, cbytes, cudaMemcpyDeviceToHost, ctx->stream));
+  VNM_TRY(end_call(ctx));
+  VNM_CUDA_TRY(cudaEventElapsedTime(&ctx->main_ms, ctx->ev_main0, ctx->ev_main1));
+  if (ctx->h_pinned[0] != 0) return VNM_ERR_INTERNAL;
+  return VNM_OK;
+}
+
+}  // extern "C"

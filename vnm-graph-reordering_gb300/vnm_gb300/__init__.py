@@ -285,3 +285,59 @@ class Context:
             ro = np.concatenate([[0], np.cumsum(nrows)])
             outs = [newpos[ro[b]:ro[b + 1]].copy() for b in range(nmat)]
         return res[:5 * nmat].reshape(nmat, 5), outs
+
+
+class SpmmMatrix:
+    """A matrix compressed into the V:N:M layout of the SpMM kernel."""
+
+    def __init__(self, ctx, nrows, row, col, val, M, V, dtype="bf16"):
+        L = lib()
+        if not hasattr(L, "_spmm_typed"):
+            L.vnm_spmm_compress.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, ctypes.c_int,
+                                            ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp)]
+            L.vnm_spmm_info.argtypes = [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]
+            L.vnm_spmm_run.argtypes = [_vp, _vp, _vp, ctypes.c_int, _vp, ctypes.c_int]
+            L.vnm_spmm_free.argtypes = [_vp]
+            L._spmm_typed = True
+        self.ctx = ctx
+        self.nrows = nrows
+        self.dtype = dtype
+        pr, pc, pv, mem, nnz, keep = ctx._arrays(row, col, val)
+        h = ctypes.c_void_p()
+        _check(L.vnm_spmm_compress(ctx.h, nrows, nnz, pr, pc, pv, mem, M, V, 1 if dtype == "bf16" else 0,
+                                   ctypes.byref(h)), "vnm_spmm_compress")
+        self.h = h
+
+    def info(self):
+        out = (ctypes.c_longlong * 8)()
+        _check(lib().vnm_spmm_info(self.h, out, 8), "vnm_spmm_info")
+        keys = ("nnz", "blocks", "valid_blocks", "slices", "slices_padded", "ksteps", "tiles", "a_bytes")
+        return dict(zip(keys, list(out)))
+
+    def run(self, B, C=None):
+        """B: torch CUDA tensor (nrows x n, bf16/f16) or numpy uint16 view; returns C (fp32)."""
+        if hasattr(B, "is_cuda") and B.is_cuda:
+            import torch
+            n = B.shape[1]
+            if C is None:
+                C = torch.empty((self.nrows, n), dtype=torch.float32, device=B.device)
+            _check(lib().vnm_spmm_run(self.ctx.h, self.h, ctypes.c_void_p(B.data_ptr()), n,
+                                      ctypes.c_void_p(C.data_ptr()), MEM_DEVICE), "vnm_spmm_run")
+            return C
+        B = np.ascontiguousarray(B)
+        n = B.shape[1]
+        C = np.zeros((self.nrows, n), np.float32)
+        _check(lib().vnm_spmm_run(self.ctx.h, self.h, ctypes.c_void_p(B.ctypes.data), n,
+                                  ctypes.c_void_p(C.ctypes.data), MEM_HOST), "vnm_spmm_run")
+        return C
+
+    def close(self):
+        if self.h:
+            lib().vnm_spmm_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
