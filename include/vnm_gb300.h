@@ -219,6 +219,36 @@ vnm_status vnm_spmm_run(vnm_ctx* ctx, const vnm_spmm_matrix* A, const void* B, i
 
 vnm_status vnm_spmm_free(vnm_spmm_matrix* A);
 
+/* ---------------------------------------------------------------------------
+ * Matrix Market files and the text round trips of the `spmm` pipeline
+ * (host code)
+ * ------------------------------------------------------------------------- */
+
+/* readMtx + Mtx::init_from_file (mtx/readMtx.hpp:354-425, mtx/Mtx.h:98-112):
+ * banner and size line, tuples, symmetric banners mirrored, repeated entries
+ * removed, sorted by (row, col), rows and cols padded to a multiple of
+ * `aligned`.  Arrays are malloc'ed; release them with vnm_host_free. */
+vnm_status vnm_mtx_read(const char* path, int aligned, int* nrows, int* ncols, int* nnz, int** row, int** col,
+                        float** val);
+void vnm_host_free(void* p);
+
+/* Mtx::write_to_file (mtx/Mtx.h:412-435): "real general" banner, size line,
+ * "%d %d %.2f" entries in the given order, 1-based. */
+vnm_status vnm_mtx_write(const char* path, int nrows, int ncols, int nnz, const int* row, const int* col,
+                         const float* val);
+
+/* Values as the VNM stage reads them from the NM stage's temp.mtx: the
+ * float64 of each value's "%.2f" text (main.cu:246-247, reordering.py:41). */
+vnm_status vnm_text_nm_values(int nnz, const float* val, double* out);
+
+/* temp.mtx written by the VNM stage (scipy mmwrite, precision=1:
+ * reordering.py:179-181) and read back by the NM stage (readMtx): "%.0e"
+ * values; under 100 rows with symmetric values only the lower triangle,
+ * mirrored back by the reader.  In: the VNM stage's n x n matrix in its
+ * entry order.  Out: the reader's COO (malloc'ed). */
+vnm_status vnm_text_vnm_roundtrip(int n, int nnz, const int* row, const int* col, const double* val, int aligned,
+                                  int* out_nrows, int* out_nnz, int** out_row, int** out_col, float** out_val);
+
 /* Host helper: the pop order of the SwapPair priority queue of
  * reorder/reorder.h:521-532 (Comparator, reorder/swappair.h:112-120) for n
  * pairs pushed in index order -- the exact emulation the kernels use. */
