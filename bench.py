@@ -33,9 +33,10 @@ sys.path.insert(0, PKG)
 
 import numpy as np  # noqa: E402
 
-N_NM, M_NM, V = 2, 4, 64
-WORKLOAD = "C2: R-MAT 16384x16384 (a=.57,b=.19,c=.19), 131072 edges symmetrised, N(0,1), 2:4, find_best_2toX"
-METRIC = "plain NM reorder throughput (find_best_2toX over schedules 0-3, R-MAT 16384, 2:4)"
+N_NM, M_NM, V, N_B = 2, 4, 64, 128
+WORKLOAD = ("C2: R-MAT 16384x16384 (a=.57,b=.19,c=.19), 131072 edges symmetrised, N(0,1), 2:4, V=64; "
+            "find_best_2toX + V:N:M SpMM with B 16384x128 bf16")
+METRIC = "reorder wall-time (find_best_2toX, R-MAT 16384, 2:4) + V:N:M SpMM, as hot-path steps per second"
 
 
 def parse():
@@ -117,6 +118,14 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
+def load_tensor_peak():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured (burst)"
+    return 1900.0, "fallback"
+
+
 def workload(rank):
     from vnm_gb300 import synth
     return synth.rmat_c2(seed=rank)
@@ -138,31 +147,46 @@ def host_threads():
         return os.cpu_count() or 1
 
 
+def cpu_port_step(nr, r, c, v, B64, threads):
+    """The CPU port of one hot-path step: find_best_2toX (C++ restatement of
+    the reference NM path, OpenMP) and the SpMM of the reordered matrix
+    (scalar FP64 loop; the reference ships no CPU SpMM)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    oracle.set_threads(threads)
+    t0 = time.perf_counter()
+    best, _ = oracle.find_best(nr, r, c, v, N_NM, M_NM)
+    _, rr, cc, _ = oracle.nm_run(nr, r, c, v, N_NM, M_NM, best)
+    oracle.spmm_f64(nr, rr, cc, v.astype(np.float64), B64)
+    return time.perf_counter() - t0, best
+
+
 def run_reference(args, rank, world):
     """CPU port of the reference path, on the host cores, rank 0 only."""
     if rank != 0:
         return
     nr, r, c, v = workload(0)
+    B64 = np.random.default_rng(1234).standard_normal((nr, N_B))
     threads = host_threads()
     for _ in range(max(0, min(args.warmup, 1))):
-        cpu_port_find_best(nr, r, c, v, threads)
+        cpu_port_step(nr, r, c, v, B64, threads)
     times = []
     for _ in range(args.steps):
-        dt, best = cpu_port_find_best(nr, r, c, v, threads)
+        dt, best = cpu_port_step(nr, r, c, v, B64, threads)
         times.append(dt)
     tot = sum(times)
     value = args.steps / tot
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": "reorders/s", "n_gpus": args.gpus,
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "hot-path steps/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32 (reorder), fp64 (SpMM)",
         "data": "synthetic (seeded R-MAT)",
-        "config": {"workload": WORKLOAD, "nrows": nr, "nnz": int(len(r)), "N": N_NM, "M": M_NM,
-                   "schedules": 4, "l2": "n/a (CPU)"},
-        "cpu_baseline": {"value": value, "unit": "reorders/s", "cores": threads, "kind": "port",
-                         "sample": "full find_best_2toX of the workload matrix per step (C++ restatement "
-                                   "of reorder/reorder.h + main.cu, OpenMP)"},
-        "e2e": {"value": value, "unit": "reorders/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config": {"workload": WORKLOAD, "nrows": nr, "nnz": int(len(r)), "N": N_NM, "M": M_NM, "V": V,
+                   "n_B": N_B, "schedules": 4, "l2": "n/a (CPU)", "best_sched": int(best)},
+        "cpu_baseline": {"value": value, "unit": "hot-path steps/s", "cores": threads, "kind": "port",
+                         "sample": "full step per measurement: find_best_2toX + the winner's run (C++ "
+                                   "restatement of reorder/reorder.h + main.cu, OpenMP) + FP64 SpMM"},
+        "e2e": {"value": value, "unit": "hot-path steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
@@ -177,13 +201,18 @@ def run_ours(args, rank, world, local):
     nr, r, c, v = workload(rank)
     ctx = vnm_gb300.Context(local)
     dev = torch.device("cuda", local)
+    g = torch.Generator().manual_seed(1234 + rank)
+    Bh = torch.randn((nr, N_B), generator=g).to(torch.bfloat16)
     tr = torch.from_numpy(r).to(dev)
     tc = torch.from_numpy(c).to(dev)
     tv = torch.from_numpy(v).to(dev)
+    tB = Bh.to(dev)
+    tC = torch.empty((nr, N_B), dtype=torch.float32, device=dev)
     # pinned host copies for the end-to-end measurement
     hr = torch.from_numpy(r).pin_memory()
     hc = torch.from_numpy(c).pin_memory()
     hv = torch.from_numpy(v).pin_memory()
+    hB = Bh.view(torch.int16).pin_memory()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
 
     def barrier():
@@ -191,85 +220,137 @@ def run_ours(args, rank, world, local):
         if world > 1:
             torch.distributed.barrier()
 
-    def step(device_inputs):
+    def step_device():
+        """One pass of the hot path, inputs in HBM: schedule search, the
+        winner's relabelling, V:N:M compression, SpMM.  Returns timings."""
         flush.zero_()
         torch.cuda.synchronize()
-        if device_inputs:
-            return ctx.nm_search(nr, tr, tc, tv, N_NM, M_NM, want_newpos=True)
-        return ctx.nm_search(nr, hr.numpy(), hc.numpy(), hv.numpy(), N_NM, M_NM, want_newpos=True)
+        t = {}
+        best, res, newpos = ctx.nm_search(nr, tr, tc, tv, N_NM, M_NM, want_newpos=True)
+        t["reorder_ms"] = ctx.last_kernel_ms
+        t["rounds_kernel_ms"] = ctx.last_main_kernel_ms
+        t["launches"] = ctx.last_launch_count
+        t["stats"] = ctx.last_stats()
+        pr, pc = tr.clone(), tc.clone()
+        ctx.permute_coo(nr, pr, pc, torch.from_numpy(newpos).to(dev))
+        t["permute_ms"] = ctx.last_kernel_ms
+        t["launches"] += ctx.last_launch_count
+        A = vnm_gb300.SpmmMatrix(ctx, nr, pr, pc, tv, M_NM, V, "bf16")
+        t["compress_ms"] = ctx.last_kernel_ms
+        t["launches"] += ctx.last_launch_count
+        A.run(tB, tC)
+        t["spmm_call_ms"] = ctx.last_kernel_ms
+        t["spmm_kernel_ms"] = ctx.last_main_kernel_ms
+        t["launches"] += ctx.last_launch_count
+        t["info"] = A.info()
+        t["best"] = best
+        A.close()
+        return t
+
+    def step_host():
+        """The same pass through the public API with host buffers."""
+        best, res, newpos = ctx.nm_search(nr, hr.numpy(), hc.numpy(), hv.numpy(), N_NM, M_NM, want_newpos=True)
+        pr, pc = ctx.permute_coo(nr, hr.numpy(), hc.numpy(), newpos)
+        A = vnm_gb300.SpmmMatrix(ctx, nr, pr, pc, hv.numpy(), M_NM, V, "bf16")
+        C = A.run(hB.numpy())
+        A.close()
+        return C
 
     for _ in range(args.warmup):
-        best, res, newpos = step(True)
-    # timed region: inputs resident in HBM
+        t = step_device()
     clocks = ClockSampler(local)
     clocks.start()
     barrier()
-    dev_ms, main_ms, launches, wall = 0.0, 0.0, 0, 0.0
-    stats_sum = None
-    phase_sum = None
+    tot = {"reorder_ms": 0.0, "rounds_kernel_ms": 0.0, "permute_ms": 0.0, "compress_ms": 0.0,
+           "spmm_call_ms": 0.0, "spmm_kernel_ms": 0.0}
+    launches, wall = 0, 0.0
+    stats_sum, phase_sum = None, None
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        best, res, newpos = step(True)
+        t = step_device()
         wall += time.perf_counter() - t0
-        dev_ms += ctx.last_kernel_ms
-        main_ms += ctx.last_main_kernel_ms
-        launches += ctx.last_launch_count
-        st = ctx.last_stats()
+        for k in tot:
+            tot[k] += t[k]
+        launches += t["launches"]
+        st = dict(t["stats"])
         ph = st.pop("phase_kcycles")
         stats_sum = st if stats_sum is None else {k: stats_sum[k] + st[k] for k in st}
-        phase_sum = ph if stats_sum is st else {k: phase_sum[k] + ph[k] for k in ph}
+        phase_sum = ph if phase_sum is None else {k: phase_sum[k] + ph[k] for k in ph}
     barrier()
     clk = clocks.stop()
-    # the search launches the four jobs and then a second single job for the
-    # winner's permutation; the kernel-time sum covers both
-    elapsed = dev_ms / 1000.0
+    info, best = t["info"], t["best"]
+    step_ms = (tot["reorder_ms"] + tot["permute_ms"] + tot["compress_ms"] + tot["spmm_call_ms"]) / args.steps
+    elapsed = step_ms * args.steps / 1000.0
     if world > 1:
-        t = torch.tensor([elapsed], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed = float(t.item())
+        x = torch.tensor([elapsed], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(x, op=torch.distributed.ReduceOp.MAX)
+        elapsed = float(x.item())
     value = world * args.steps / elapsed
-    # end to end: pinned host buffers through the public API
-    for _ in range(1):
-        step(False)
+    # end to end through the public API with pinned host buffers
+    step_host()
     barrier()
     e2e_t = 0.0
     for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        step(False)
+        C = step_host()
         e2e_t += time.perf_counter() - t0
     barrier()
     if world > 1:
-        t = torch.tensor([e2e_t], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_t = float(t.item())
+        x = torch.tensor([e2e_t], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(x, op=torch.distributed.ReduceOp.MAX)
+        e2e_t = float(x.item())
     e2e_value = world * args.steps / e2e_t
-    h2d = 12 * len(r)
-    d2h = 4 * 20 + 4 + 4 * nr
-    # roofline of the persistent reorder kernel: bytes its algorithm must move
-    # per launch = per round the segment-count scan (4 B x nseg) + per
+    nnz = len(r)
+    h2d = 12 * nnz + 8 * nnz + 4 * nr + 12 * nnz + 2 * nr * N_B
+    d2h = 4 * 20 + 4 + 4 * nr + 8 * nnz + 4 * nr * N_B
+    # SpMM accuracy against the FP64 oracle (outside the timed region)
+    spmm_err = None
+    if rank == 0:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import oracle
+        _, rr, cc, nv = oracle.nm_run(nr, r, c, v, N_NM, M_NM, best)
+        ref = oracle.spmm_f64(nr, rr, cc, v.astype(np.float64), Bh.float().numpy().astype(np.float64))
+        spmm_err = float(np.abs(C.astype(np.float64) - ref).max() / np.abs(ref).max())
+    # roofline of the persistent reorder kernel: the bytes its algorithm must
+    # move per step = per round the segment-count scan (4 B x nseg) + per
     # gathered column entry 4 B (row id) + 16 B record update, + per touched
     # row the 16 B record read and clear
-    st = stats_sum
-    alg_bytes = 4.0 * st["rounds"] * st["nseg"] + 20.0 * st["gathered"] + 32.0 * st["touched"]
+    stt = stats_sum
+    alg_bytes = 4.0 * stt["rounds"] * stt["nseg"] + 20.0 * stt["gathered"] + 32.0 * stt["touched"]
     peak, peak_kind = load_peaks()
-    achieved = alg_bytes / (main_ms / 1000.0) / 1e9 if main_ms > 0 else 0.0
+    achieved = alg_bytes / (tot["rounds_kernel_ms"] / 1000.0) / 1e9 if tot["rounds_kernel_ms"] > 0 else 0.0
+    tflops_peak, tkind = load_tensor_peak()
+    issued = 2.0 * 128 * 16 * N_B * info["ksteps"]
+    useful = 2.0 * nnz * N_B
+    sk = tot["spmm_kernel_ms"] / args.steps / 1000.0
     out = {
-        "metric": METRIC, "value": value, "unit": "reorders/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded R-MAT, seed = rank)",
-        "config": {"workload": WORKLOAD, "nrows": nr, "nnz": int(len(r)), "N": N_NM, "M": M_NM, "schedules": 4,
-                   "parallelism": "replicas" if world > 1 else "single", "l2": "flushed (256 MB write) before "
-                   "every step", "best_sched": int(best), "rounds_per_search": int(st["rounds"] // args.steps)},
-        "e2e": {"value": e2e_value, "unit": "reorders/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+        "metric": METRIC, "value": value, "unit": "hot-path steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32 (reorder), bf16 x bf16 -> fp32 (SpMM)",
+        "data": "synthetic (seeded R-MAT, seed = rank; B ~ N(0,1))",
+        "config": {"workload": WORKLOAD, "nrows": nr, "nnz": nnz, "N": N_NM, "M": M_NM, "V": V, "n_B": N_B,
+                   "schedules": 4, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "flushed (256 MB write) before every step", "best_sched": int(best),
+                   "rounds_per_search": int(stt["rounds"] // args.steps)},
+        "breakdown_ms": {"reorder_search": tot["reorder_ms"] / args.steps, "permute": tot["permute_ms"] / args.steps,
+                         "compress": tot["compress_ms"] / args.steps, "spmm_call": tot["spmm_call_ms"] / args.steps,
+                         "spmm_kernel": tot["spmm_kernel_ms"] / args.steps},
+        "e2e": {"value": e2e_value, "unit": "hot-path steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": 1000.0 * e2e_t / args.steps},
         "roofline": {"kernel": "k_nm_rounds<4>", "bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
-                     "alg_bytes_per_step": alg_bytes / args.steps,
-                     "kernel_ms_per_step": main_ms / args.steps,
-                     "note": "latency-bound sequential greedy; see profiles/",
-                     "round_phase_share": {k: round(v / max(1, sum(phase_sum.values())), 4)
-                                           for k, v in phase_sum.items()},
-                     "us_per_round": 1000.0 * main_ms / max(1, st["rounds"] / max(1, st["jobs"]))},
+                     "alg_bytes_per_launch": alg_bytes / args.steps,
+                     "kernel_ms_per_launch": tot["rounds_kernel_ms"] / args.steps,
+                     "note": "latency-bound sequential greedy (4 thread blocks); see profiles/",
+                     "round_phase_share": {k: round(vv / max(1, sum(phase_sum.values())), 4)
+                                           for k, vv in phase_sum.items()}},
+        "spmm": {"kernel": "k_spmm_vnm<128>", "useful_tflops": useful / sk / 1e12,
+                 "issued_tflops": issued / sk / 1e12, "bound": "tensor", "peak_tflops": tflops_peak,
+                 "peak_kind": tkind, "issued_frac": issued / sk / 1e12 / tflops_peak,
+                 "max_rel_err_vs_fp64": spmm_err, "slices": info["slices"], "ksteps": info["ksteps"],
+                 "blocks": info["blocks"], "valid_blocks": info["valid_blocks"]},
         "gpu_launches": launches,
         "clocks": clk,
         "wall_ms_per_step": 1000.0 * wall / args.steps,
@@ -277,9 +358,10 @@ def run_ours(args, rank, world, local):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = host_threads()
         dt, cbest = cpu_port_find_best(nr, r, c, v, threads)
-        out["cpu_baseline"] = {"value": 1.0 / dt, "unit": "reorders/s", "cores": threads, "kind": "port",
+        out["cpu_baseline"] = {"value": 1.0 / dt, "unit": "hot-path steps/s", "cores": threads, "kind": "port",
                                "sample": "one full find_best_2toX of the same matrix (C++ restatement of the "
-                                         "reference NM path, OpenMP)", "best_sched": int(cbest)}
+                                         "reference NM path, OpenMP); the SpMM part is not included",
+                               "best_sched": int(cbest)}
         out["cpu_baseline_agrees"] = bool(cbest == best)
     if rank == 0:
         print(json.dumps(out), flush=True)
