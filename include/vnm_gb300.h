@@ -169,6 +169,83 @@ vnm_status vnm_nm_pair_score(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
                              int mem, int N, int M, int seg1, int seg2, int* score);
 
 /* ---------------------------------------------------------------------------
+ * Learned-proposal reorder.  No counterpart in the reference: a parallel
+ * search with the reference's objective (fewer invalid M-groups), or with
+ * the retained-nonzero count of an N:M pruning, for matrices where the
+ * sequential greedy of run_onepair is too slow.  Not bit-exact with
+ * vnm_nm_reorder by design.
+ *
+ * Each round, every segment holding an invalid group proposes swaps of its
+ * M nodes with the nodes of `targets` sampled segments (targets*M*M
+ * candidates); the candidates are ranked (by the proposal network, at
+ * random, or not at all), the best topk (or all, exhaustive mode) are scored
+ * exactly by an integer kernel, each segment keeps its best improving swap,
+ * and a claim-based matching accepts swaps that touch disjoint segments, so
+ * every accepted gain is exact and they add up.  Rounds stop after
+ * `max_rounds`, when no segment holds an invalid group, after `patience`
+ * rounds in a row that accepted nothing, or once the gain reaches
+ * `stop_gain` (time to a target quality).  The network proposes at most one
+ * swap per target segment.
+ * ------------------------------------------------------------------------- */
+
+#define VNM_LEARNED_MLP 0        /* network ranks, the top topk scored exactly */
+#define VNM_LEARNED_EXHAUSTIVE 1 /* every candidate scored exactly */
+#define VNM_LEARNED_RANDOM 2     /* topk random candidates scored exactly */
+
+#define VNM_MLP_FEATURES 32
+#define VNM_MLP_HIDDEN 128
+
+/* Proposal network: 32 features -> 128 -> 128 -> 1, ReLU, BF16 operands
+ * and FP32 accumulation at inference (tcgen05), FP32 master weights and
+ * Adam state on the device.  Parameter vector (vnm_mlp_param_count floats):
+ * W1[128][32], b1[128], W2[128][128], b2[128], w3[128], b3. */
+typedef struct vnm_mlp vnm_mlp;
+int vnm_mlp_param_count(void);
+vnm_status vnm_mlp_create(vnm_ctx* ctx, unsigned seed, vnm_mlp** net);
+vnm_status vnm_mlp_free(vnm_mlp* net);
+vnm_status vnm_mlp_get(const vnm_mlp* net, float* params);
+vnm_status vnm_mlp_set(vnm_mlp* net, const float* params); /* also resets Adam */
+/* Scores of n feature rows X[n][32] (host) into Y[n] (host), tensor cores. */
+vnm_status vnm_mlp_forward(vnm_ctx* ctx, const vnm_mlp* net, const float* X, int n, float* Y);
+/* Gradient of L = mean((f(x) - t)^2) / 2 over one batch of B rows (host
+ * X[B][32], t[B]); the forward pass rounds layer inputs and weights to BF16
+ * as the inference does.  grads: vnm_mlp_param_count floats (host). */
+vnm_status vnm_mlp_grad(vnm_ctx* ctx, vnm_mlp* net, const float* X, const float* t, int B, float* grads,
+                        float* loss);
+/* Adam (beta 0.9 / 0.999) over n rows in mini-batches of B, `epochs` passes
+ * in the given order; *final_loss = mean batch loss of the last pass. */
+vnm_status vnm_mlp_train(vnm_ctx* ctx, vnm_mlp* net, const float* X, const float* t, int n, int B, int epochs,
+                         float lr, float* final_loss);
+
+typedef struct vnm_learned_params {
+  int mode;            /* VNM_LEARNED_* */
+  int objective;       /* 0 invalid groups, 1 retained nonzeros (sum of min(popcount, N)) */
+  int targets;         /* target segments sampled per proposing segment and round; targets*M*M <= 2048 */
+  int topk;            /* proposals per segment scored exactly (1..8; network and random modes) */
+  int max_rounds;
+  int patience;        /* >= 1 */
+  unsigned seed;
+  int dump_every;      /* > 0: keep 1 in dump_every exactly scored candidates as training pairs */
+  int dump_cap;        /* capacity of the dump buffers (pairs) */
+  float* dump_features; /* host [dump_cap][32] */
+  float* dump_gains;    /* host [dump_cap], exact gain in objective units */
+  long long stop_gain;  /* > 0: stop once the accepted gains add up to this much */
+} vnm_learned_params;
+
+typedef struct vnm_learned_result {
+  long long init_invalid, final_invalid;   /* groups with popcount > N */
+  long long init_retained, final_retained; /* sum over groups of min(popcount, N) */
+  long long gain;                          /* sum of accepted exact gains */
+  long long exact_scored;                  /* candidates scored exactly */
+  int rounds, swaps, ndump, reserved;
+} vnm_learned_result;
+
+/* Same input contract as vnm_nm_reorder; newpos optional (nrows ints). */
+vnm_status vnm_nm_learned(vnm_ctx* ctx, int nrows, int nnz, const int* row, const int* col, const float* val,
+                          int mem, int N, int M, const vnm_mlp* net, const vnm_learned_params* params,
+                          vnm_learned_result* result, int* newpos);
+
+/* ---------------------------------------------------------------------------
  * VNM stage (the row sort of reordering.py)
  * ------------------------------------------------------------------------- */
 

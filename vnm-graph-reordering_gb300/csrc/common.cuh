@@ -105,6 +105,24 @@ vnm_status radix_sort_u64(vnm_ctx* ctx, const unsigned long long* keys, const in
                           unsigned long long** out_keys, int** out_vals);
 size_t radix_sort_scratch_bytes(int n);
 
+// The nonzero-valued pattern of one square matrix on the device: entries
+// with val != 0 in (row, col) order, the same entries by column (CSC), and
+// the invalid / present row counts of each M-column segment.
+struct Pattern {
+  int R = 0, nseg = 0, np = 0;
+  int* prow = nullptr;
+  int* pcol = nullptr;
+  int* cptr = nullptr;
+  int* crow = nullptr;
+  int* inv0 = nullptr;
+  int* pres0 = nullptr;
+};
+size_t pattern_bytes(int R, int nnz);
+// validates (row, col) order and range, then builds P in the arena;
+// h_scratch: at least 2 pinned ints
+vnm_status build_pattern(vnm_ctx* ctx, int R, int nnz, const int* d_row, const int* d_col, const float* d_val,
+                         int N, int M, Pattern& P, int* h_scratch);
+
 }  // namespace vnm
 
 #endif

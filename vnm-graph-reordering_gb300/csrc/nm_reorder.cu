@@ -992,16 +992,6 @@ __global__ void __launch_bounds__(NM_THREADS) k_pair_score(NMJob J, int N, int s
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
-struct Pattern {  // the nonzero-valued pattern of one matrix on the device
-  int R = 0, nseg = 0, np = 0;
-  int* prow = nullptr;
-  int* pcol = nullptr;
-  int* cptr = nullptr;
-  int* crow = nullptr;
-  int* inv0 = nullptr;
-  int* pres0 = nullptr;
-};
-
 static inline int grid_for(const vnm_ctx* ctx, long long n, int nt = 256) {
   long long g = (n + nt - 1) / nt;
   long long cap = (long long)ctx->num_sms * 8;
@@ -1070,8 +1060,8 @@ static vnm_status build_pattern_t(vnm_ctx* ctx, int R, int nnz, const int* d_row
   return VNM_OK;
 }
 
-static vnm_status build_pattern(vnm_ctx* ctx, int R, int nnz, const int* d_row, const int* d_col,
-                                const float* d_val, int N, int M, Pattern& P, int* h_scratch) {
+vnm_status build_pattern(vnm_ctx* ctx, int R, int nnz, const int* d_row, const int* d_col, const float* d_val,
+                         int N, int M, Pattern& P, int* h_scratch) {
   switch (M) {
     case 2: return build_pattern_t<2>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch);
     case 3: return build_pattern_t<3>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch);

@@ -341,3 +341,133 @@ class SpmmMatrix:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------------------
+# Learned-proposal reorder
+# ---------------------------------------------------------------------------
+LEARNED_MLP, LEARNED_EXHAUSTIVE, LEARNED_RANDOM = 0, 1, 2
+MLP_FEATURES, MLP_HIDDEN = 32, 128
+OBJ_INVALID, OBJ_RETAINED = 0, 1
+
+
+class _LearnedParams(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int), ("objective", ctypes.c_int), ("targets", ctypes.c_int),
+                ("topk", ctypes.c_int), ("max_rounds", ctypes.c_int), ("patience", ctypes.c_int), ("seed", ctypes.c_uint),
+                ("dump_every", ctypes.c_int), ("dump_cap", ctypes.c_int), ("dump_features", _f32p),
+                ("dump_gains", _f32p), ("stop_gain", ctypes.c_longlong)]
+
+
+class _LearnedResult(ctypes.Structure):
+    _fields_ = [("init_invalid", ctypes.c_longlong), ("final_invalid", ctypes.c_longlong),
+                ("init_retained", ctypes.c_longlong), ("final_retained", ctypes.c_longlong),
+                ("gain", ctypes.c_longlong), ("exact_scored", ctypes.c_longlong), ("rounds", ctypes.c_int),
+                ("swaps", ctypes.c_int), ("ndump", ctypes.c_int), ("reserved", ctypes.c_int)]
+
+
+def _learned_lib():
+    L = lib()
+    if not hasattr(L, "_learned_typed"):
+        L.vnm_mlp_param_count.restype = ctypes.c_int
+        L.vnm_mlp_create.argtypes = [_vp, ctypes.c_uint, ctypes.POINTER(_vp)]
+        L.vnm_mlp_free.argtypes = [_vp]
+        L.vnm_mlp_get.argtypes = [_vp, _f32p]
+        L.vnm_mlp_set.argtypes = [_vp, _f32p]
+        L.vnm_mlp_forward.argtypes = [_vp, _vp, _f32p, ctypes.c_int, _f32p]
+        L.vnm_mlp_grad.argtypes = [_vp, _vp, _f32p, _f32p, ctypes.c_int, _f32p, _f32p]
+        L.vnm_mlp_train.argtypes = [_vp, _vp, _f32p, _f32p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_float, _f32p]
+        L.vnm_nm_learned.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, _vp, ctypes.POINTER(_LearnedParams),
+                                     ctypes.POINTER(_LearnedResult), _i32p]
+        L._learned_typed = True
+    return L
+
+
+class Mlp:
+    """The swap-proposal network (FP32 master weights and Adam state on the
+    device of `ctx`).  Parameters as one flat float32 vector:
+    W1[128][32], b1[128], W2[128][128], b2[128], w3[128], b3."""
+
+    def __init__(self, ctx, seed=0):
+        L = _learned_lib()
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        _check(L.vnm_mlp_create(ctx.h, int(seed), ctypes.byref(h)), "vnm_mlp_create")
+        self.h = h
+
+    @staticmethod
+    def param_count():
+        return _learned_lib().vnm_mlp_param_count()
+
+    def get(self):
+        p = np.zeros(self.param_count(), np.float32)
+        _check(_learned_lib().vnm_mlp_get(self.h, p.ctypes.data_as(_f32p)), "vnm_mlp_get")
+        return p
+
+    def set(self, p):
+        p = _host(p, np.float32)
+        assert p.size == self.param_count()
+        _check(_learned_lib().vnm_mlp_set(self.h, p.ctypes.data_as(_f32p)), "vnm_mlp_set")
+
+    def forward(self, X):
+        X = _host(X, np.float32).reshape(-1, MLP_FEATURES)
+        Y = np.zeros(len(X), np.float32)
+        _check(_learned_lib().vnm_mlp_forward(self.ctx.h, self.h, X.ctypes.data_as(_f32p), len(X),
+                                              Y.ctypes.data_as(_f32p)), "vnm_mlp_forward")
+        return Y
+
+    def grad(self, X, t):
+        X = _host(X, np.float32).reshape(-1, MLP_FEATURES)
+        t = _host(t, np.float32)
+        g = np.zeros(self.param_count(), np.float32)
+        loss = ctypes.c_float()
+        _check(_learned_lib().vnm_mlp_grad(self.ctx.h, self.h, X.ctypes.data_as(_f32p), t.ctypes.data_as(_f32p),
+                                           len(X), g.ctypes.data_as(_f32p), ctypes.byref(loss)), "vnm_mlp_grad")
+        return g, loss.value
+
+    def train(self, X, t, batch=1024, epochs=1, lr=1e-3):
+        X = _host(X, np.float32).reshape(-1, MLP_FEATURES)
+        t = _host(t, np.float32)
+        loss = ctypes.c_float()
+        _check(_learned_lib().vnm_mlp_train(self.ctx.h, self.h, X.ctypes.data_as(_f32p), t.ctypes.data_as(_f32p),
+                                            len(X), int(batch), int(epochs), float(lr), ctypes.byref(loss)),
+               "vnm_mlp_train")
+        return loss.value
+
+    def close(self):
+        if self.h:
+            _learned_lib().vnm_mlp_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def nm_learned(ctx, nrows, row, col, val, N, M, mode=LEARNED_MLP, net=None, objective=OBJ_RETAINED, targets=16,
+               topk=8, max_rounds=64, patience=2, seed=0, dump_every=0, dump_cap=0, stop_gain=0, want_newpos=True):
+    """Learned-proposal (or exhaustive / random-proposal) reorder.  Returns
+    (result dict, newpos or None, (features, gains) or None)."""
+    L = _learned_lib()
+    pr, pc, pv, mem, nnz, keep = ctx._arrays(row, col, val)
+    p = _LearnedParams()
+    p.mode, p.objective, p.targets, p.topk = int(mode), int(objective), int(targets), int(topk)
+    p.max_rounds, p.patience, p.seed = int(max_rounds), int(patience), int(seed) & 0xffffffff
+    p.stop_gain = int(stop_gain)
+    dx = dy = None
+    if dump_every > 0 and dump_cap > 0:
+        dx = np.zeros((dump_cap, MLP_FEATURES), np.float32)
+        dy = np.zeros(dump_cap, np.float32)
+        p.dump_every, p.dump_cap = int(dump_every), int(dump_cap)
+        p.dump_features, p.dump_gains = dx.ctypes.data_as(_f32p), dy.ctypes.data_as(_f32p)
+    r = _LearnedResult()
+    newpos = np.zeros(nrows, np.int32) if want_newpos else None
+    _check(L.vnm_nm_learned(ctx.h, nrows, nnz, pr, pc, pv, mem, N, M, net.h if net is not None else None,
+                            ctypes.byref(p), ctypes.byref(r),
+                            newpos.ctypes.data_as(_i32p) if newpos is not None else None), "vnm_nm_learned")
+    res = {k: getattr(r, k) for k, _ in _LearnedResult._fields_ if k != "reserved"}
+    dump = (dx[:r.ndump], dy[:r.ndump]) if dx is not None else None
+    return res, newpos, dump
