@@ -20,11 +20,12 @@
 //     bytes), and the 16 B rows it multiplies are listed by index.
 //   - values are stored divided by their block row's scale (max |a| of the
 //     V rows), and the epilogue multiplies each output row back by it.
-// Kernel: one CTA per (tile, column block of C).  A producer thread streams
+// Kernel: one CTA per (tile, column block of C).  A producer warp streams
 // each K-step's A tile (one bulk copy) and gathers its 16 B rows with TMA
-// tile::gather4 (rows in 128-byte swizzled layout); one thread issues the
-// MMA per K-step; two stages overlap copies with MMAs.  Four warps then read
-// the FP32 accumulator out of tensor memory, scale and store it.
+// tile::gather4 (rows in 128-byte swizzled layout), with the row ids loaded
+// eight K-steps ahead; one thread issues the MMA per K-step; eight stages
+// keep copies in flight while the MMAs run.  Four warps then read the FP32
+// accumulator out of tensor memory, scale and store it.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -266,7 +267,8 @@ struct SpmmArgs {
   int* err;
 };
 
-constexpr int SP_STAGES = 2;
+constexpr int SP_STAGES = 8;  // K-steps in flight per CTA
+constexpr int SP_PF = 4;      // pairs of K-steps whose column ids are loaded ahead
 
 template <int NT>
 struct SpmmSmem {
@@ -310,31 +312,62 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
   ptx::tc_fence_after();
   const uint32_t tmem = sm.tmem_base;
 
-  int issued = 0;  // K-steps whose copies were issued (producer thread)
+  int issued = 0;  // K-steps whose copies were issued (producer warp)
   if (nsteps > 0) {
-    if (tid == 0) {
-      // producer: A tile by bulk copy, 16 B rows by gather4 (64 columns each)
-      for (int i = 0; i < nsteps; ++i) {
-        const int s = i % SP_STAGES;
-        if (i >= SP_STAGES && !ptx::mbar_wait(&sm.empty[s], ((i / SP_STAGES) - 1) & 1, SP_WAIT_LIMIT)) {
-          atomicOr(p.err, 1);
-          sm.abort = 1;
-          break;
+    if (warp == 0) {
+      // producer warp.  Lane l holds column id (l & 15) of K-step
+      // i + 2q + (l >> 4) for the SP_PF pairs q ahead (coalesced 128-byte
+      // loads issued 2*SP_PF steps before use); lane 0 issues the A tile by
+      // bulk copy and the 16 B rows by gather4 (64 columns each).
+      int pf[SP_PF];
+#pragma unroll
+      for (int q = 0; q < SP_PF; ++q) {
+        const int st = 2 * q + (lane >> 4);
+        pf[q] = st < nsteps ? p.cols[(size_t)(s0 + st) * 16 + (lane & 15)] : 0;
+      }
+      bool stop = false;
+      for (int i = 0; i < nsteps && !stop; i += 2) {
+        const int cur = pf[0];
+#pragma unroll
+        for (int q = 0; q + 1 < SP_PF; ++q) pf[q] = pf[q + 1];
+        {
+          const int st = i + 2 * SP_PF + (lane >> 4);
+          pf[SP_PF - 1] = st < nsteps ? p.cols[(size_t)(s0 + st) * 16 + (lane & 15)] : 0;
         }
-        ptx::mbar_arrive_expect_tx(&sm.full[s], SP_KSTEP_BYTES + 16 * NT * 2);
-        ptx::bulk_g2s(sm.a[s], p.a + (size_t)(s0 + i) * SP_KSTEP_BYTES, SP_KSTEP_BYTES, &sm.full[s]);
-        const int* c = p.cols + (size_t)(s0 + i) * 16;
-#pragma unroll
-        for (int g = 0; g < 4; ++g) {
-          const int y0 = c[4 * g], y1 = c[4 * g + 1], y2 = c[4 * g + 2], y3 = c[4 * g + 3];
-#pragma unroll
-          for (int h = 0; h < NT / 64; ++h) {
-            // atom (k block g/2, n block h): 8 k-rows x 128 bytes; rows 4(g%2)..
-            unsigned char* dst = sm.b[s] + h * 2048 + (g >> 1) * 1024 + (g & 1) * 512;
-            ptx::tma_gather4(dst, &tmap, n0 + 64 * h, y0, y1, y2, y3, &sm.full[s]);
+        for (int d = 0; d < 2 && i + d < nsteps; ++d) {
+          const int ii = i + d, s = ii % SP_STAGES;
+          int ok = 1;
+          if (lane == 0 && ii >= SP_STAGES)
+            ok = ptx::mbar_wait(&sm.empty[s], ((ii / SP_STAGES) - 1) & 1, SP_WAIT_LIMIT) ? 1 : 0;
+          ok = __shfl_sync(0xffffffffu, ok, 0);
+          if (!ok) {
+            if (lane == 0) {
+              atomicOr(p.err, 1);
+              sm.abort = 1;
+            }
+            stop = true;
+            break;
           }
+          int y[16];
+#pragma unroll
+          for (int k = 0; k < 16; ++k) y[k] = __shfl_sync(0xffffffffu, cur, d * 16 + k);
+          if (lane == 0) {
+            ptx::mbar_arrive_expect_tx(&sm.full[s], SP_KSTEP_BYTES + 16 * NT * 2);
+            ptx::bulk_g2s(sm.a[s], p.a + (size_t)(s0 + ii) * SP_KSTEP_BYTES, SP_KSTEP_BYTES, &sm.full[s]);
+#pragma unroll
+            for (int g = 0; g < 4; ++g) {
+#pragma unroll
+              for (int h = 0; h < NT / 64; ++h) {
+                // atom (k block g/2, n block h): 8 k-rows x 128 bytes; rows 4(g%2)..
+                unsigned char* dst = sm.b[s] + h * 2048 + (g >> 1) * 1024 + (g & 1) * 512;
+                ptx::tma_gather4(dst, &tmap, n0 + 64 * h, y[4 * g], y[4 * g + 1], y[4 * g + 2], y[4 * g + 3],
+                                 &sm.full[s]);
+              }
+            }
+          }
+          __syncwarp();
+          issued = ii + 1;
         }
-        issued = i + 1;
       }
     } else if (tid == 32) {
       // MMA issuer
