@@ -48,7 +48,7 @@ namespace vnm {
 
 size_t scan_scratch_bytes(int n);
 
-constexpr int NM_THREADS = 512;  // threads per job block
+constexpr int NM_THREADS = 1024;  // threads per job block
 constexpr unsigned FULL = 0xffffffffu;
 
 // status bits a job reports in res[5]
@@ -810,13 +810,13 @@ __device__ void apply_phase(RoundSmem<M>& sm, const NMJob& J, int N, int round, 
   constexpr int K = M + 1;
   const int tid = threadIdx.x;
   (void)round;
-  if (tid == 0) {
-    for (int q = 0; q < sm.nswaps; ++q) {
-      const int v1 = sm.swaps[2 * q], v2 = sm.swaps[2 * q + 1];
-      const int o1 = J.orig[v1], o2 = J.orig[v2];
-      J.orig[v1] = o2;
-      J.orig[v2] = o1;
-    }
+  // a round's swaps are disjoint transpositions (the walk never reuses a
+  // visited position), so each thread applies one of them
+  if (tid < sm.nswaps) {
+    const int v1 = sm.swaps[2 * tid], v2 = sm.swaps[2 * tid + 1];
+    const int o1 = J.orig[v1], o2 = J.orig[v2];
+    J.orig[v1] = o2;
+    J.orig[v2] = o1;
   }
   const int Kn = sm.K_;
   const int lane = tid & 31;
