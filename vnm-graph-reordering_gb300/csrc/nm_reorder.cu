@@ -37,12 +37,16 @@
 // no allocation.  Many jobs (four schedules, or a batch of matrices) run in
 // one launch.
 
+#include <cooperative_groups.h>
+
 #include <cstdio>
 #include <cstring>
 #include <vector>
 
 #include "common.cuh"
 #include "swap_heap.h"
+
+namespace cg = cooperative_groups;
 
 namespace vnm {
 
@@ -55,6 +59,12 @@ constexpr unsigned FULL = 0xffffffffu;
 constexpr int JOB_OK = 0;
 constexpr int JOB_EMPTY_HEAP = 1;   // reference would call top() on an empty queue
 constexpr int JOB_BAD_STATE = 2;    // a count went out of range
+
+// The part of a job's row work one thread block does: block `rank` of the
+// `cs` blocks (a thread-block cluster) that share the job.
+struct Slice {
+  int rank, cs;
+};
 
 struct NMJob {
   int R;              // padded rows = columns
@@ -187,6 +197,7 @@ struct RoundSmem {
   int use_table;    // this round's records are in `table` (else in J.rec)
   int status;
   int nswaps;
+  int go;           // the leader's decision to run another round (copied to every block)
   int S[K][M];                 // S_x(k): rows with bit k set and popcount == N+1
   int CL[NPAIR][MM];           // per unordered pair (a < b): left-side corrections
   int CR[NPAIR][MM];           //                              right-side corrections
@@ -427,8 +438,9 @@ __device__ void clear_round_smem(RoundSmem<M>& sm) {
 
 // OR the bitmaps of the round's segments into per-row records.
 template <int M>
-__device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J) {
+__device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J, Slice sl = Slice{0, 1}, int* ntp = nullptr) {
   const int tid = threadIdx.x;
+  if (!ntp) ntp = &sm.ntouched;
   const int KM = sm.K_ * M;
   if (tid < KM) {
     const int xi = tid / M, k = tid % M;
@@ -478,13 +490,15 @@ __device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J) {
   // GATHER_U entries per thread per step: their row loads, their bitmap ORs
   // (no result used, so they issue as reductions) and their first-touch
   // atomics are all in flight together instead of one chain at a time.
+  // The entries are dealt out over all threads of the job's blocks.
   constexpr int GATHER_U = 4;
-  for (int base = tid; base < E; base += NM_THREADS * GATHER_U) {
+  const int gthreads = sl.cs * NM_THREADS;
+  for (int base = sl.rank * NM_THREADS + tid; base < E; base += gthreads * GATHER_U) {
     int rr[GATHER_U];
     unsigned word[GATHER_U], bit[GATHER_U];
 #pragma unroll
     for (int u = 0; u < GATHER_U; ++u) {
-      const int e = base + u * NM_THREADS;
+      const int e = base + u * gthreads;
       rr[u] = -1;
       word[u] = 0;
       bit[u] = 0;
@@ -509,7 +523,7 @@ __device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J) {
     for (int u = 0; u < GATHER_U; ++u) first[u] = rr[u] >= 0 ? atomicOr(&recw[4 * rr[u] + 3], 1u) : 1u;
 #pragma unroll
     for (int u = 0; u < GATHER_U; ++u)
-      if (first[u] == 0u) J.touched[atomicAdd(&sm.ntouched, 1)] = rr[u];
+      if (first[u] == 0u) J.touched[atomicAdd(ntp, 1)] = rr[u];
   }
   __syncthreads();
 }
@@ -525,17 +539,20 @@ __device__ __forceinline__ unsigned rec_byte(const uint4& w, int xi) {
 // lane first loads the records of TOUCH_U rows so their L2 round trips
 // overlap.
 template <int M, class F>
-__device__ __forceinline__ void for_touched_warp(const RoundSmem<M>& sm, const NMJob& J, F&& f) {
+__device__ __forceinline__ void for_touched_warp(const RoundSmem<M>& sm, const NMJob& J, Slice sl, F&& f) {
   constexpr int TOUCH_U = 4;
   constexpr int NW = NM_THREADS / 32;
   const int nt = sm.ntouched;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int base = w * 32 * TOUCH_U; base < nt; base += NW * 32 * TOUCH_U) {
+  // 32-row chunks dealt round-robin over every warp of the job's blocks, so
+  // a round with few touched rows still spreads over all of them
+  const int NWt = sl.cs * NW;
+  const int lane = threadIdx.x & 31, w = sl.rank * NW + (threadIdx.x >> 5);
+  for (int c0 = w; c0 * 32 < nt; c0 += NWt * TOUCH_U) {
     int rv[TOUCH_U];
     uint4 wv[TOUCH_U];
 #pragma unroll
     for (int u = 0; u < TOUCH_U; ++u) {
-      const int t = base + u * 32 + lane;
+      const int t = (c0 + u * NWt) * 32 + lane;
       rv[u] = t < nt ? J.touched[t] : -1;
     }
 #pragma unroll
@@ -549,8 +566,8 @@ __device__ __forceinline__ void for_touched_warp(const RoundSmem<M>& sm, const N
 // slots (index = slot) when the records are in shared memory, else the
 // touched rows (index = row).  Warp-uniform like for_touched_warp.
 template <int M, class F>
-__device__ __forceinline__ void for_rows_warp(const RoundSmem<M>& sm, const NMJob& J, F&& f) {
-  if (sm.use_table) {
+__device__ __forceinline__ void for_rows_warp(const RoundSmem<M>& sm, const NMJob& J, Slice sl, F&& f) {
+  if (sm.use_table) {  // one block per job only
     constexpr int NW = NM_THREADS / 32;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int base = w * 32; base < sm.ts_max; base += NW * 32) {
@@ -559,7 +576,7 @@ __device__ __forceinline__ void for_rows_warp(const RoundSmem<M>& sm, const NMJo
       f(slot, v, v.w != 0u);
     }
   } else {
-    for_touched_warp<M>(sm, J, f);
+    for_touched_warp<M>(sm, J, sl, f);
   }
 }
 
@@ -572,14 +589,14 @@ __device__ __forceinline__ void for_rows_warp(const RoundSmem<M>& sm, const NMJo
 //   CR(i, j) = sum  L_i * eR_j,   eR = R if pR == N+1, ~R if pR == N, else 0
 //   S_a(k)   = sum over all rows of [L_k and pL == N+1]
 template <int M>
-__device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N) {
+__device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl = Slice{0, 1}) {
   constexpr int K = M + 1;
   constexpr int MM = M * M;
   constexpr unsigned MASK = (1u << M) - 1u;
   const int Kn = sm.K_;
   const bool self = sm.mode == 2;
   const int lane = threadIdx.x & 31;
-  for_rows_warp<M>(sm, J, [&](int r, const uint4& w, bool valid) {
+  for_rows_warp<M>(sm, J, sl, [&](int r, const uint4& w, bool valid) {
     (void)r;
     unsigned b[K];
     int p[K];
@@ -804,15 +821,15 @@ __device__ void walk_phase(RoundSmem<M>& sm, int sched) {
   }
 }
 
-// Apply the swaps to orig[] and recount the touched segments.
+// Apply the swaps to orig[] (the leader block) and recount this block's
+// slice of the touched rows into newinv / newpres.
 template <int M>
-__device__ void apply_phase(RoundSmem<M>& sm, const NMJob& J, int N, int round, int* cnt) {
+__device__ void apply_recount(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl) {
   constexpr int K = M + 1;
   const int tid = threadIdx.x;
-  (void)round;
   // a round's swaps are disjoint transpositions (the walk never reuses a
   // visited position), so each thread applies one of them
-  if (tid < sm.nswaps) {
+  if (sl.rank == 0 && tid < sm.nswaps) {
     const int v1 = sm.swaps[2 * tid], v2 = sm.swaps[2 * tid + 1];
     const int o1 = J.orig[v1], o2 = J.orig[v2];
     J.orig[v1] = o2;
@@ -820,7 +837,7 @@ __device__ void apply_phase(RoundSmem<M>& sm, const NMJob& J, int N, int round, 
   }
   const int Kn = sm.K_;
   const int lane = tid & 31;
-  for_rows_warp<M>(sm, J, [&](int r, const uint4& w, bool valid) {
+  for_rows_warp<M>(sm, J, sl, [&](int r, const uint4& w, bool valid) {
     unsigned nb[K];
 #pragma unroll
     for (int xi = 0; xi < K; ++xi) nb[xi] = 0;
@@ -853,24 +870,59 @@ __device__ void apply_phase(RoundSmem<M>& sm, const NMJob& J, int N, int round, 
     }
   });
   __syncthreads();
-  if (tid < Kn) {
+}
+
+// The new counts of the round's segments (leader block).
+template <int M>
+__device__ void apply_finish(RoundSmem<M>& sm, const NMJob& J, int* cnt) {
+  const int tid = threadIdx.x;
+  if (tid < sm.K_) {
     cnt[sm.xseg[tid]] = sm.newinv[tid];
     J.zc[sm.xseg[tid]] = J.R - sm.newpres[tid];
   }
   __syncthreads();
 }
 
+// Leader block: add the other blocks' partial sums of n ints at `mine`.
+template <int M>
+__device__ void cluster_reduce(cg::cluster_group& cl, int cs, int* mine, int n) {
+  for (int i = threadIdx.x; i < n; i += NM_THREADS) {
+    int v = 0;
+    for (int r = 1; r < cs; ++r) v += cl.map_shared_rank(mine, r)[i];
+    mine[i] += v;
+  }
+  __syncthreads();
+}
+
+// All rounds of a job.  With cs == 1 one thread block runs the job; with
+// cs > 1 the job runs on a thread-block cluster of cs blocks: the leader
+// (rank 0) runs the sequential parts (segment choice, heaps, walk, counts)
+// and every block gathers, scores and recounts its share of the rows, the
+// partial sums meeting in the leader's shared memory.  Every block of a
+// cluster runs the same sequence of cluster barriers: the leader's decision
+// to run a round is copied to every block before the barrier that opens it.
 template <int M>
 __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __restrict__ jobs, int N,
-                                                              int cnt_in_smem, int ts_max) {
+                                                              int cnt_in_smem, int ts_max, int cs) {
+  constexpr int K = M + 1;
   __shared__ RoundSmem<M> sm;
+  static_assert(offsetof(RoundSmem<M>, CL) == offsetof(RoundSmem<M>, S) + sizeof(int) * K * M, "S, CL adjacent");
+  static_assert(offsetof(RoundSmem<M>, CR) == offsetof(RoundSmem<M>, CL) + sizeof(int) * RoundSmem<M>::NPAIR *
+                                                                              RoundSmem<M>::MM, "CL, CR adjacent");
+  static_assert(offsetof(RoundSmem<M>, newpres) == offsetof(RoundSmem<M>, newinv) + sizeof(int) * K,
+                "newinv, newpres adjacent");
+  constexpr int NSUM = K * M + 2 * RoundSmem<M>::NPAIR * RoundSmem<M>::MM;
   // dynamic shared memory: [row-record table: ts_max x 16 B][segment counts]
   extern __shared__ uint4 smem_dyn[];
   int* smem_cnt = reinterpret_cast<int*>(smem_dyn + ts_max);
-  const NMJob J = jobs[blockIdx.x];
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = cs > 1 ? (int)cl.block_rank() : 0;
+  const bool lead = rank == 0;
+  const Slice sl{rank, cs};
+  const NMJob J = jobs[blockIdx.x / cs];
   const int tid = threadIdx.x;
   int* cnt = cnt_in_smem ? smem_cnt : J.cnt;
-  if (cnt_in_smem)
+  if (lead && cnt_in_smem)
     for (int s = tid; s < J.nseg; s += NM_THREADS) smem_cnt[s] = J.cnt[s];
   for (int i = tid; i < ts_max; i += NM_THREADS) smem_dyn[i] = make_uint4(0u, 0u, 0u, 0u);
   if (tid == 0) {
@@ -879,62 +931,108 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     sm.ts_max = ts_max;
     sm.ts_shift = 32 - (31 - __clz(ts_max > 0 ? ts_max : 1));
     sm.use_table = 0;
+    sm.go = 0;
   }
   clear_round_smem<M>(sm);
   __syncthreads();
-  select_phase<M>(sm, J, cnt);
+  if (lead) select_phase<M>(sm, J, cnt);
   const int init_size = sm.lsize, init_cnt = sm.ltotal;
   const int MAXITER = J.maxiter > init_size ? J.maxiter : init_size;  // reorder.h:1819
   int round = 1;
   int committed = 0;
   unsigned long long sumE = 0, sumT = 0;
-  // cycles spent in each phase of a round, measured by thread 0 at the
-  // barriers that end the phases: select, choose, gather, process, heap,
-  // walk, apply
+  // cycles spent in each phase of a round, measured by thread 0 of the
+  // leader at the barriers that end the phases: select, choose, gather,
+  // process, heap, walk, apply
   unsigned long long tph[7] = {0, 0, 0, 0, 0, 0, 0};
   long long t0 = clock64(), t1;
-#define VNM_PHASE(i)                     \
-  if (tid == 0) {                        \
-    t1 = clock64();                      \
+#define VNM_PHASE(i)                         \
+  if (tid == 0) {                            \
+    t1 = clock64();                          \
     tph[i] += (unsigned long long)(t1 - t0); \
-    t0 = t1;                             \
+    t0 = t1;                                 \
   }
-  while (round <= MAXITER && sm.lsize >= 1) {
-    if (sm.lsize == 1) minseg_phase<M>(sm, J);
-    VNM_PHASE(0);
-    choose_segments<M>(sm, J.sched);
-    __syncthreads();
-    VNM_PHASE(1);
-    gather_phase<M>(sm, J);
-    VNM_PHASE(2);
-    process_phase<M>(sm, J, N);
-    VNM_PHASE(3);
-    heap_phase<M>(sm);
-    VNM_PHASE(4);
-    walk_phase<M>(sm, J.sched);
-    __syncthreads();
-    VNM_PHASE(5);
-    if (tid == 0 && J.trace_pairs) {
-      for (int q = 0; q < sm.nswaps; ++q) {
-        if (committed < J.trace_cap_pairs) {
-          J.trace_pairs[2 * committed] = sm.swaps[2 * q];
-          J.trace_pairs[2 * committed + 1] = sm.swaps[2 * q + 1];
-        }
-        ++committed;
+  if (cs > 1) cl.sync();  // every block's shared memory is set up before any remote access
+  for (;;) {
+    if (lead) {
+      if (tid == 0) sm.go = (round <= MAXITER && sm.lsize >= 1 && sm.status == JOB_OK) ? 1 : 0;
+      __syncthreads();
+      if (sm.go) {
+        if (sm.lsize == 1) minseg_phase<M>(sm, J);
+        VNM_PHASE(0);
+        choose_segments<M>(sm, J.sched);
+        __syncthreads();
+        VNM_PHASE(1);
       }
-      if (round - 1 < J.trace_cap_rounds) J.trace_rounds[round - 1] = committed;
+      for (int r = 1; r < cs; ++r) {  // the round's segments to every block
+        RoundSmem<M>* rs = cl.map_shared_rank(&sm, r);
+        if (tid == 0) {
+          rs->go = sm.go;
+          rs->K_ = sm.K_;
+          rs->mode = sm.mode;
+        }
+        if (tid < K) rs->xseg[tid] = sm.xseg[tid];
+      }
     }
-    sumE += (unsigned)sm.E;
-    sumT += (unsigned)sm.ntouched;
-    apply_phase<M>(sm, J, N, round, cnt);
-    clear_round_smem<M>(sm);
-    __syncthreads();
-    VNM_PHASE(6);
-    select_phase<M>(sm, J, cnt);
+    if (cs > 1) cl.sync();
+    if (!sm.go) break;  // the same decision in every block of the job
+    if (!lead) {        // the leader read last round's partial sums before the barrier
+      clear_round_smem<M>(sm);
+      __syncthreads();
+    }
+    gather_phase<M>(sm, J, sl, lead ? &sm.ntouched : cl.map_shared_rank(&sm.ntouched, 0));
+    if (cs > 1) {
+      cl.sync();
+      if (!lead && tid == 0) sm.ntouched = *cl.map_shared_rank(&sm.ntouched, 0);
+      __syncthreads();
+    }
+    VNM_PHASE(2);
+    process_phase<M>(sm, J, N, sl);
+    if (cs > 1) {
+      cl.sync();
+      if (lead) cluster_reduce<M>(cl, cs, &sm.S[0][0], NSUM);
+    }
+    VNM_PHASE(3);
+    if (lead) {
+      heap_phase<M>(sm);
+      VNM_PHASE(4);
+      walk_phase<M>(sm, J.sched);
+      __syncthreads();
+      VNM_PHASE(5);
+      if (tid == 0 && J.trace_pairs) {
+        for (int q = 0; q < sm.nswaps; ++q) {
+          if (committed < J.trace_cap_pairs) {
+            J.trace_pairs[2 * committed] = sm.swaps[2 * q];
+            J.trace_pairs[2 * committed + 1] = sm.swaps[2 * q + 1];
+          }
+          ++committed;
+        }
+        if (round - 1 < J.trace_cap_rounds) J.trace_rounds[round - 1] = committed;
+      }
+      sumE += (unsigned)sm.E;
+      sumT += (unsigned)sm.ntouched;
+      for (int r = 1; r < cs; ++r) {  // where each bit of the round's segments goes
+        RoundSmem<M>* rs = cl.map_shared_rank(&sm, r);
+        if (tid < K * M) (&rs->dest[0][0])[tid] = (&sm.dest[0][0])[tid];
+      }
+    }
+    if (cs > 1) cl.sync();
+    apply_recount<M>(sm, J, N, sl);
+    if (cs > 1) {
+      cl.sync();
+      if (lead) cluster_reduce<M>(cl, cs, &sm.newinv[0], 2 * K);
+    }
+    if (lead) {
+      apply_finish<M>(sm, J, cnt);
+      clear_round_smem<M>(sm);
+      __syncthreads();
+      VNM_PHASE(6);
+      select_phase<M>(sm, J, cnt);
+    }
     round += 1;
-    if (sm.status != JOB_OK) break;
   }
 #undef VNM_PHASE
+  if (!lead) return;
   if (cnt_in_smem)
     for (int s = tid; s < J.nseg; s += NM_THREADS) J.cnt[s] = smem_cnt[s];
   if (tid == 0) {
@@ -1112,29 +1210,65 @@ static vnm_status make_job(vnm_ctx* ctx, const Pattern& P, int sched, int maxite
 constexpr size_t NM_SMEM_BUDGET = 200u << 10;
 
 template <int M>
-static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, int N, int max_nseg) {
+static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, int N, int max_nseg, int cs) {
   const size_t cbytes = (size_t)max_nseg * sizeof(int);
   const int in_smem = cbytes <= (64u << 10) ? 1 : 0;
   const size_t fixed = sizeof(RoundSmem<M>) + (in_smem ? cbytes : 0);
   int ts = 8192;
   while (ts >= 1024 && fixed + (size_t)ts * sizeof(uint4) > NM_SMEM_BUDGET) ts >>= 1;
-  if (ts < 1024) ts = 0;
+  if (ts < 1024 || cs > 1) ts = 0;  // the shared-memory row table serves single-block jobs
   const size_t dyn = (size_t)ts * sizeof(uint4) + (in_smem ? cbytes : 0);
   if (dyn > 48u * 1024u)
     VNM_CUDA_TRY(cudaFuncSetAttribute(k_nm_rounds<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-  VNM_LAUNCH(ctx, k_nm_rounds<M>, njobs, NM_THREADS, dyn, d_jobs, N, in_smem, ts);
+  if (cs > 1) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(njobs * cs));
+    cfg.blockDim = dim3(NM_THREADS);
+    cfg.dynamicSmemBytes = dyn;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, k_nm_rounds<M>, &cfg) != cudaSuccess || nclusters < 1) {
+      (void)cudaGetLastError();
+      cs = 1;  // this GPU cannot co-schedule the cluster: one block per job
+    } else {
+      VNM_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_nm_rounds<M>, d_jobs, N, in_smem, ts, cs));
+      ctx->launches++;
+      return VNM_OK;
+    }
+    ts = 8192;
+    while (ts >= 1024 && fixed + (size_t)ts * sizeof(uint4) > NM_SMEM_BUDGET) ts >>= 1;
+    if (ts < 1024) ts = 0;
+    const size_t dyn1 = (size_t)ts * sizeof(uint4) + (in_smem ? cbytes : 0);
+    if (dyn1 > 48u * 1024u)
+      VNM_CUDA_TRY(cudaFuncSetAttribute(k_nm_rounds<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn1));
+    VNM_LAUNCH(ctx, k_nm_rounds<M>, njobs, NM_THREADS, dyn1, d_jobs, N, in_smem, ts, 1);
+    return VNM_OK;
+  }
+  VNM_LAUNCH(ctx, k_nm_rounds<M>, njobs, NM_THREADS, dyn, d_jobs, N, in_smem, ts, 1);
   return VNM_OK;
 }
 
-static vnm_status launch_rounds(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, int N, int M, int max_nseg) {
+// Blocks per job: a cluster of NM_CLUSTER blocks for calls with few jobs
+// (one matrix, or its four schedules), one block each for batches.
+constexpr int NM_CLUSTER = 8;
+
+static vnm_status launch_rounds(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, int N, int M, int max_nseg,
+                                int cs = 1) {
   switch (M) {
-    case 2: return launch_rounds_t<2>(ctx, d_jobs, njobs, N, max_nseg);
-    case 3: return launch_rounds_t<3>(ctx, d_jobs, njobs, N, max_nseg);
-    case 4: return launch_rounds_t<4>(ctx, d_jobs, njobs, N, max_nseg);
-    case 5: return launch_rounds_t<5>(ctx, d_jobs, njobs, N, max_nseg);
-    case 6: return launch_rounds_t<6>(ctx, d_jobs, njobs, N, max_nseg);
-    case 7: return launch_rounds_t<7>(ctx, d_jobs, njobs, N, max_nseg);
-    case 8: return launch_rounds_t<8>(ctx, d_jobs, njobs, N, max_nseg);
+    case 2: return launch_rounds_t<2>(ctx, d_jobs, njobs, N, max_nseg, cs);
+    case 3: return launch_rounds_t<3>(ctx, d_jobs, njobs, N, max_nseg, cs);
+    case 4: return launch_rounds_t<4>(ctx, d_jobs, njobs, N, max_nseg, cs);
+    case 5: return launch_rounds_t<5>(ctx, d_jobs, njobs, N, max_nseg, cs);
+    case 6: return launch_rounds_t<6>(ctx, d_jobs, njobs, N, max_nseg, cs);
+    case 7: return launch_rounds_t<7>(ctx, d_jobs, njobs, N, max_nseg, cs);
+    case 8: return launch_rounds_t<8>(ctx, d_jobs, njobs, N, max_nseg, cs);
   }
   return VNM_ERR_ARG;
 }
@@ -1206,7 +1340,7 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
   if (!d_jobs) return VNM_ERR_NOMEM;
   VNM_CUDA_TRY(cudaMemcpyAsync(d_jobs, hj, sizeof(NMJob) * nsched, cudaMemcpyHostToDevice, ctx->stream));
   VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main0, ctx->stream));
-  VNM_TRY(launch_rounds(ctx, d_jobs, nsched, N, M, P.nseg));
+  VNM_TRY(launch_rounds(ctx, d_jobs, nsched, N, M, P.nseg, NM_CLUSTER));
   VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main1, ctx->stream));
   int* hres = ctx->h_pinned;
   for (int s = 0; s < nsched; ++s)
