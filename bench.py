@@ -354,10 +354,13 @@ def run_ours(args, rank, world, local):
         "e2e": {"value": e2e_value, "unit": "hot-path steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": 1000.0 * e2e_t / args.steps},
         "roofline": {"kernel": "k_nm_rounds<4>", "bound": "hbm", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     # dram__bytes_read.sum + dram__bytes_write.sum of one launch, from the ncu
+                     # capture summarised in profiles/k_nm_rounds_c2_rmat16384_m4.md
+                     "traffic": 2.12e6, "traffic_unit": "bytes per launch",
                      "alg_bytes_per_launch": alg_bytes / args.steps,
                      "kernel_ms_per_launch": tot["rounds_kernel_ms"] / args.steps,
-                     "note": "latency-bound sequential greedy (4 thread blocks); see profiles/",
+                     "note": "latency-bound sequential greedy (4 jobs x cluster of 8 blocks); see profiles/",
                      "round_phase_share": {k: round(vv / max(1, sum(phase_sum.values())), 4)
                                            for k, vv in phase_sum.items()}},
         "spmm": {"kernel": "k_spmm_vnm<128>", "useful_tflops": useful / sk / 1e12,
