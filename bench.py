@@ -347,7 +347,8 @@ def run_ours(args, rank, world, local):
         "config": {"workload": WORKLOAD, "nrows": nr, "nnz": nnz, "N": N_NM, "M": M_NM, "V": V, "n_B": N_B,
                    "schedules": 4, "parallelism": "replicas" if world > 1 else "single",
                    "l2": "flushed (256 MB write) before every step", "best_sched": int(best),
-                   "rounds_per_search": int(stt["rounds"] // args.steps)},
+                   "rounds_per_search": int(stt["rounds"] // args.steps),
+                   "blocks_per_job": int(t["stats"]["blocks_per_job"])},
         "breakdown_ms": {"reorder_search": tot["reorder_ms"] / args.steps, "permute": tot["permute_ms"] / args.steps,
                          "compress": tot["compress_ms"] / args.steps, "spmm_call": tot["spmm_call_ms"] / args.steps,
                          "spmm_kernel": tot["spmm_kernel_ms"] / args.steps},

@@ -71,7 +71,8 @@ float vnm_last_main_kernel_ms(const vnm_ctx* ctx);
 /* Work counters of the last NM call (for roofline accounting):
  * out[0] rounds summed over jobs, out[1] column entries gathered,
  * out[2] row records touched, out[3] segments per job, out[4] jobs,
- * out[5] nonzero-valued entries of the pattern, out[8..14] kilocycles
+ * out[5] nonzero-valued entries of the pattern, out[6] thread blocks per
+ * job (the cluster size the launch used), out[8..14] kilocycles
  * spent per round phase (select, choose, gather, process, heap, walk,
  * apply) summed over jobs.  n <= 16 values. */
 vnm_status vnm_last_stats(const vnm_ctx* ctx, long long* out, int n);
@@ -99,8 +100,10 @@ vnm_status vnm_last_stats(const vnm_ctx* ctx, long long* out, int n);
 vnm_status vnm_nm_reorder(vnm_ctx* ctx, int nrows, int nnz, const int* row, const int* col, const float* val,
                           int mem, int N, int M, int sched, int nm_maxiter, int* res5, int* newpos);
 
-/* All four schedules of one matrix in a single persistent launch, one
- * thread block per schedule; then the choice of find_best_2toX
+/* All four schedules of one matrix in a single persistent launch, one job
+ * per schedule (each job on a thread-block cluster of 2-16 blocks, chosen
+ * by matrix size and by what the GPU can co-schedule; vnm_last_stats out[6]
+ * reports it); then the choice of find_best_2toX
  * (main.cu:72-114): the largest improve rate (init_cnt-final_cnt)/init_cnt,
  * ties to the lowest schedule id (the reference breaks ties by wall time).
  * Returns 0 as the best schedule when nnz == 0 or init_size == 0 (main.cu:85).

@@ -123,3 +123,25 @@ def test_errors_are_reported(ctx):
         ctx.nm_reorder(6, r[:0], c[:0], v[:0], 2, 4, 0)  # nrows not a multiple of M
     res, newpos = ctx.nm_reorder(8, r[:0], c[:0], v[:0], 2, 4, 0)  # empty matrix
     assert res.tolist() == [0, 0, 0, 0, 0] and newpos.tolist() == list(range(8))
+
+
+@pytest.mark.parametrize("M", [4, 8])
+def test_cluster_sizes_agree(ctx, M):
+    """Each job runs on a thread-block cluster whose size depends on the
+    matrix; every size gives the oracle's result bit for bit."""
+    import os
+    from vnm_gb300 import synth
+    n, r, c, v = synth.rmat(12, 4096 * 8, 17 + M, "normal")
+    ores, _, _, opos = oracle.nm_run(n, r, c, v, 2, M, 1)
+    old = os.environ.get("VNM_NM_CLUSTER")
+    try:
+        for cs in ("1", "2", "4", "8", "16"):
+            os.environ["VNM_NM_CLUSTER"] = cs
+            res, newpos = ctx.nm_reorder(n, r, c, v, 2, M, 1)
+            assert np.array_equal(res, ores), cs
+            assert np.array_equal(newpos, opos), cs
+    finally:
+        if old is None:
+            os.environ.pop("VNM_NM_CLUSTER", None)
+        else:
+            os.environ["VNM_NM_CLUSTER"] = old

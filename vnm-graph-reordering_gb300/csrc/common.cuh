@@ -53,6 +53,7 @@ struct vnm_ctx {
   float main_ms = 0.f;
   long long stats[16] = {0};  // work counters of the last call
   int launches = 0;
+  int last_cluster = 1;  // blocks per job of the last NM round launch
   DeviceArena arena;
   // pinned staging for small results
   int* h_pinned = nullptr;

@@ -40,6 +40,7 @@
 #include <cooperative_groups.h>
 
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -1218,46 +1219,79 @@ static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, 
   while (ts >= 1024 && fixed + (size_t)ts * sizeof(uint4) > NM_SMEM_BUDGET) ts >>= 1;
   if (ts < 1024 || cs > 1) ts = 0;  // the shared-memory row table serves single-block jobs
   const size_t dyn = (size_t)ts * sizeof(uint4) + (in_smem ? cbytes : 0);
-  if (dyn > 48u * 1024u)
-    VNM_CUDA_TRY(cudaFuncSetAttribute(k_nm_rounds<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+  // static + dynamic shared memory may pass the 48 KB a launch gets without
+  // opting in (RoundSmem<8> alone is ~30 KB)
+  VNM_CUDA_TRY(cudaFuncSetAttribute(k_nm_rounds<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+  if (cs > 8)
+    VNM_CUDA_TRY(cudaFuncSetAttribute(k_nm_rounds<M>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   if (cs > 1) {
+    // How many clusters of a size the GPU can hold at once depends on the
+    // SMs of each of its GPCs; take the largest size (halving from cs) at
+    // which every job of the call runs concurrently, else the largest that
+    // fits at all.
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)(njobs * cs));
     cfg.blockDim = dim3(NM_THREADS);
     cfg.dynamicSmemBytes = dyn;
     cfg.stream = ctx->stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = (unsigned)cs;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    int nclusters = 0;
-    if (cudaOccupancyMaxActiveClusters(&nclusters, k_nm_rounds<M>, &cfg) != cudaSuccess || nclusters < 1) {
-      (void)cudaGetLastError();
-      cs = 1;  // this GPU cannot co-schedule the cluster: one block per job
-    } else {
-      VNM_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_nm_rounds<M>, d_jobs, N, in_smem, ts, cs));
+    int pick = 1, fallback = 1;
+    for (int c = cs; c > 1; c >>= 1) {
+      attr[0].val.clusterDim.x = (unsigned)c;
+      cfg.gridDim = dim3((unsigned)(njobs * c));
+      int nclusters = 0;
+      if (cudaOccupancyMaxActiveClusters(&nclusters, k_nm_rounds<M>, &cfg) != cudaSuccess) {
+        (void)cudaGetLastError();
+        continue;
+      }
+      if (nclusters >= 1 && fallback == 1) fallback = c;
+      if (nclusters >= njobs) {
+        pick = c;
+        break;
+      }
+    }
+    if (pick == 1) pick = fallback;
+    if (pick > 1) {
+      attr[0].val.clusterDim.x = (unsigned)pick;
+      cfg.gridDim = dim3((unsigned)(njobs * pick));
+      VNM_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_nm_rounds<M>, d_jobs, N, in_smem, ts, pick));
       ctx->launches++;
+      ctx->last_cluster = pick;
       return VNM_OK;
     }
+    // no cluster fits: one block per job, with the shared-memory row table
     ts = 8192;
     while (ts >= 1024 && fixed + (size_t)ts * sizeof(uint4) > NM_SMEM_BUDGET) ts >>= 1;
     if (ts < 1024) ts = 0;
     const size_t dyn1 = (size_t)ts * sizeof(uint4) + (in_smem ? cbytes : 0);
-    if (dyn1 > 48u * 1024u)
-      VNM_CUDA_TRY(cudaFuncSetAttribute(k_nm_rounds<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn1));
+    VNM_CUDA_TRY(cudaFuncSetAttribute(k_nm_rounds<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn1));
     VNM_LAUNCH(ctx, k_nm_rounds<M>, njobs, NM_THREADS, dyn1, d_jobs, N, in_smem, ts, 1);
+    ctx->last_cluster = 1;
     return VNM_OK;
   }
   VNM_LAUNCH(ctx, k_nm_rounds<M>, njobs, NM_THREADS, dyn, d_jobs, N, in_smem, ts, 1);
+  ctx->last_cluster = 1;
   return VNM_OK;
 }
 
-// Blocks per job: a cluster of NM_CLUSTER blocks for calls with few jobs
-// (one matrix, or its four schedules), one block each for batches.
-constexpr int NM_CLUSTER = 8;
+// Blocks per job for calls with few jobs (one matrix, or its four
+// schedules); batches run one block per job.  Measured on GB300 (find_best,
+// four jobs): R-MAT 16384 2:4 (228 K entries) 59 / 40 / 32 / 27 / 27 ms and
+// R-MAT 65536 2:8 (1.8 M entries) 4111 / 2204 / 1323 / 880 / 709 ms with 1 /
+// 2 / 4 / 8 / 16 blocks, so 16 (a non-portable cluster size) from 1 M
+// pattern entries on, 8 below.  VNM_NM_CLUSTER (1..16) in the environment
+// overrides the choice.
+static int nm_cluster_size(long long np) {
+  if (const char* e = getenv("VNM_NM_CLUSTER")) {
+    const int v = atoi(e);
+    if (v >= 1 && v <= 16) return v;
+  }
+  return np >= (1ll << 20) ? 16 : 8;
+}
 
 static vnm_status launch_rounds(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, int N, int M, int max_nseg,
                                 int cs = 1) {
@@ -1340,7 +1374,7 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
   if (!d_jobs) return VNM_ERR_NOMEM;
   VNM_CUDA_TRY(cudaMemcpyAsync(d_jobs, hj, sizeof(NMJob) * nsched, cudaMemcpyHostToDevice, ctx->stream));
   VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main0, ctx->stream));
-  VNM_TRY(launch_rounds(ctx, d_jobs, nsched, N, M, P.nseg, NM_CLUSTER));
+  VNM_TRY(launch_rounds(ctx, d_jobs, nsched, N, M, P.nseg, nm_cluster_size(P.np)));
   VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main1, ctx->stream));
   int* hres = ctx->h_pinned;
   for (int s = 0; s < nsched; ++s)
@@ -1353,6 +1387,7 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
   ctx->stats[3] = P.nseg;
   ctx->stats[4] = nsched;
   ctx->stats[5] = P.np;
+  ctx->stats[6] = ctx->last_cluster;
   for (int s = 0; s < nsched; ++s) {
     const int* h = hres_copy + 24 * s;
     if (h[5] != 0) return VNM_ERR_INTERNAL;

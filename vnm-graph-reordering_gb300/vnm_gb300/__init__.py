@@ -153,8 +153,8 @@ class Context:
     def last_stats(self):
         out = (ctypes.c_longlong * 16)()
         _check(lib().vnm_last_stats(self.h, out, 16), "vnm_last_stats")
-        keys = ("rounds", "gathered", "touched", "nseg", "jobs", "pattern_nnz")
-        d = dict(zip(keys, list(out)[:6]))
+        keys = ("rounds", "gathered", "touched", "nseg", "jobs", "pattern_nnz", "blocks_per_job")
+        d = dict(zip(keys, list(out)[:7]))
         d["phase_kcycles"] = dict(zip(("select", "choose", "gather", "process", "heap", "walk", "apply"),
                                       list(out)[8:15]))
         return d
