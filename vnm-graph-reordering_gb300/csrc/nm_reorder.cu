@@ -624,9 +624,10 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
       return;
     }
     // solo terms
-#pragma unroll
-    for (int xi = 0; xi < K; ++xi) {
-      const unsigned s = p[xi] == N + 1 ? b[xi] : 0u;
+#pragma unroll 1
+    for (int xi = 0; xi < Kn; ++xi) {
+      const unsigned bx = valid ? rec_byte(w, xi) : 0u;
+      const unsigned s = __popc(bx) == N + 1 ? bx : 0u;
       if (__ballot_sync(FULL, s != 0u) == 0u) continue;
 #pragma unroll
       for (int k = 0; k < M; ++k) {
@@ -634,16 +635,29 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
         if (lane == k && v) atomicAdd(&sm.S[xi][k], __popc(v));
       }
     }
-    // pair corrections
+    // pair corrections, over the segment pairs that some row of this warp
+    // holds both of (a compact loop: the pair body is emitted once)
+    unsigned segs = 0;
 #pragma unroll
-    for (int a = 0; a < K; ++a) {
+    for (int xi = 0; xi < K; ++xi) segs |= (b[xi] != 0u ? 1u : 0u) << xi;
+    unsigned wsegs = __popc(segs) >= 2 ? segs : 0u;
 #pragma unroll
-      for (int c = a + 1; c < K; ++c) {
-        const bool both = b[a] != 0u && b[c] != 0u;
+    for (int o = 16; o > 0; o >>= 1) wsegs |= __shfl_xor_sync(FULL, wsegs, o);
+#pragma unroll 1
+    for (unsigned sa = wsegs; sa; sa &= sa - 1) {
+      const int a = __ffs(sa) - 1;
+      const unsigned Lf = valid ? rec_byte(w, a) : 0u;
+      const int pa = __popc(Lf);
+#pragma unroll 1
+      for (unsigned sc = sa & (sa - 1); sc; sc &= sc - 1) {
+        const int c = __ffs(sc) - 1;
+        const unsigned Rf = valid ? rec_byte(w, c) : 0u;
+        const bool both = Lf != 0u && Rf != 0u;
         if (__ballot_sync(FULL, both) == 0u) continue;
-        const unsigned L = both ? b[a] : 0u, Rb = both ? b[c] : 0u;
-        const unsigned eL = p[a] == N + 1 ? L : (p[a] == N ? (~L & MASK) : 0u);
-        const unsigned eR = p[c] == N + 1 ? Rb : (p[c] == N ? (~Rb & MASK) : 0u);
+        const int pc = __popc(Rf);
+        const unsigned L = both ? Lf : 0u, Rb = both ? Rf : 0u;
+        const unsigned eL = pa == N + 1 ? L : (pa == N ? (~L & MASK) : 0u);
+        const unsigned eR = pc == N + 1 ? Rb : (pc == N ? (~Rb & MASK) : 0u);
         unsigned vL[M], vR[M], vE[M], vF[M];  // ballots of L_i, R_j, eL_i, eR_j
 #pragma unroll
         for (int k = 0; k < M; ++k) {
@@ -690,14 +704,56 @@ __device__ void heap_phase(RoundSmem<M>& sm) {
   if (t < Kn * Kn) {
     const int a = t / Kn, b = t % Kn;
     if (a != b || sm.mode == 2) {
-      int64_t key[MM];
-      uint8_t heap[MM];
-      for (int idx = 0; idx < MM; ++idx) {
+      // the sift steps of swap_heap_pop_order, with each entry's key kept
+      // beside it in the heap so a comparison is one load, not two
+      int64_t hk[MM];
+      uint8_t hi[MM];
+      for (int len = 0; len < MM; ++len) {  // MM pushes
         int l, r;
-        pair_gains<M>(sm, a, b, idx, l, r);
-        key[idx] = swap_key(l, r);
+        pair_gains<M>(sm, a, b, len, l, r);
+        const int64_t kv = swap_key(l, r);
+        int hole = len, parent = (hole - 1) / 2;
+        while (hole > 0 && hk[parent] <= kv) {
+          hk[hole] = hk[parent];
+          hi[hole] = hi[parent];
+          hole = parent;
+          parent = (hole - 1) / 2;
+        }
+        hk[hole] = kv;
+        hi[hole] = (uint8_t)len;
       }
-      swap_heap_pop_order(MM, key, heap, sm.ord[a * K + b]);
+      uint8_t* ord = sm.ord[a * K + b];
+      for (int len = MM, k = 0; len > 0; --len, ++k) {  // MM pops
+        ord[k] = hi[0];
+        if (len > 1) {
+          const int last = len - 1;
+          const int64_t kv = hk[last];
+          const uint8_t v = hi[last];
+          int hole = 0, second = 0;
+          while (second < (last - 1) / 2) {
+            second = 2 * (second + 1);
+            if (hk[second] <= hk[second - 1]) second--;
+            hk[hole] = hk[second];
+            hi[hole] = hi[second];
+            hole = second;
+          }
+          if ((last & 1) == 0 && second == (last - 2) / 2) {
+            second = 2 * (second + 1);
+            hk[hole] = hk[second - 1];
+            hi[hole] = hi[second - 1];
+            hole = second - 1;
+          }
+          int parent = (hole - 1) / 2;
+          while (hole > 0 && hk[parent] <= kv) {
+            hk[hole] = hk[parent];
+            hi[hole] = hi[parent];
+            hole = parent;
+            parent = (hole - 1) / 2;
+          }
+          hk[hole] = kv;
+          hi[hole] = v;
+        }
+      }
     }
   }
   __syncthreads();
@@ -826,7 +882,6 @@ __device__ void walk_phase(RoundSmem<M>& sm, int sched) {
 // slice of the touched rows into newinv / newpres.
 template <int M>
 __device__ void apply_recount(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl) {
-  constexpr int K = M + 1;
   const int tid = threadIdx.x;
   // a round's swaps are disjoint transpositions (the walk never reuses a
   // visited position), so each thread applies one of them
@@ -839,29 +894,29 @@ __device__ void apply_recount(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl)
   const int Kn = sm.K_;
   const int lane = tid & 31;
   for_rows_warp<M>(sm, J, sl, [&](int r, const uint4& w, bool valid) {
-    unsigned nb[K];
-#pragma unroll
-    for (int xi = 0; xi < K; ++xi) nb[xi] = 0;
-#pragma unroll
-    for (int xi = 0; xi < K; ++xi) {
-      if (xi >= Kn) break;
+    // the row's groups after the swaps, packed like the record (4 segments
+    // per word)
+    unsigned n0 = 0, n1 = 0, n2 = 0;
+#pragma unroll 1
+    for (int xi = 0; xi < Kn; ++xi) {
       unsigned bb = valid ? rec_byte(w, xi) : 0u;
       while (bb) {
         const int k = __ffs(bb) - 1;
         bb &= bb - 1;
         const int d = sm.dest[xi][k];
         const int dx = d >> 4, dk = d & 15;
-#pragma unroll
-        for (int z = 0; z < K; ++z)
-          if (z == dx) nb[z] |= 1u << dk;
+        const unsigned bit = (1u << dk) << ((dx & 3) * 8);
+        if (dx < 4) n0 |= bit;
+        else if (dx < 8) n1 |= bit;
+        else n2 |= bit;
       }
     }
     // non-empty and invalid groups per segment, one shared add per warp
-#pragma unroll
-    for (int xi = 0; xi < K; ++xi) {
-      if (xi >= Kn) break;
-      const unsigned pres = __ballot_sync(FULL, nb[xi] != 0u);
-      const unsigned inv = __ballot_sync(FULL, __popc(nb[xi]) > N);
+#pragma unroll 1
+    for (int xi = 0; xi < Kn; ++xi) {
+      const unsigned nb = ((xi < 4 ? n0 : (xi < 8 ? n1 : n2)) >> ((xi & 3) * 8)) & 0xffu;
+      const unsigned pres = __ballot_sync(FULL, nb != 0u);
+      const unsigned inv = __ballot_sync(FULL, __popc(nb) > N);
       if (lane == 0 && pres) atomicAdd(&sm.newpres[xi], __popc(pres));
       if (lane == 0 && inv) atomicAdd(&sm.newinv[xi], __popc(inv));
     }
@@ -888,8 +943,13 @@ __device__ void apply_finish(RoundSmem<M>& sm, const NMJob& J, int* cnt) {
 template <int M>
 __device__ void cluster_reduce(cg::cluster_group& cl, int cs, int* mine, int n) {
   for (int i = threadIdx.x; i < n; i += NM_THREADS) {
-    int v = 0;
-    for (int r = 1; r < cs; ++r) v += cl.map_shared_rank(mine, r)[i];
+    int v = 0, r = 1;
+    for (; r + 3 < cs; r += 4) {  // four remote loads in flight at a time
+      const int a0 = cl.map_shared_rank(mine, r)[i], a1 = cl.map_shared_rank(mine, r + 1)[i];
+      const int a2 = cl.map_shared_rank(mine, r + 2)[i], a3 = cl.map_shared_rank(mine, r + 3)[i];
+      v += (a0 + a1) + (a2 + a3);
+    }
+    for (; r < cs; ++r) v += cl.map_shared_rank(mine, r)[i];
     mine[i] += v;
   }
   __syncthreads();
