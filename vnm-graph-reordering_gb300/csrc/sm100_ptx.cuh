@@ -76,6 +76,17 @@ __device__ __forceinline__ void tma_gather4(void* dst, const void* tmap, int x, 
       : "memory");
 }
 
+// 16-byte global -> shared copy on the load/store path (cp.async).
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+
+// Arrive on `bar` once this thread's earlier cp.async copies have landed;
+// the arrival counts toward the barrier's expected count (.noinc).
+__device__ __forceinline__ void cp_async_mbar_arrive(uint64_t* bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 __device__ __forceinline__ void prefetch_tmap(const void* tmap) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(tmap) : "memory");
 }

@@ -21,10 +21,12 @@
 //   - values are stored divided by their block row's scale (max |a| of the
 //     V rows), and the epilogue multiplies each output row back by it.
 // Kernel: one CTA per (tile, column block of C).  A producer warp streams
-// each K-step's A tile (one bulk copy) and gathers its 16 B rows with TMA
-// tile::gather4 (rows in 128-byte swizzled layout), with the row ids loaded
-// eight K-steps ahead; one thread issues the MMA per K-step; eight stages
-// keep copies in flight while the MMAs run.  Four warps then read the FP32
+// each K-step's A tile (one bulk copy) and copies its 16 B rows with 16-byte
+// cp.async loads into the 128-byte swizzled layout (one warp instruction
+// per 512-byte row; the TMA's tile::gather4 issued too slowly here, one
+// K-step per ~2 us per CTA), with the row ids loaded eight K-steps ahead;
+// one thread issues the MMA per K-step; eight stages keep copies in flight
+// while the MMAs run.  Four warps then read the FP32
 // accumulator out of tensor memory, scale and store it.
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -260,6 +262,8 @@ struct SpmmArgs {
   const int* tile_step;
   const int* cols;
   const unsigned char* a;
+  const unsigned char* B;  // dense operand, row-major, 16-bit values
+  size_t ldb;              // its row stride in bytes
   const float* rscale;
   float* C;
   int R, n, ldc;
@@ -284,7 +288,7 @@ struct SpmmSmem {
 
 template <int NT>
 __global__ void __launch_bounds__(SP_THREADS, 1)
-    k_spmm_vnm(const __grid_constant__ CUtensorMap tmap, SpmmArgs p) {
+    k_spmm_vnm(SpmmArgs p) {
   extern __shared__ unsigned char sp_raw[];
   SpmmSmem<NT>& sm = *reinterpret_cast<SpmmSmem<NT>*>(
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(sp_raw) + 1023) & ~uintptr_t(1023)));
@@ -295,13 +299,12 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
 
   if (tid == 0) {
     for (int s = 0; s < SP_STAGES; ++s) {
-      ptx::mbar_init(&sm.full[s], 1);
+      ptx::mbar_init(&sm.full[s], 1 + 32);  // the A copy's expect-tx arrival + one per producer lane
       ptx::mbar_init(&sm.empty[s], 1);
     }
     ptx::mbar_init(&sm.done, 1);
     sm.abort = 0;
     ptx::fence_mbar_init();
-    ptx::prefetch_tmap(&tmap);
   }
   if (warp == 0) {
     ptx::tmem_alloc(&sm.tmem_base, NT);
@@ -318,7 +321,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
       // producer warp.  Lane l holds column id (l & 15) of K-step
       // i + 2q + (l >> 4) for the SP_PF pairs q ahead (coalesced 128-byte
       // loads issued 2*SP_PF steps before use); lane 0 issues the A tile by
-      // bulk copy and the 16 B rows by gather4 (64 columns each).
+      // bulk copy, and every lane copies its 16-byte pieces of the 16 B rows.
       int pf[SP_PF];
 #pragma unroll
       for (int q = 0; q < SP_PF; ++q) {
@@ -348,22 +351,28 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             stop = true;
             break;
           }
-          int y[16];
-#pragma unroll
-          for (int k = 0; k < 16; ++k) y[k] = __shfl_sync(0xffffffffu, cur, d * 16 + k);
           if (lane == 0) {
-            ptx::mbar_arrive_expect_tx(&sm.full[s], SP_KSTEP_BYTES + 16 * NT * 2);
+            ptx::mbar_arrive_expect_tx(&sm.full[s], SP_KSTEP_BYTES);
             ptx::bulk_g2s(sm.a[s], p.a + (size_t)(s0 + ii) * SP_KSTEP_BYTES, SP_KSTEP_BYTES, &sm.full[s]);
+          }
+          // the 16 B rows: each lane copies 16-byte chunks into the
+          // 128-byte-swizzled layout of the MMA's B operand (atoms of 8 k-rows
+          // x 128 bytes, n-atoms 2048 bytes apart, k-atoms 1024 bytes apart,
+          // chunk j of k-row r stored at chunk j ^ (r % 8))
+          {
+            constexpr int CPR = NT / 8;       // 16-byte chunks per row
+            constexpr int RPI = 32 / CPR;     // rows per warp instruction
+            const int c = lane % CPR, sub = lane / CPR;
+            unsigned char* bs = sm.b[s];
 #pragma unroll
-            for (int g = 0; g < 4; ++g) {
-#pragma unroll
-              for (int h = 0; h < NT / 64; ++h) {
-                // atom (k block g/2, n block h): 8 k-rows x 128 bytes; rows 4(g%2)..
-                unsigned char* dst = sm.b[s] + h * 2048 + (g >> 1) * 1024 + (g & 1) * 512;
-                ptx::tma_gather4(dst, &tmap, n0 + 64 * h, y[4 * g], y[4 * g + 1], y[4 * g + 2], y[4 * g + 3],
-                                 &sm.full[s]);
-              }
+            for (int kr0 = 0; kr0 < 16; kr0 += RPI) {
+              const int kr = kr0 + sub;
+              const int row = __shfl_sync(0xffffffffu, cur, d * 16 + kr);
+              const unsigned char* src = p.B + (size_t)row * p.ldb + (size_t)(n0 + 8 * c) * 2;
+              unsigned char* dst = bs + (c >> 3) * 2048 + (kr >> 3) * 1024 + (kr & 7) * 128 + (((c & 7) ^ (kr & 7)) << 4);
+              ptx::cp_async16(dst, src);
             }
+            ptx::cp_async_mbar_arrive(&sm.full[s]);
           }
           __syncwarp();
           issued = ii + 1;
@@ -378,6 +387,9 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
           sm.abort = 1;
           break;
         }
+        // the B rows were written by the load/store path: order them before
+        // the tensor core reads shared memory
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         ptx::tc_fence_after();
         const uint64_t adesc = ptx::smem_desc(ptx::smem_addr(sm.a[s]), 128, 256, 0);
         const uint64_t bdesc = ptx::smem_desc(ptx::smem_addr(sm.b[s]), 2048, 1024, 2);
@@ -429,25 +441,6 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
 // ---------------------------------------------------------------------------
 // Host
 // ---------------------------------------------------------------------------
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-static EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(p);
-    else
-      (void)cudaGetLastError();
-  }
-  return fn;
-}
-
 template <class T>
 static vnm_status compress_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, const int* d_col, const float* d_val,
                              int M, int V, vnm_spmm_matrix* out) {
@@ -529,7 +522,7 @@ static vnm_status compress_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, con
 }
 
 template <int NT>
-static vnm_status launch_spmm(vnm_ctx* ctx, const vnm_spmm_matrix* A, const CUtensorMap& tmap, SpmmArgs& p) {
+static vnm_status launch_spmm(vnm_ctx* ctx, const vnm_spmm_matrix* A, SpmmArgs& p) {
   // at least 100 KB so that at most two CTAs share an SM: two NT <= 256
   // column accumulators fit the SM's 512 tensor-memory columns, so the
   // allocation never has to wait for another CTA
@@ -538,7 +531,7 @@ static vnm_status launch_spmm(vnm_ctx* ctx, const vnm_spmm_matrix* A, const CUte
   VNM_CUDA_TRY(cudaFuncSetAttribute(k_spmm_vnm<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   p.idesc = ptx::idesc_f16(A->dtype == 1 ? 1u : 0u, 0u, 1u, SP_TM, NT);
   dim3 grid(A->ntiles, p.n / NT);
-  VNM_LAUNCH(ctx, k_spmm_vnm<NT>, grid, SP_THREADS, smem, tmap, p);
+  VNM_LAUNCH(ctx, k_spmm_vnm<NT>, grid, SP_THREADS, smem, p);
   return VNM_OK;
 }
 
@@ -608,8 +601,6 @@ vnm_status vnm_spmm_run(vnm_ctx* ctx, const vnm_spmm_matrix* A, const void* B, i
   if (!ctx || !A || !B || !C || n <= 0 || (n % 64) != 0) return VNM_ERR_ARG;
   if (mem != VNM_MEM_HOST && mem != VNM_MEM_DEVICE) return VNM_ERR_ARG;
   if (A->device != ctx->device) return VNM_ERR_ARG;
-  EncodeTiledFn enc = encode_fn();
-  if (!enc) return VNM_ERR_CUDA;
   const size_t bbytes = (size_t)A->R * n * 2, cbytes = (size_t)A->R * n * sizeof(float);
   VNM_TRY(arena_reserve(ctx, (mem == VNM_MEM_HOST ? bbytes + cbytes : 0) + 4096));
   VNM_TRY(pinned_reserve(ctx, 64));
@@ -625,16 +616,6 @@ vnm_status vnm_spmm_run(vnm_ctx* ctx, const vnm_spmm_matrix* A, const void* B, i
   }
   if ((reinterpret_cast<uintptr_t>(dB) & 15) != 0 || (reinterpret_cast<uintptr_t>(dC) & 15) != 0)
     return VNM_ERR_ARG;
-  CUtensorMap tmap;
-  const cuuint64_t gdim[2] = {(cuuint64_t)n, (cuuint64_t)A->R};
-  const cuuint64_t gstride[1] = {(cuuint64_t)n * 2};
-  const cuuint32_t box[2] = {64, 1};
-  const cuuint32_t estr[2] = {1, 1};
-  CUresult cr = enc(&tmap, A->dtype == 1 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2,
-                    const_cast<void*>(dB), gdim, gstride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                    CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (cr != CUDA_SUCCESS) return VNM_ERR_ARG;
   int* err = arena_take<int>(ctx, 1);
   if (!err) return VNM_ERR_NOMEM;
   VNM_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
@@ -642,6 +623,8 @@ vnm_status vnm_spmm_run(vnm_ctx* ctx, const vnm_spmm_matrix* A, const void* B, i
   p.tile_step = A->tile_step;
   p.cols = A->cols;
   p.a = A->a;
+  p.B = static_cast<const unsigned char*>(dB);
+  p.ldb = (size_t)n * 2;
   p.rscale = A->rscale;
   p.C = dC;
   p.R = A->R;
@@ -649,9 +632,9 @@ vnm_status vnm_spmm_run(vnm_ctx* ctx, const vnm_spmm_matrix* A, const void* B, i
   p.ldc = n;
   p.err = err;
   VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main0, ctx->stream));
-  if (n % 256 == 0) VNM_TRY(launch_spmm<256>(ctx, A, tmap, p));
-  else if (n % 128 == 0) VNM_TRY(launch_spmm<128>(ctx, A, tmap, p));
-  else VNM_TRY(launch_spmm<64>(ctx, A, tmap, p));
+  if (n % 256 == 0) VNM_TRY(launch_spmm<256>(ctx, A, p));
+  else if (n % 128 == 0) VNM_TRY(launch_spmm<128>(ctx, A, p));
+  else VNM_TRY(launch_spmm<64>(ctx, A, p));
   VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main1, ctx->stream));
   VNM_CUDA_TRY(cudaMemcpyAsync(ctx->h_pinned, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   if (mem == VNM_MEM_HOST)
