@@ -12,7 +12,7 @@ C ABI.
          flushed before every step
   e2e    the same through the public API with host (pinned) buffers: the
          COO and B go host->device and the permutation and C come back
-  roofline  the persistent reorder kernel (k_nm_rounds, 98 % of the step)
+  roofline  the persistent reorder kernel (k_nm_rounds, 96 % of the step)
          against HBM; the SpMM's issued and useful tensor rates beside it
   cpu_baseline  the CPU port of the reference path (oracle/) on the host cores
 
@@ -138,6 +138,20 @@ def load_tensor_peak():
         with open(p) as f:
             return float(json.load(f)["bf16_tflops"]), "measured (burst)"
     return 1900.0, "fallback"
+
+
+def whole_job_rate(elapsed_s, steps, world, device=None):
+    """Replicas: every rank ran `steps` steps on its own matrix; the job's
+    rate is all ranks' steps over the slowest rank's time (MAX over ranks,
+    on whatever process group is initialised: NCCL in the bench, gloo in
+    the CPU tests).  Returns (steps per second, slowest elapsed)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        x = torch.tensor([elapsed_s], dtype=torch.float64, device=device)
+        dist.all_reduce(x, op=dist.ReduceOp.MAX)
+        elapsed_s = float(x.item())
+    return world * steps / elapsed_s, elapsed_s
 
 
 def workload(rank):
@@ -295,11 +309,7 @@ def run_ours(args, rank, world, local):
     info, best = t["info"], t["best"]
     step_ms = (tot["reorder_ms"] + tot["permute_ms"] + tot["compress_ms"] + tot["spmm_call_ms"]) / args.steps
     elapsed = step_ms * args.steps / 1000.0
-    if world > 1:
-        x = torch.tensor([elapsed], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(x, op=torch.distributed.ReduceOp.MAX)
-        elapsed = float(x.item())
-    value = world * args.steps / elapsed
+    value, elapsed = whole_job_rate(elapsed, args.steps, world, dev)
     # end to end through the public API with pinned host buffers
     step_host()
     barrier()
@@ -311,11 +321,7 @@ def run_ours(args, rank, world, local):
         C = step_host()
         e2e_t += time.perf_counter() - t0
     barrier()
-    if world > 1:
-        x = torch.tensor([e2e_t], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(x, op=torch.distributed.ReduceOp.MAX)
-        e2e_t = float(x.item())
-    e2e_value = world * args.steps / e2e_t
+    e2e_value, e2e_t = whole_job_rate(e2e_t, args.steps, world, dev)
     nnz = len(r)
     h2d = 12 * nnz + 8 * nnz + 4 * nr + 12 * nnz + 2 * nr * N_B
     d2h = 4 * 20 + 4 + 4 * nr + 8 * nnz + 4 * nr * N_B
