@@ -274,22 +274,32 @@ __device__ __forceinline__ void topk_warp_merge(unsigned long long (&a)[K], unsi
   }
 }
 
-// Scan the segment counts: list size, total, first K in both orders.
+__device__ __forceinline__ unsigned long long desc_key(int c, int s) {  // cnt descending, segment ascending
+  return ((unsigned long long)(unsigned)c << 32) | (unsigned)(0xffffffffu - (unsigned)s);
+}
+__device__ __forceinline__ unsigned long long rev_key(int c, int s) {  // cnt ascending, segment descending
+  return ((unsigned long long)(unsigned)(0x7fffffff - c) << 32) | (unsigned)s;
+}
+
+// Scan the segment counts of segments [s_beg, s_end) except the nx listed
+// in xs: list size, total, first K in both orders.
 template <int M>
-__device__ void select_phase(RoundSmem<M>& sm, const NMJob& J, const int* cnt) {
+__device__ void select_range(RoundSmem<M>& sm, const int* cnt, int s_beg, int s_end, const int* xs, int nx) {
   constexpr int K = M + 1;
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   unsigned long long kd[K], kr[K];
 #pragma unroll
   for (int q = 0; q < K; ++q) kd[q] = kr[q] = 0;
   int lsz = 0, tot = 0;
-  for (int s = tid; s < J.nseg; s += NM_THREADS) {
-    const int c = cnt[s];
+  for (int s = s_beg + tid; s < s_end; s += NM_THREADS) {
+    bool skip = false;
+    for (int t = 0; t < nx; ++t) skip |= (xs[t] == s);
+    const int c = skip ? 0 : cnt[s];
     if (c > 0) {
       lsz++;
       tot += c;
-      topk_insert<K>(kd, ((unsigned long long)(unsigned)c << 32) | (unsigned)(0xffffffffu - (unsigned)s));
-      topk_insert<K>(kr, ((unsigned long long)(unsigned)(0x7fffffff - c) << 32) | (unsigned)s);
+      topk_insert<K>(kd, desc_key(c, s));
+      topk_insert<K>(kr, rev_key(c, s));
     }
   }
   topk_warp_merge<K>(kd, sm.wtop[0][w]);
@@ -312,6 +322,61 @@ __device__ void select_phase(RoundSmem<M>& sm, const NMJob& J, const int* cnt) {
   } else if (w == 2) {
     int v0 = lane < RoundSmem<M>::NW ? sm.red32[0][lane] : 0;
     int v1 = lane < RoundSmem<M>::NW ? sm.red32[1][lane] : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      v0 += __shfl_xor_sync(FULL, v0, o);
+      v1 += __shfl_xor_sync(FULL, v1, o);
+    }
+    if (lane == 0) {
+      sm.lsize = v0;
+      sm.ltotal = v1;
+    }
+  }
+  __syncthreads();
+}
+
+// Scan the segment counts: list size, total, first K in both orders.
+template <int M>
+__device__ void select_phase(RoundSmem<M>& sm, const NMJob& J, const int* cnt) {
+  select_range<M>(sm, cnt, 0, J.nseg, nullptr, 0);
+}
+
+// The same result as select_phase after a round, from the other blocks'
+// scans of all segments but this round's (made while the leader ran the
+// heaps and the walk; those counts did not change) and this round's
+// segments with their new counts (leader block of a cluster).
+template <int M>
+__device__ void select_merge(RoundSmem<M>& sm, cg::cluster_group& cl, int cs, const int* cnt) {
+  constexpr int K = M + 1;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  if (w < 2) {  // warp 0 the descending lists, warp 1 the reverse ones
+    unsigned long long a[K];
+#pragma unroll
+    for (int q = 0; q < K; ++q) a[q] = 0;
+    if (lane + 1 < cs) {
+      const RoundSmem<M>* rs = cl.map_shared_rank(&sm, lane + 1);
+#pragma unroll
+      for (int q = 0; q < K; ++q) topk_insert<K>(a, rs->top[w][q]);
+    }
+    if (lane < sm.K_) {
+      const int sg = sm.xseg[lane], c = cnt[sg];
+      if (c > 0) topk_insert<K>(a, w == 0 ? desc_key(c, sg) : rev_key(c, sg));
+    }
+    topk_warp_merge<K>(a, sm.top[w]);
+  } else if (w == 2) {
+    int v0 = 0, v1 = 0;
+    if (lane + 1 < cs) {
+      const RoundSmem<M>* rs = cl.map_shared_rank(&sm, lane + 1);
+      v0 = rs->lsize;
+      v1 = rs->ltotal;
+    }
+    if (lane < sm.K_) {
+      const int c = cnt[sm.xseg[lane]];
+      if (c > 0) {
+        v0 += 1;
+        v1 += c;
+      }
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       v0 += __shfl_xor_sync(FULL, v0, o);
@@ -1051,7 +1116,13 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     process_phase<M>(sm, J, N, sl);
     if (cs > 1) {
       cl.sync();
-      if (lead) cluster_reduce<M>(cl, cs, &sm.S[0][0], NSUM);
+      if (lead) {
+        cluster_reduce<M>(cl, cs, &sm.S[0][0], NSUM);
+      } else {  // while the leader runs the heaps and the walk: next round's scan
+        const int nh = cs - 1, hr = rank - 1;
+        const int sb = (int)((long long)J.nseg * hr / nh), se = (int)((long long)J.nseg * (hr + 1) / nh);
+        select_range<M>(sm, cnt_in_smem ? cl.map_shared_rank(smem_cnt, 0) : J.cnt, sb, se, sm.xseg, sm.K_);
+      }
     }
     VNM_PHASE(3);
     if (lead) {
@@ -1088,7 +1159,8 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
       clear_round_smem<M>(sm);
       __syncthreads();
       VNM_PHASE(6);
-      select_phase<M>(sm, J, cnt);
+      if (cs > 1) select_merge<M>(sm, cl, cs, cnt);
+      else select_phase<M>(sm, J, cnt);
     }
     round += 1;
   }
