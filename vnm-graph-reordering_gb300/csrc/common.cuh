@@ -54,6 +54,10 @@ struct vnm_ctx {
   long long stats[16] = {0};  // work counters of the last call
   int launches = 0;
   int last_cluster = 1;  // blocks per job of the last NM round launch
+  // SpMM column-block widths measured fastest, by (rows, K-steps, B width)
+  long long spmm_tune_key[8][3] = {};
+  int spmm_tune_nt[8] = {};
+  int spmm_tune_next = 0;
   DeviceArena arena;
   // pinned staging for small results
   int* h_pinned = nullptr;

@@ -523,11 +523,12 @@ static vnm_status compress_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, con
 
 template <int NT>
 static vnm_status launch_spmm(vnm_ctx* ctx, const vnm_spmm_matrix* A, SpmmArgs& p) {
-  // at least 100 KB so that at most two CTAs share an SM: two NT <= 256
-  // column accumulators fit the SM's 512 tensor-memory columns, so the
-  // allocation never has to wait for another CTA
+  // enough shared memory that at most 512 / NT CTAs share an SM: their NT
+  // column accumulators then fit the SM's 512 tensor-memory columns, so an
+  // allocation never waits for another CTA (228 KB of shared memory per SM)
+  constexpr size_t floor_bytes = (228u << 10) / (512 / NT + 1) + 1024;
   size_t smem = sizeof(SpmmSmem<NT>) + 1024;
-  if (smem < (100u << 10)) smem = 100u << 10;
+  if (smem < floor_bytes) smem = floor_bytes;
   VNM_CUDA_TRY(cudaFuncSetAttribute(k_spmm_vnm<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   p.idesc = ptx::idesc_f16(A->dtype == 1 ? 1u : 0u, 0u, 1u, SP_TM, NT);
   dim3 grid(A->ntiles, p.n / NT);
@@ -631,10 +632,43 @@ vnm_status vnm_spmm_run(vnm_ctx* ctx, const vnm_spmm_matrix* A, const void* B, i
   p.n = n;
   p.ldc = n;
   p.err = err;
+  // column-block width: the one the context measured fastest for an
+  // operand of this shape and this n (all widths compute the same
+  // products; the first call for a shape times each width once)
+  const long long key[3] = {A->R, A->nsteps, n};
+  int nt = 0;
+  for (int q = 0; q < 8; ++q)
+    if (ctx->spmm_tune_nt[q] && ctx->spmm_tune_key[q][0] == key[0] && ctx->spmm_tune_key[q][1] == key[1] &&
+        ctx->spmm_tune_key[q][2] == key[2])
+      nt = ctx->spmm_tune_nt[q];
+  auto launch_nt = [&](int w) -> vnm_status {
+    if (w == 256) return launch_spmm<256>(ctx, A, p);
+    if (w == 128) return launch_spmm<128>(ctx, A, p);
+    return launch_spmm<64>(ctx, A, p);
+  };
+  if (nt == 0) {
+    const int cand[3] = {256, 128, 64};
+    float best = 0.f;
+    for (int w : cand) {
+      if (n % w) continue;
+      VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main0, ctx->stream));
+      VNM_TRY(launch_nt(w));
+      VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main1, ctx->stream));
+      VNM_CUDA_TRY(cudaEventSynchronize(ctx->ev_main1));
+      float ms = 0.f;
+      VNM_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev_main0, ctx->ev_main1));
+      if (nt == 0 || ms < best) {
+        best = ms;
+        nt = w;
+      }
+    }
+    const int slot = ctx->spmm_tune_next;
+    ctx->spmm_tune_next = (slot + 1) % 8;
+    for (int k = 0; k < 3; ++k) ctx->spmm_tune_key[slot][k] = key[k];
+    ctx->spmm_tune_nt[slot] = nt;
+  }
   VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main0, ctx->stream));
-  if (n % 256 == 0) VNM_TRY(launch_spmm<256>(ctx, A, p));
-  else if (n % 128 == 0) VNM_TRY(launch_spmm<128>(ctx, A, p));
-  else VNM_TRY(launch_spmm<64>(ctx, A, p));
+  VNM_TRY(launch_nt(nt));
   VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main1, ctx->stream));
   VNM_CUDA_TRY(cudaMemcpyAsync(ctx->h_pinned, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   if (mem == VNM_MEM_HOST)
