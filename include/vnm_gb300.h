@@ -297,7 +297,8 @@ vnm_status vnm_spmm_info(const vnm_spmm_matrix* A, long long* info, int n);
  * (device: 16-byte aligned).  The kernel works on column blocks of 256, 128
  * or 64; the first call of a context for an operand shape (rows, K-steps)
  * and n times each width that divides n once and keeps the fastest for
- * later calls (up to 8 shapes per context). */
+ * later calls (up to 8 shapes per context).  VNM_SPMM_WIDTH=64|128|256 in
+ * the environment fixes the width where it divides n. */
 vnm_status vnm_spmm_run(vnm_ctx* ctx, const vnm_spmm_matrix* A, const void* B, int n, float* C, int mem);
 
 vnm_status vnm_spmm_free(vnm_spmm_matrix* A);

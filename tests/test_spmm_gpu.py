@@ -56,3 +56,22 @@ def test_spmm_partial_last_tile_and_empty_tiles(ctx):
     v = np.array([1.5, -2.0, 0.25, 3.0, -1.0], np.float32)
     err, info = _run(ctx, nr, r, c, v, 8, 64, 64, "bf16")
     assert err < TOL
+
+
+@pytest.mark.parametrize("width", [64, 128, 256])
+def test_spmm_every_column_block_width(ctx, width):
+    """The kernel's column-block widths (the call picks one by timing) each
+    match the FP64 oracle; VNM_SPMM_WIDTH fixes the width."""
+    import os
+    from vnm_gb300 import synth
+    old = os.environ.get("VNM_SPMM_WIDTH")
+    os.environ["VNM_SPMM_WIDTH"] = str(width)
+    try:
+        nr, r, c, v = synth.rmat(10, 1024 * 6, 9, "normal")
+        err, info = _run(ctx, nr, r, c, v, 8, 64, 256, "bf16")
+        assert err < TOL, (width, err)
+    finally:
+        if old is None:
+            os.environ.pop("VNM_SPMM_WIDTH", None)
+        else:
+            os.environ["VNM_SPMM_WIDTH"] = old

@@ -32,6 +32,7 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -637,7 +638,11 @@ vnm_status vnm_spmm_run(vnm_ctx* ctx, const vnm_spmm_matrix* A, const void* B, i
   // products; the first call for a shape times each width once)
   const long long key[3] = {A->R, A->nsteps, n};
   int nt = 0;
-  for (int q = 0; q < 8; ++q)
+  if (const char* e = getenv("VNM_SPMM_WIDTH")) {  // a fixed width (64, 128 or 256) that divides n
+    const int w = atoi(e);
+    if ((w == 64 || w == 128 || w == 256) && n % w == 0) nt = w;
+  }
+  for (int q = 0; q < 8 && nt == 0; ++q)
     if (ctx->spmm_tune_nt[q] && ctx->spmm_tune_key[q][0] == key[0] && ctx->spmm_tune_key[q][1] == key[1] &&
         ctx->spmm_tune_key[q][2] == key[2])
       nt = ctx->spmm_tune_nt[q];
