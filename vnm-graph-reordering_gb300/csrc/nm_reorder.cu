@@ -761,9 +761,105 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
 }
 
 // Pop order of every ordered pair's swap heap (fact 4).
+// M <= 5: one warp per ordered pair, lane i holding heap slot i (key and
+// swap id in registers), so every sift step is a few shuffles; the steps
+// are those of swap_heap_pop_order.
+template <int M>
+__device__ void heap_phase_warp(RoundSmem<M>& sm) {
+  constexpr int K = M + 1, MM = M * M;
+  static_assert(MM <= 32, "one heap slot per lane");
+  constexpr int NW = NM_THREADS / 32;
+  const int Kn = sm.K_;
+  const int lane = threadIdx.x & 31;
+  for (int pq = threadIdx.x >> 5; pq < Kn * Kn; pq += NW) {
+    const int a = pq / Kn, b = pq % Kn;
+    if (a == b && sm.mode != 2) continue;
+    long long mykey = 0;  // key of swap `lane`
+    if (lane < MM) {
+      int l, r;
+      pair_gains<M>(sm, a, b, lane, l, r);
+      mykey = swap_key(l, r);
+    }
+    long long hk = 0;  // this lane's heap slot
+    int hi = 0;
+    for (int len = 0; len < MM; ++len) {  // MM pushes
+      const long long kv = __shfl_sync(FULL, mykey, len);
+      int hole = len;
+      while (hole > 0) {
+        const int parent = (hole - 1) >> 1;
+        const long long pk = __shfl_sync(FULL, hk, parent);
+        if (!(pk <= kv)) break;
+        const int pi = __shfl_sync(FULL, hi, parent);
+        if (lane == hole) {
+          hk = pk;
+          hi = pi;
+        }
+        hole = parent;
+      }
+      if (lane == hole) {
+        hk = kv;
+        hi = len;
+      }
+    }
+    uint8_t* ord = sm.ord[a * K + b];
+    for (int len = MM, k = 0; len > 0; --len, ++k) {  // MM pops
+      const int top = __shfl_sync(FULL, hi, 0);
+      if (lane == 0) ord[k] = (uint8_t)top;
+      if (len > 1) {
+        const int last = len - 1;
+        const long long kv = __shfl_sync(FULL, hk, last);
+        const int v = __shfl_sync(FULL, hi, last);
+        int hole = 0, second = 0;
+        while (second < (last - 1) / 2) {
+          second = 2 * (second + 1);
+          const long long k2 = __shfl_sync(FULL, hk, second), k1 = __shfl_sync(FULL, hk, second - 1);
+          const int i2 = __shfl_sync(FULL, hi, second), i1 = __shfl_sync(FULL, hi, second - 1);
+          const bool left = k2 <= k1;
+          if (left) second--;
+          if (lane == hole) {
+            hk = left ? k1 : k2;
+            hi = left ? i1 : i2;
+          }
+          hole = second;
+        }
+        if ((last & 1) == 0 && second == (last - 2) / 2) {
+          second = 2 * (second + 1);
+          const long long k1 = __shfl_sync(FULL, hk, second - 1);
+          const int i1 = __shfl_sync(FULL, hi, second - 1);
+          if (lane == hole) {
+            hk = k1;
+            hi = i1;
+          }
+          hole = second - 1;
+        }
+        while (hole > 0) {  // __push_heap(first, hole, 0, v)
+          const int parent = (hole - 1) >> 1;
+          const long long pk = __shfl_sync(FULL, hk, parent);
+          if (!(pk <= kv)) break;
+          const int pi = __shfl_sync(FULL, hi, parent);
+          if (lane == hole) {
+            hk = pk;
+            hi = pi;
+          }
+          hole = parent;
+        }
+        if (lane == hole) {
+          hk = kv;
+          hi = v;
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
 template <int M>
 __device__ void heap_phase(RoundSmem<M>& sm) {
   constexpr int K = M + 1, MM = M * M;
+  if constexpr (MM <= 32) {
+    heap_phase_warp<M>(sm);
+    return;
+  }
   const int Kn = sm.K_;
   const int t = threadIdx.x;
   if (t < Kn * Kn) {
