@@ -65,17 +65,6 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       : "memory");
 }
 
-// TMA gather of four rows (y0..y3) of a 2-D tensor, starting at column x,
-// box width from the tensor map, into consecutive shared memory.
-__device__ __forceinline__ void tma_gather4(void* dst, const void* tmap, int x, int y0, int y1, int y2, int y3,
-                                            uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(smem_addr(dst)),
-      "l"(tmap), "r"(x), "r"(y0), "r"(y1), "r"(y2), "r"(y3), "r"(smem_addr(bar))
-      : "memory");
-}
-
 // 16-byte global -> shared copy on the load/store path (cp.async).
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
@@ -87,9 +76,6 @@ __device__ __forceinline__ void cp_async_mbar_arrive(uint64_t* bar) {
   asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
-__device__ __forceinline__ void prefetch_tmap(const void* tmap) {
-  asm volatile("prefetch.tensormap [%0];" ::"l"(tmap) : "memory");
-}
 
 // ---- tcgen05 -----------------------------------------------------------------
 // Allocate `ncols` (power of two >= 32) tensor-memory columns; the base
