@@ -482,6 +482,20 @@ def bench_learned_c4(ctx, reps=3):
         out[name] = row
     lw = out["network_top8"]["to_plain"]["wall_ms"]
     out["speedup_to_equal_retained_wall"] = plain_wall / lw
+    # the same two calls with the COO already in HBM (device arrays): the
+    # reorders alone, without the host-to-device copy of the matrix
+    import torch
+    dr, dc, dv = (torch.from_numpy(x).cuda() for x in (r, c, v))
+    torch.cuda.synchronize()
+    dev_plain, dev_net = [], []
+    for _ in range(reps):
+        ctx.nm_search(n, dr, dc, dv, N, M, want_newpos=False)
+        dev_plain.append(ctx.last_kernel_ms)
+        vnm_gb300.nm_learned(ctx, n, dr, dc, dv, N, M, mode=vnm_gb300.LEARNED_MLP, net=net, topk=8, targets=16,
+                             max_rounds=64, patience=3, seed=1, stop_gain=target, want_newpos=False)
+        dev_net.append(ctx.last_kernel_ms)
+    out["inputs_in_hbm"] = {"plain_device_ms": _median(dev_plain), "network_top8_to_plain_device_ms": _median(dev_net),
+                            "speedup": _median(dev_plain) / _median(dev_net)}
     out["retained_converged_vs_plain"] = out["network_top8"]["converged"]["retained"] / max(1, pl["init_retained"])
     X = np.random.default_rng(0).normal(0, 1, (1 << 20, 32)).astype(np.float32)
     ms = []
