@@ -47,6 +47,11 @@ sys.path.insert(0, PKG)
 import numpy as np  # noqa: E402
 
 N_NM, M_NM, V, N_B = 2, 4, 64, 128
+# target segments each proposing segment samples per learned round (swept on
+# GB300 at R-MAT 65536 2:8: 2 / 4 / 8 / 16 / 32 -> 2.9 / 3.0 / 3.2 / 3.6 /
+# 5.7 ms to the plain reorder's retained-nnz with the network, all in 3
+# rounds); 4 keeps the candidate pool wide at little cost
+TARGETS = 4
 WORKLOAD = ("C2: R-MAT 16384x16384 (a=.57,b=.19,c=.19), 131072 edges symmetrised, N(0,1), 2:4, V=64; "
             "find_best_2toX + V:N:M SpMM with B 16384x128 bf16")
 METRIC = "reorder wall-time (find_best_2toX, R-MAT 16384, 2:4) + V:N:M SpMM, as hot-path steps per second"
@@ -473,7 +478,7 @@ def bench_learned_c4(ctx, reps=3):
                 t0 = time.perf_counter()
                 res, pos, _ = vnm_gb300.nm_learned(ctx, n, r, c, v, N, M, mode=mode,
                                                    net=net if mode == vnm_gb300.LEARNED_MLP else None, topk=topk,
-                                                   targets=16, max_rounds=64, patience=3, seed=1, stop_gain=stop)
+                                                   targets=TARGETS, max_rounds=64, patience=3, seed=1, stop_gain=stop)
                 walls.append(1000.0 * (time.perf_counter() - t0))
                 devs.append(ctx.last_kernel_ms)
             row[label] = {"wall_ms": _median(walls), "device_ms": _median(devs), "rounds": res["rounds"],
@@ -491,7 +496,7 @@ def bench_learned_c4(ctx, reps=3):
     for _ in range(reps):
         ctx.nm_search(n, dr, dc, dv, N, M, want_newpos=False)
         dev_plain.append(ctx.last_kernel_ms)
-        vnm_gb300.nm_learned(ctx, n, dr, dc, dv, N, M, mode=vnm_gb300.LEARNED_MLP, net=net, topk=8, targets=16,
+        vnm_gb300.nm_learned(ctx, n, dr, dc, dv, N, M, mode=vnm_gb300.LEARNED_MLP, net=net, topk=8, targets=TARGETS,
                              max_rounds=64, patience=3, seed=1, stop_gain=target, want_newpos=False)
         dev_net.append(ctx.last_kernel_ms)
     out["inputs_in_hbm"] = {"plain_device_ms": _median(dev_plain), "network_top8_to_plain_device_ms": _median(dev_net),
@@ -525,7 +530,7 @@ def bench_gcn_c5(ctx, reps=100):
     net = learned.load(ctx, N, M)
     t0 = time.perf_counter()
     res, newpos, _ = vnm_gb300.nm_learned(ctx, n, r, c, v, N, M, mode=vnm_gb300.LEARNED_MLP, net=net, topk=8,
-                                          targets=16, max_rounds=64, patience=3, seed=1)
+                                          targets=TARGETS, max_rounds=64, patience=3, seed=1)
     reorder_wall = 1000.0 * (time.perf_counter() - t0)
     reorder_dev = ctx.last_kernel_ms
     net.close()
