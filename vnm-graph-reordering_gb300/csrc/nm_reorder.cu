@@ -29,7 +29,7 @@
 //      that touch both segments need the per-(i, j) terms.
 //   4. The pop order of the swap-pair heap is fixed once its gains are known;
 //      the visited filter only skips ahead in it.  So each ordered pair's pop
-//      order is computed once per round by one thread (exact libstdc++ sift
+//      order is computed once per round by one warp (exact libstdc++ sift
 //      steps, swap_heap.h) and the walk reads the first unvisited entry.
 //
 // One thread block runs one job (a matrix and a schedule) for all of its
@@ -202,7 +202,14 @@ struct RoundSmem {
   int S[K][M];                 // S_x(k): rows with bit k set and popcount == N+1
   int CL[NPAIR][MM];           // per unordered pair (a < b): left-side corrections
   int CR[NPAIR][MM];           //                              right-side corrections
-  uint8_t ord[K * K][MM];      // pop order per ordered pair (a * K + b)
+  static constexpr int HSTR = (K * K + 31) / 32 * 32;  // heaps, rounded up to whole warps
+  // Scratch at the head of dynamic shared memory, used by two phases in turn:
+  // the process phase's per-warp row masks (2 x K x M words a warp) and the
+  // heap phase's slots [MM][HSTR] (4 B) and ranks [MM][HSTR] (1 B).
+  static constexpr int PROC_BYTES = NW * 2 * K * M * 4;
+  static constexpr int HEAP_BYTES = MM * HSTR * 5;
+  static constexpr int SCR_U4 = ((PROC_BYTES > HEAP_BYTES ? PROC_BYTES : HEAP_BYTES) + 15) / 16;
+  uint8_t ord[MM][HSTR];       // pop order: ord[k][a * K + b] is the k-th pop of ordered pair (a, b)
   int colstart[K * M];
   int colpre[K * M + 1];
   uint8_t dest[K][M];          // bit moves of this round's swaps: (xi << 4) | k
@@ -662,6 +669,9 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
   const int Kn = sm.K_;
   const bool self = sm.mode == 2;
   const int lane = threadIdx.x & 31;
+  // this warp's row masks: VL[x][k] at vw[2x * M + k], VE[x][k] at vw[(2x + 1) * M + k]
+  extern __shared__ uint4 smem_heap[];
+  unsigned* vw = reinterpret_cast<unsigned*>(smem_heap) + (threadIdx.x >> 5) * (2 * K * M);
   for_rows_warp<M>(sm, J, sl, [&](int r, const uint4& w, bool valid) {
     (void)r;
     unsigned b[K];
@@ -688,232 +698,212 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
       }
       return;
     }
-    // solo terms
+    // Per segment x of the round, over the chunk's rows: VL[x][k] = rows
+    // with bit k, VE[x][k] = rows with bit k of eL, and the solo terms.
+    // Lane k < M keeps the masks of bit k in this warp's scratch.
 #pragma unroll 1
     for (int xi = 0; xi < Kn; ++xi) {
       const unsigned bx = valid ? rec_byte(w, xi) : 0u;
-      const unsigned s = __popc(bx) == N + 1 ? bx : 0u;
-      if (__ballot_sync(FULL, s != 0u) == 0u) continue;
+      if (__ballot_sync(FULL, bx != 0u) == 0u) continue;
+      const int px = __popc(bx);
+      const unsigned ex = px == N + 1 ? bx : (px == N ? (~bx & MASK) : 0u);
+      const unsigned sx = px == N + 1 ? bx : 0u;
+      unsigned vl = 0u, ve = 0u;
 #pragma unroll
       for (int k = 0; k < M; ++k) {
-        const unsigned v = __ballot_sync(FULL, (s >> k) & 1u);
-        if (lane == k && v) atomicAdd(&sm.S[xi][k], __popc(v));
+        const unsigned l = __ballot_sync(FULL, (bx >> k) & 1u);
+        const unsigned e = __ballot_sync(FULL, (ex >> k) & 1u);
+        const unsigned so = __ballot_sync(FULL, (sx >> k) & 1u);
+        if (lane == k) {
+          vl = l;
+          ve = e;
+          if (so) atomicAdd(&sm.S[xi][k], __popc(so));
+        }
+      }
+      if (lane < M) {
+        vw[(2 * xi) * M + lane] = vl;
+        vw[(2 * xi + 1) * M + lane] = ve;
       }
     }
-    // pair corrections, over the segment pairs that some row of this warp
-    // holds both of (a compact loop: the pair body is emitted once)
+    __syncwarp();
+    // Pair corrections, over the segment pairs that some row of this chunk
+    // holds both of.  For the pair (a, c) the masks restricted to rows with
+    // both segments non-empty are VE[a][i] & NZ[c] and VL[c][j] & NZ[a];
+    // VE[a][i] lies inside NZ[a] (eL is empty when L is) and VL[c][j] inside
+    // NZ[c], so CL(i, j) = popc(VE[a][i] & VL[c][j]) and likewise
+    // CR(i, j) = popc(VL[a][i] & VE[c][j]).
     unsigned segs = 0;
 #pragma unroll
     for (int xi = 0; xi < K; ++xi) segs |= (b[xi] != 0u ? 1u : 0u) << xi;
     unsigned wsegs = __popc(segs) >= 2 ? segs : 0u;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) wsegs |= __shfl_xor_sync(FULL, wsegs, o);
+    constexpr int U = (MM + 31) / 32;  // (i, j) entries per lane
 #pragma unroll 1
     for (unsigned sa = wsegs; sa; sa &= sa - 1) {
       const int a = __ffs(sa) - 1;
-      const unsigned Lf = valid ? rec_byte(w, a) : 0u;
-      const int pa = __popc(Lf);
+      unsigned ea[U], la[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = (lane + 32 * u < MM ? lane + 32 * u : 0) / M;
+        ea[u] = vw[(2 * a + 1) * M + i];
+        la[u] = vw[(2 * a) * M + i];
+      }
 #pragma unroll 1
       for (unsigned sc = sa & (sa - 1); sc; sc &= sc - 1) {
         const int c = __ffs(sc) - 1;
-        const unsigned Rf = valid ? rec_byte(w, c) : 0u;
-        const bool both = Lf != 0u && Rf != 0u;
-        if (__ballot_sync(FULL, both) == 0u) continue;
-        const int pc = __popc(Rf);
-        const unsigned L = both ? Lf : 0u, Rb = both ? Rf : 0u;
-        const unsigned eL = pa == N + 1 ? L : (pa == N ? (~L & MASK) : 0u);
-        const unsigned eR = pc == N + 1 ? Rb : (pc == N ? (~Rb & MASK) : 0u);
-        unsigned vL[M], vR[M], vE[M], vF[M];  // ballots of L_i, R_j, eL_i, eR_j
-#pragma unroll
-        for (int k = 0; k < M; ++k) {
-          vL[k] = __ballot_sync(FULL, (L >> k) & 1u);
-          vR[k] = __ballot_sync(FULL, (Rb >> k) & 1u);
-          vE[k] = __ballot_sync(FULL, both && ((eL >> k) & 1u));
-          vF[k] = __ballot_sync(FULL, both && ((eR >> k) & 1u));
-        }
         const int pid = pair_id<M>(a, c);
 #pragma unroll
-        for (int idx0 = 0; idx0 < MM; idx0 += 32) {
-          const int idx = idx0 + lane;
+        for (int u = 0; u < U; ++u) {
+          const int idx = lane + 32 * u;
           if (idx < MM) {
-            const int i = idx / M, j = idx % M;
-            unsigned e_i = 0, l_i = 0, r_j = 0, f_j = 0;
-#pragma unroll
-            for (int k = 0; k < M; ++k) {
-              if (k == i) {
-                e_i = vE[k];
-                l_i = vL[k];
-              }
-              if (k == j) {
-                r_j = vR[k];
-                f_j = vF[k];
-              }
-            }
-            const int cl = __popc(e_i & r_j), cr = __popc(l_i & f_j);
+            const int j = idx % M;
+            const int cl = __popc(ea[u] & vw[(2 * c) * M + j]);
+            const int cr = __popc(la[u] & vw[(2 * c + 1) * M + j]);
             if (cl) atomicAdd(&sm.CL[pid][idx], cl);
             if (cr) atomicAdd(&sm.CR[pid][idx], cr);
           }
         }
       }
     }
+    __syncwarp();  // the masks are read before the next chunk writes them
   });
   __syncthreads();
 }
 
-// Pop order of every ordered pair's swap heap (fact 4).
-// M <= 5: one warp per ordered pair, lane i holding heap slot i (key and
-// swap id in registers), so every sift step is a few shuffles; the steps
-// are those of swap_heap_pop_order.
-template <int M>
-__device__ void heap_phase_warp(RoundSmem<M>& sm) {
-  constexpr int K = M + 1, MM = M * M;
-  static_assert(MM <= 32, "one heap slot per lane");
-  constexpr int NW = NM_THREADS / 32;
-  const int Kn = sm.K_;
-  const int lane = threadIdx.x & 31;
-  for (int pq = threadIdx.x >> 5; pq < Kn * Kn; pq += NW) {
-    const int a = pq / Kn, b = pq % Kn;
-    if (a == b && sm.mode != 2) continue;
-    long long mykey = 0;  // key of swap `lane`
-    if (lane < MM) {
-      int l, r;
-      pair_gains<M>(sm, a, b, lane, l, r);
-      mykey = swap_key(l, r);
-    }
-    long long hk = 0;  // this lane's heap slot
-    int hi = 0;
-    for (int len = 0; len < MM; ++len) {  // MM pushes
-      const long long kv = __shfl_sync(FULL, mykey, len);
-      int hole = len;
-      while (hole > 0) {
-        const int parent = (hole - 1) >> 1;
-        const long long pk = __shfl_sync(FULL, hk, parent);
-        if (!(pk <= kv)) break;
-        const int pi = __shfl_sync(FULL, hi, parent);
-        if (lane == hole) {
-          hk = pk;
-          hi = pi;
-        }
-        hole = parent;
-      }
-      if (lane == hole) {
-        hk = kv;
-        hi = len;
-      }
-    }
-    uint8_t* ord = sm.ord[a * K + b];
-    for (int len = MM, k = 0; len > 0; --len, ++k) {  // MM pops
-      const int top = __shfl_sync(FULL, hi, 0);
-      if (lane == 0) ord[k] = (uint8_t)top;
-      if (len > 1) {
-        const int last = len - 1;
-        const long long kv = __shfl_sync(FULL, hk, last);
-        const int v = __shfl_sync(FULL, hi, last);
-        int hole = 0, second = 0;
-        while (second < (last - 1) / 2) {
-          second = 2 * (second + 1);
-          const long long k2 = __shfl_sync(FULL, hk, second), k1 = __shfl_sync(FULL, hk, second - 1);
-          const int i2 = __shfl_sync(FULL, hi, second), i1 = __shfl_sync(FULL, hi, second - 1);
-          const bool left = k2 <= k1;
-          if (left) second--;
-          if (lane == hole) {
-            hk = left ? k1 : k2;
-            hi = left ? i1 : i2;
-          }
-          hole = second;
-        }
-        if ((last & 1) == 0 && second == (last - 2) / 2) {
-          second = 2 * (second + 1);
-          const long long k1 = __shfl_sync(FULL, hk, second - 1);
-          const int i1 = __shfl_sync(FULL, hi, second - 1);
-          if (lane == hole) {
-            hk = k1;
-            hi = i1;
-          }
-          hole = second - 1;
-        }
-        while (hole > 0) {  // __push_heap(first, hole, 0, v)
-          const int parent = (hole - 1) >> 1;
-          const long long pk = __shfl_sync(FULL, hk, parent);
-          if (!(pk <= kv)) break;
-          const int pi = __shfl_sync(FULL, hi, parent);
-          if (lane == hole) {
-            hk = pk;
-            hi = pi;
-          }
-          hole = parent;
-        }
-        if (lane == hole) {
-          hk = kv;
-          hi = v;
-        }
-      }
-    }
-  }
-  __syncthreads();
-}
-
+// Pop order of every ordered pair's swap heap (fact 4).  The sift steps are
+// those of swap_heap_pop_order; what differs is how a heap is held:
+//  - a comparison needs only the order of two keys, so each swap's 64-bit
+//    key is first replaced by its rank among its heap's keys (how many are
+//    smaller; equal keys get equal ranks), one warp per heap, and a heap
+//    entry becomes one word, rank << 8 | swap index;
+//  - then one thread per heap runs the sift steps on slots kept in shared
+//    memory as [slot][heap], a row being a multiple of 32 words, so every
+//    lane reads and writes its own bank whatever slot it is at;
+//  - the steps are latency chains of dependent loads, so a push loads the
+//    whole ancestor path at once, and a pop walks down on children loaded a
+//    level ahead and writes its path back once (below).
 template <int M>
 __device__ void heap_phase(RoundSmem<M>& sm) {
-  constexpr int K = M + 1, MM = M * M;
-  if constexpr (MM <= 32) {
-    heap_phase_warp<M>(sm);
-    return;
-  }
-  const int Kn = sm.K_;
-  const int t = threadIdx.x;
-  if (t < Kn * Kn) {
-    const int a = t / Kn, b = t % Kn;
-    if (a != b || sm.mode == 2) {
-      // the sift steps of swap_heap_pop_order, with each entry's key kept
-      // beside it in the heap so a comparison is one load, not two
-      int64_t hk[MM];
-      uint8_t hi[MM];
-      for (int len = 0; len < MM; ++len) {  // MM pushes
+  constexpr int K = M + 1, MM = M * M, SL = (MM + 31) / 32;
+  constexpr int HS = RoundSmem<M>::HSTR;
+  constexpr int NW = NM_THREADS / 32;
+  static_assert(MM <= 64, "swap index in 8 bits, rank in 8 bits");
+  constexpr int D = MM <= 4 ? 2 : MM <= 8 ? 3 : MM <= 16 ? 4 : MM <= 32 ? 5 : 6;  // ceil(log2(MM))
+  const int Kn = sm.K_, np = Kn * Kn;
+  const int tid = threadIdx.x, lane = tid & 31;
+  // the scratch heads the kernel's dynamic shared memory (declared here too so
+  // that accesses compile as shared-memory ones)
+  extern __shared__ uint4 smem_heap[];
+  unsigned* slot = reinterpret_cast<unsigned*>(smem_heap);    // [MM][HS]
+  uint8_t* rk8 = reinterpret_cast<uint8_t*>(slot + MM * HS);  // [MM][HS]
+  for (int pq = tid >> 5; pq < np; pq += NW) {  // ranks, one warp per heap
+    const int a = pq / Kn, b = pq % Kn;
+    if (a == b && sm.mode != 2) continue;
+    long long key[SL];
+#pragma unroll
+    for (int q = 0; q < SL; ++q) {
+      const int idx = lane + 32 * q;
+      key[q] = 0;
+      if (idx < MM) {
         int l, r;
-        pair_gains<M>(sm, a, b, len, l, r);
-        const int64_t kv = swap_key(l, r);
-        int hole = len, parent = (hole - 1) / 2;
-        while (hole > 0 && hk[parent] <= kv) {
-          hk[hole] = hk[parent];
-          hi[hole] = hi[parent];
-          hole = parent;
-          parent = (hole - 1) / 2;
-        }
-        hk[hole] = kv;
-        hi[hole] = (uint8_t)len;
+        pair_gains<M>(sm, a, b, idx, l, r);
+        key[q] = swap_key(l, r);
       }
-      uint8_t* ord = sm.ord[a * K + b];
-      for (int len = MM, k = 0; len > 0; --len, ++k) {  // MM pops
-        ord[k] = hi[0];
-        if (len > 1) {
-          const int last = len - 1;
-          const int64_t kv = hk[last];
-          const uint8_t v = hi[last];
-          int hole = 0, second = 0;
-          while (second < (last - 1) / 2) {
-            second = 2 * (second + 1);
-            if (hk[second] <= hk[second - 1]) second--;
-            hk[hole] = hk[second];
-            hi[hole] = hi[second];
-            hole = second;
-          }
-          if ((last & 1) == 0 && second == (last - 2) / 2) {
-            second = 2 * (second + 1);
-            hk[hole] = hk[second - 1];
-            hi[hole] = hi[second - 1];
-            hole = second - 1;
-          }
-          int parent = (hole - 1) / 2;
-          while (hole > 0 && hk[parent] <= kv) {
-            hk[hole] = hk[parent];
-            hi[hole] = hi[parent];
-            hole = parent;
-            parent = (hole - 1) / 2;
-          }
-          hk[hole] = kv;
-          hi[hole] = v;
+    }
+    unsigned rk[SL];
+#pragma unroll
+    for (int q = 0; q < SL; ++q) rk[q] = 0;
+#pragma unroll 8
+    for (int j = 0; j < MM; ++j) {
+      long long kr = key[0];
+#pragma unroll
+      for (int q = 1; q < SL; ++q)
+        if ((j >> 5) == q) kr = key[q];
+      const long long kj = __shfl_sync(FULL, kr, j & 31);
+#pragma unroll
+      for (int q = 0; q < SL; ++q) rk[q] += kj < key[q] ? 1u : 0u;
+    }
+    const int c = a * K + b;  // column of the ordered pair in ord, slots and ranks
+#pragma unroll
+    for (int q = 0; q < SL; ++q)
+      if (lane + 32 * q < MM) rk8[(lane + 32 * q) * HS + c] = (uint8_t)rk[q];
+  }
+  __syncthreads();
+  const int a = tid / Kn, b = tid % Kn, pq = a * K + b;
+  if (tid < np && (a != b || sm.mode == 2)) {
+    unsigned* hs = slot + pq;
+    uint8_t* ord = &sm.ord[0][0] + pq;
+    auto ld = [&](int i) { return hs[(i < MM ? i : MM - 1) * HS]; };
+    // MM pushes: heap.push_back(v); __push_heap(first, len, 0, v).  The
+    // ancestors of `len` are loaded together; keys do not decrease going up
+    // a path, so the entry rises past exactly the ancestors with key <= its own.
+    for (int len = 0; len < MM; ++len) {
+      const unsigned kv = ((unsigned)rk8[len * HS + pq] << 8) | (unsigned)len;
+      int pn[D + 1];
+      unsigned av[D];
+      pn[0] = len;
+#pragma unroll
+      for (int t = 0; t < D; ++t) {
+        pn[t + 1] = pn[t] > 0 ? (pn[t] - 1) >> 1 : 0;
+        av[t] = hs[pn[t + 1] * HS];
+      }
+      int m = 0;
+#pragma unroll
+      for (int t = 0; t < D; ++t) m += (pn[t] > 0 && (av[t] >> 8) <= (kv >> 8)) ? 1 : 0;
+      int pm = pn[0];
+#pragma unroll
+      for (int t = 0; t < D; ++t) {
+        if (t < m) hs[pn[t] * HS] = av[t];
+        if (t + 1 == m) pm = pn[t + 1];
+      }
+      hs[pm * HS] = kv;
+    }
+    // MM pops: pop_heap(first, last) then pop_back().  __adjust_heap's walk
+    // down to a leaf reads only children of the path, so it runs on values
+    // loaded one level ahead, keeps the path in registers, finishes the
+    // __push_heap of the old last entry there, and writes the path once.
+    for (int len = MM, k = 0; len > 0; --len, ++k) {
+      ord[k * HS] = (uint8_t)(hs[0] & 255u);
+      if (len == 1) break;
+      const int last = len - 1, lim = (last - 1) / 2;
+      const unsigned kv = hs[last * HS];
+      unsigned c1 = ld(1), c2 = ld(2), g0 = ld(3), g1 = ld(4), g2 = ld(5), g3 = ld(6);
+      unsigned pv[D + 2];  // values moved up along the path, root first
+      unsigned right = 0;  // bit t: step t of the path went to the right child
+      int d = 0, second = 0;
+#pragma unroll
+      for (int lv = 0; lv < D; ++lv) {
+        if (second < lim) {  // c1, c2: children of `second`; g0..g3: their children
+          const bool left = (c2 >> 8) <= (c1 >> 8);
+          const int x = left ? 2 * second + 1 : 2 * second + 2;
+          pv[lv] = left ? c1 : c2;
+          right |= left ? 0u : 1u << lv;
+          d = lv + 1;
+          second = x;
+          c1 = left ? g0 : g2;
+          c2 = left ? g1 : g3;
+          g0 = ld(4 * x + 3);
+          g1 = ld(4 * x + 4);
+          g2 = ld(4 * x + 5);
+          g3 = ld(4 * x + 6);
         }
+      }
+      if ((last & 1) == 0 && second == (last - 2) / 2) {  // one child left: c1, a left step
+#pragma unroll
+        for (int t = 0; t <= D; ++t)
+          if (t == d) pv[t] = c1;
+        ++d;
+      }
+      int m = 0;
+#pragma unroll
+      for (int t = 0; t <= D; ++t) m += (t < d && (pv[t] >> 8) <= (kv >> 8)) ? 1 : 0;
+      const int cut = d - m;  // kv lands at path position cut, the rest below it move down one
+      int node = 0;
+#pragma unroll
+      for (int t = 0; t <= D + 1; ++t) {
+        if (t <= d) hs[node * HS] = t < cut ? pv[t] : (t == cut ? kv : pv[t > 0 ? t - 1 : 0]);
+        node = 2 * node + 1 + (int)((right >> t) & 1u);
       }
     }
   }
@@ -941,7 +931,7 @@ __device__ void walk_phase(RoundSmem<M>& sm, int sched) {
   if (sm.mode != 0) {
     // |L| == 1: best pair of (top, minseg) with no visited filter (:1837-1860)
     const int b = sm.mode == 2 ? 0 : 1;
-    commit(0, b, sm.ord[0 * K + b][0]);
+    commit(0, b, sm.ord[0][0 * K + b]);
   } else {
     const bool rev_list = sched >= 2;                     // inv_seg_list / updatePQ comparator
     const bool trav_rev = (sched == 1 || sched == 2);     // traversal comparator is cmp_reverse
@@ -988,10 +978,10 @@ __device__ void walk_phase(RoundSmem<M>& sm, int sched) {
         if (pc <= 0 || vis[pxi] == FULLM) break;
         const int txi = T[x];
         int tc = Tc[x];
-        const uint8_t* ord = sm.ord[pxi * K + txi];
+        const uint8_t* ord = &sm.ord[0][pxi * K + txi];  // k-th pop at ord[k * HSTR]
         int pick = -1;
         for (int k = 0; k < MM; ++k) {
-          const int idx = ord[k];
+          const int idx = ord[k * RoundSmem<M>::HSTR];
           if (!((vis[pxi] >> (idx / M)) & 1u) && !((vis[txi] >> (idx % M)) & 1u)) {
             pick = idx;
             break;
@@ -999,7 +989,7 @@ __device__ void walk_phase(RoundSmem<M>& sm, int sched) {
         }
         if (pick < 0) {  // unreachable: a scored target always has an unvisited node
           sm.status |= JOB_EMPTY_HEAP;
-          pick = ord[MM - 1];
+          pick = ord[(MM - 1) * RoundSmem<M>::HSTR];
         }
         int l, r;
         pair_gains<M>(sm, pxi, txi, pick, l, r);
@@ -1134,8 +1124,9 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
   static_assert(offsetof(RoundSmem<M>, newpres) == offsetof(RoundSmem<M>, newinv) + sizeof(int) * K,
                 "newinv, newpres adjacent");
   constexpr int NSUM = K * M + 2 * RoundSmem<M>::NPAIR * RoundSmem<M>::MM;
-  // dynamic shared memory: [row-record table: ts_max x 16 B][segment counts]
-  extern __shared__ uint4 smem_dyn[];
+  // dynamic shared memory: [heap scratch][row-record table: ts_max x 16 B][segment counts]
+  extern __shared__ uint4 smem_heap[];
+  uint4* smem_dyn = smem_heap + RoundSmem<M>::SCR_U4;
   int* smem_cnt = reinterpret_cast<int*>(smem_dyn + ts_max);
   cg::cluster_group cl = cg::this_cluster();
   const int rank = cs > 1 ? (int)cl.block_rank() : 0;
@@ -1284,7 +1275,7 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
 // phases the round kernel uses; orig is the identity here.
 template <int M>
 __global__ void __launch_bounds__(NM_THREADS) k_pair_score(NMJob J, int N, int s1, int s2, int* score) {
-  __shared__ RoundSmem<M> sm;
+  __shared__ RoundSmem<M> sm;  // + RoundSmem<M>::SCR_U4 x 16 B of dynamic scratch
   clear_round_smem<M>(sm);
   if (threadIdx.x == 0) {
     sm.table = nullptr;
@@ -1433,20 +1424,21 @@ static vnm_status make_job(vnm_ctx* ctx, const Pattern& P, int sched, int maxite
   return VNM_OK;
 }
 
-// Shared memory beyond RoundSmem: the segment counts when they are small
-// (<= 64 KB), and a row-record table of up to 8192 16-byte slots in what is
-// left of a 200 KB budget.
+// Shared memory beyond RoundSmem: the swap-heap scratch, the segment counts when
+// they are small (<= 64 KB), and a row-record table of up to 8192 16-byte
+// slots in what is left of a 200 KB budget.
 constexpr size_t NM_SMEM_BUDGET = 200u << 10;
 
 template <int M>
 static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, int N, int max_nseg, int cs) {
   const size_t cbytes = (size_t)max_nseg * sizeof(int);
   const int in_smem = cbytes <= (64u << 10) ? 1 : 0;
-  const size_t fixed = sizeof(RoundSmem<M>) + (in_smem ? cbytes : 0);
+  const size_t hbytes = (size_t)RoundSmem<M>::SCR_U4 * sizeof(uint4);
+  const size_t fixed = sizeof(RoundSmem<M>) + hbytes + (in_smem ? cbytes : 0);
   int ts = 8192;
   while (ts >= 1024 && fixed + (size_t)ts * sizeof(uint4) > NM_SMEM_BUDGET) ts >>= 1;
   if (ts < 1024 || cs > 1) ts = 0;  // the shared-memory row table serves single-block jobs
-  const size_t dyn = (size_t)ts * sizeof(uint4) + (in_smem ? cbytes : 0);
+  const size_t dyn = hbytes + (size_t)ts * sizeof(uint4) + (in_smem ? cbytes : 0);
   // static + dynamic shared memory may pass the 48 KB a launch gets without
   // opting in (RoundSmem<8> alone is ~30 KB)
   VNM_CUDA_TRY(cudaFuncSetAttribute(k_nm_rounds<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
@@ -1495,7 +1487,7 @@ static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, 
     ts = 8192;
     while (ts >= 1024 && fixed + (size_t)ts * sizeof(uint4) > NM_SMEM_BUDGET) ts >>= 1;
     if (ts < 1024) ts = 0;
-    const size_t dyn1 = (size_t)ts * sizeof(uint4) + (in_smem ? cbytes : 0);
+    const size_t dyn1 = hbytes + (size_t)ts * sizeof(uint4) + (in_smem ? cbytes : 0);
     VNM_CUDA_TRY(cudaFuncSetAttribute(k_nm_rounds<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn1));
     VNM_LAUNCH(ctx, k_nm_rounds<M>, njobs, NM_THREADS, dyn1, d_jobs, N, in_smem, ts, 1);
     ctx->last_cluster = 1;
@@ -1944,7 +1936,10 @@ vnm_status vnm_nm_pair_score(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
   switch (M) {
 #define VNM_PS(MM)                                                                          \
   case MM:                                                                                  \
-    VNM_LAUNCH(ctx, k_pair_score<MM>, 1, NM_THREADS, 0, J, N, seg1, seg2, d_score);         \
+    VNM_CUDA_TRY(cudaFuncSetAttribute(k_pair_score<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                      RoundSmem<MM>::SCR_U4 * 16));                                   \
+    VNM_LAUNCH(ctx, k_pair_score<MM>, 1, NM_THREADS, RoundSmem<MM>::SCR_U4 * 16, J, N, seg1, seg2,   \
+               d_score);                                                                              \
     break;
     VNM_PS(2) VNM_PS(3) VNM_PS(4) VNM_PS(5) VNM_PS(6) VNM_PS(7) VNM_PS(8)
 #undef VNM_PS
