@@ -910,123 +910,113 @@ __device__ void heap_phase(RoundSmem<M>& sm) {
   __syncthreads();
 }
 
-// The greedy walk of run_onepair* over this round's segments (thread 0).
+// The greedy walk of run_onepair* over this round's segments, on warp 0.
+// Lane q holds round segment q: its current count and visited bits.  The
+// list is a set (the primary is the list's top and the targets follow in
+// traversal order, both strict total orders on (count, segment)), kept as
+// a lane mask; each step is a few warp votes and shuffles:
+//   - primary: the largest list key among the list's lanes;
+//   - targets: each lane's position in traversal order by comparing keys;
+//   - the first unvisited swap of a pair's pop order: a ballot over all
+//     pops at once;
+//   - each committed swap's bit moves go straight into dest.
+__device__ __forceinline__ unsigned order_key_hi(int c, bool rev) {  // count, order-preserving
+  const unsigned u = (unsigned)c ^ 0x80000000u;
+  return rev ? ~u : u;
+}
+__device__ __forceinline__ unsigned order_key_lo(int s, bool rev) {  // segment: ascending first for cmp
+  return rev ? (unsigned)s : ~(unsigned)s;
+}
+
 template <int M>
 __device__ void walk_phase(RoundSmem<M>& sm, int sched) {
   constexpr int K = M + 1, MM = M * M;
+  constexpr int HS = RoundSmem<M>::HSTR;
   constexpr unsigned FULLM = (1u << M) - 1u;
-  if (threadIdx.x != 0) return;
-  unsigned vis[K];
-#pragma unroll
-  for (int q = 0; q < K; ++q) vis[q] = 0;
+  if (threadIdx.x >= 32) return;
+  const int lane = threadIdx.x;
+  // bit moves of the swaps for the recount (identity elsewhere)
+  for (int t = lane; t < K * M; t += 32) (&sm.dest[0][0])[t] = (uint8_t)(((t / M) << 4) | (t % M));
+  __syncwarp();
   int nsw = 0;
-  auto commit = [&](int a, int b, int idx) {
+  const uint8_t* ord0 = &sm.ord[0][0];
+  auto commit = [&](int a, int b, int idx) {  // lane 0 writes; every lane counts
     const int i = idx / M, j = idx % M;
-    sm.swaps[2 * nsw] = sm.xseg[a] * M + i;
-    sm.swaps[2 * nsw + 1] = sm.xseg[b] * M + j;
+    if (lane == 0) {
+      sm.swaps[2 * nsw] = sm.xseg[a] * M + i;
+      sm.swaps[2 * nsw + 1] = sm.xseg[b] * M + j;
+      sm.dest[a][i] = (uint8_t)((b << 4) | j);
+      sm.dest[b][j] = (uint8_t)((a << 4) | i);
+    }
     ++nsw;
-    vis[a] |= 1u << i;
-    vis[b] |= 1u << j;
   };
   if (sm.mode != 0) {
     // |L| == 1: best pair of (top, minseg) with no visited filter (:1837-1860)
     const int b = sm.mode == 2 ? 0 : 1;
-    commit(0, b, sm.ord[0][0 * K + b]);
+    commit(0, b, ord0[0 * K + b]);
   } else {
-    const bool rev_list = sched >= 2;                     // inv_seg_list / updatePQ comparator
-    const bool trav_rev = (sched == 1 || sched == 2);     // traversal comparator is cmp_reverse
-    int W[K], Wc[K];
-    int nW = sm.K_;
-    for (int q = 0; q < nW; ++q) {
-      W[q] = q;
-      Wc[q] = sm.xcnt[q];
-    }
-    while (nW >= 2) {
-      // primary = top of the list
-      int bp = 0;
-      for (int q = 1; q < nW; ++q) {
-        const int sa = sm.xseg[W[q]], sb = sm.xseg[W[bp]];
-        const bool bef = rev_list ? before_rev(sa, Wc[q], sb, Wc[bp]) : before_cmp(sa, Wc[q], sb, Wc[bp]);
-        if (bef) bp = q;
+    const bool rev_list = sched >= 2;                  // inv_seg_list / updatePQ comparator
+    const bool trav_rev = (sched == 1 || sched == 2);  // traversal comparator is cmp_reverse
+    const int Kn = sm.K_;
+    const int seg = lane < Kn ? sm.xseg[lane] : 0;
+    int cnt = lane < Kn ? sm.xcnt[lane] : 0;
+    unsigned vis = 0;
+    unsigned Wm = (1u << Kn) - 1u;
+    while (__popc(Wm) >= 2) {
+      const bool inW = (Wm >> lane) & 1u;
+      // primary = top of the list (largest key; 0 marks lanes outside it)
+      const unsigned lh = inW ? order_key_hi(cnt, rev_list) : 0u, ll = inW ? order_key_lo(seg, rev_list) : 0u;
+      const unsigned mh = __reduce_max_sync(FULL, lh);
+      const unsigned ml = __reduce_max_sync(FULL, lh == mh ? ll : 0u);
+      const int pxi = __ffs(__ballot_sync(FULL, inW && lh == mh && ll == ml)) - 1;
+      int pc = __shfl_sync(FULL, cnt, pxi);
+      // targets: the rest of the list, by position in traversal order
+      const unsigned Tm = Wm & ~(1u << pxi);
+      const bool isT = (Tm >> lane) & 1u;
+      const unsigned th = isT ? order_key_hi(cnt, trav_rev) : 0u, tl = isT ? order_key_lo(seg, trav_rev) : 0u;
+      int pos = 0;
+      for (int q = 0; q < Kn; ++q) {
+        const unsigned qh = __shfl_sync(FULL, th, q), ql = __shfl_sync(FULL, tl, q);
+        pos += (((Tm >> q) & 1u) && (qh > th || (qh == th && ql > tl))) ? 1 : 0;
       }
-      const int pxi = W[bp];
-      int pc = Wc[bp];
-      // targets: the rest, in traversal order (selection sort, <= M entries)
-      int T[K], Tc[K], nT = 0;
-      for (int q = 0; q < nW; ++q)
-        if (q != bp) {
-          T[nT] = W[q];
-          Tc[nT] = Wc[q];
-          ++nT;
-        }
+      const int nT = __popc(Tm);
+      unsigned Um = 0;
       for (int x = 0; x < nT; ++x) {
-        int best = x;
-        for (int y = x + 1; y < nT; ++y) {
-          const int sa = sm.xseg[T[y]], sb = sm.xseg[T[best]];
-          const bool bef = trav_rev ? before_rev(sa, Tc[y], sb, Tc[best]) : before_cmp(sa, Tc[y], sb, Tc[best]);
-          if (bef) best = y;
-        }
-        int t0 = T[x], t1 = Tc[x];
-        T[x] = T[best];
-        Tc[x] = Tc[best];
-        T[best] = t0;
-        Tc[best] = t1;
-      }
-      int nU = 0;
-      int U[K], Uc[K];
-      for (int x = 0; x < nT; ++x) {
-        if (pc <= 0 || vis[pxi] == FULLM) break;
-        const int txi = T[x];
-        int tc = Tc[x];
-        const uint8_t* ord = &sm.ord[0][pxi * K + txi];  // k-th pop at ord[k * HSTR]
+        const unsigned vp = __shfl_sync(FULL, vis, pxi);
+        if (pc <= 0 || vp == FULLM) break;
+        const int txi = __ffs(__ballot_sync(FULL, isT && pos == x)) - 1;
+        const unsigned vt = __shfl_sync(FULL, vis, txi);
+        int tc = __shfl_sync(FULL, cnt, txi);
+        // first pop of the pair whose two nodes are both unvisited
+        const uint8_t* ord = ord0 + pxi * K + txi;
         int pick = -1;
-        for (int k = 0; k < MM; ++k) {
-          const int idx = ord[k * RoundSmem<M>::HSTR];
-          if (!((vis[pxi] >> (idx / M)) & 1u) && !((vis[txi] >> (idx % M)) & 1u)) {
-            pick = idx;
-            break;
-          }
+#pragma unroll
+        for (int k0 = 0; k0 < MM; k0 += 32) {
+          const int k = k0 + lane;
+          const int e = k < MM ? ord[k * HS] : 0;
+          const bool ok = k < MM && !((vp >> (e / M)) & 1u) && !((vt >> (e % M)) & 1u);
+          const unsigned bal = __ballot_sync(FULL, ok);
+          const int first = __shfl_sync(FULL, e, __ffs(bal | (bal == 0u ? 1u : 0u)) - 1);
+          if (pick < 0 && bal != 0u) pick = first;
         }
         if (pick < 0) {  // unreachable: a scored target always has an unvisited node
-          sm.status |= JOB_EMPTY_HEAP;
-          pick = ord[(MM - 1) * RoundSmem<M>::HSTR];
+          if (lane == 0) sm.status |= JOB_EMPTY_HEAP;
+          pick = ord[(MM - 1) * HS];
         }
         int l, r;
         pair_gains<M>(sm, pxi, txi, pick, l, r);
         commit(pxi, txi, pick);
+        if (lane == pxi) vis |= 1u << (pick / M);
+        if (lane == txi) vis |= 1u << (pick % M);
         pc -= l;
         tc -= r;
-        if (tc > 0) {
-          U[nU] = txi;
-          Uc[nU] = tc;
-          ++nU;
-        }
+        if (lane == txi) cnt = tc;
+        if (tc > 0) Um |= 1u << txi;
       }
-      for (int q = 0; q < nU; ++q) {
-        W[q] = U[q];
-        Wc[q] = Uc[q];
-      }
-      nW = nU;
+      Wm = Um;
     }
   }
-  sm.nswaps = nsw;
-  // bit moves of the swaps for the recount (identity elsewhere)
-  for (int xi = 0; xi < K; ++xi)
-    for (int k = 0; k < M; ++k) sm.dest[xi][k] = (uint8_t)((xi << 4) | k);
-  for (int q = 0; q < nsw; ++q) {
-    const int v1 = sm.swaps[2 * q], v2 = sm.swaps[2 * q + 1];
-    int a = -1, b = -1;
-    for (int xi = 0; xi < sm.K_; ++xi) {
-      if (sm.xseg[xi] == v1 / M && a < 0) a = xi;
-      if (sm.xseg[xi] == v2 / M && b < 0) b = xi;
-    }
-    if (a < 0 || b < 0) {  // every swap lies in this round's segments
-      sm.status |= JOB_BAD_STATE;
-      continue;
-    }
-    sm.dest[a][v1 % M] = (uint8_t)((b << 4) | (v2 % M));
-    sm.dest[b][v2 % M] = (uint8_t)((a << 4) | (v1 % M));
-  }
+  if (lane == 0) sm.nswaps = nsw;
 }
 
 // Apply the swaps to orig[] (the leader block) and recount this block's
