@@ -203,9 +203,11 @@ struct RoundSmem {
   int CL[NPAIR][MM];           // per unordered pair (a < b): left-side corrections
   int CR[NPAIR][MM];           //                              right-side corrections
   static constexpr int HSTR = (K * K + 31) / 32 * 32;  // heaps, rounded up to whole warps
-  // Scratch at the head of dynamic shared memory, used by two phases in turn:
-  // the process phase's per-warp row masks (2 x K x M words a warp) and the
-  // heap phase's slots [MM][HSTR] (4 B) and ranks [MM][HSTR] (1 B).
+  // Scratch at the head of dynamic shared memory, used by three phases in
+  // turn: the process phase's per-warp row masks (2 x K x M words a warp),
+  // the heap phase's slots [MM][HSTR] (4 B) and ranks [MM][HSTR] (1 B), and
+  // the apply phase's bit-move table (K x ceil(M/4) x 16 x 16 B, less than
+  // the row masks).
   static constexpr int PROC_BYTES = NW * 2 * K * M * 4;
   static constexpr int HEAP_BYTES = MM * HSTR * 5;
   static constexpr int SCR_U4 = ((PROC_BYTES > HEAP_BYTES ? PROC_BYTES : HEAP_BYTES) + 15) / 16;
@@ -631,7 +633,7 @@ __device__ __forceinline__ void for_touched_warp(const RoundSmem<M>& sm, const N
 #pragma unroll
     for (int u = 0; u < TOUCH_U; ++u) wv[u] = rv[u] >= 0 ? J.rec[rv[u]] : make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll 1
-    for (int u = 0; u < TOUCH_U; ++u) f(rv[u], wv[u], rv[u] >= 0);
+    for (int u = 0; u < TOUCH_U && (c0 + u * NWt) * 32 < nt; ++u) f(rv[u], wv[u], rv[u] >= 0);
   }
 }
 
@@ -646,7 +648,7 @@ __device__ __forceinline__ void for_rows_warp(const RoundSmem<M>& sm, const NMJo
     for (int base = w * 32; base < sm.ts_max; base += NW * 32) {
       const int slot = base + lane;
       const uint4 v = sm.table[slot];
-      f(slot, v, v.w != 0u);
+      if (__ballot_sync(FULL, v.w != 0u) != 0u) f(slot, v, v.w != 0u);  // f is a no-op on empty slots
     }
   } else {
     for_touched_warp<M>(sm, J, sl, f);
@@ -700,29 +702,27 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
     }
     // Per segment x of the round, over the chunk's rows: VL[x][k] = rows
     // with bit k, VE[x][k] = rows with bit k of eL, and the solo terms.
-    // Lane k < M keeps the masks of bit k in this warp's scratch.
+    // With P1 = rows of popcount N+1 and P0 = rows of popcount N,
+    // VE[x][k] = (VL[x][k] & P1) | (~VL[x][k] & P0) and the solo rows of
+    // bit k are VL[x][k] & P1.  Lane k < M keeps the masks of bit k in this
+    // warp's scratch.
 #pragma unroll 1
     for (int xi = 0; xi < Kn; ++xi) {
       const unsigned bx = valid ? rec_byte(w, xi) : 0u;
       if (__ballot_sync(FULL, bx != 0u) == 0u) continue;
       const int px = __popc(bx);
-      const unsigned ex = px == N + 1 ? bx : (px == N ? (~bx & MASK) : 0u);
-      const unsigned sx = px == N + 1 ? bx : 0u;
-      unsigned vl = 0u, ve = 0u;
+      const unsigned p1 = __ballot_sync(FULL, px == N + 1), p0 = __ballot_sync(FULL, px == N);
+      unsigned vl = 0u;
 #pragma unroll
       for (int k = 0; k < M; ++k) {
         const unsigned l = __ballot_sync(FULL, (bx >> k) & 1u);
-        const unsigned e = __ballot_sync(FULL, (ex >> k) & 1u);
-        const unsigned so = __ballot_sync(FULL, (sx >> k) & 1u);
-        if (lane == k) {
-          vl = l;
-          ve = e;
-          if (so) atomicAdd(&sm.S[xi][k], __popc(so));
-        }
+        if (lane == k) vl = l;
       }
       if (lane < M) {
+        const unsigned so = vl & p1;
+        if (so) atomicAdd(&sm.S[xi][lane], __popc(so));
         vw[(2 * xi) * M + lane] = vl;
-        vw[(2 * xi + 1) * M + lane] = ve;
+        vw[(2 * xi + 1) * M + lane] = so | (~vl & p0);
       }
     }
     __syncwarp();
@@ -1034,22 +1034,42 @@ __device__ void apply_recount(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl)
   }
   const int Kn = sm.K_;
   const int lane = tid & 31;
+  // where the bits of each nibble of each segment's group go, packed like
+  // the record (4 segments per word): one table entry per (segment, nibble
+  // position, nibble value)
+  constexpr int NH = (M + 3) / 4;
+  extern __shared__ uint4 smem_heap[];
+  uint4 (*bitmove)[NH][16] = reinterpret_cast<uint4 (*)[NH][16]>(smem_heap);  // [K][NH][16]
+  static_assert((M + 1) * NH * 16 * 16 <= RoundSmem<M>::PROC_BYTES, "bit-move table fits the scratch");
+  for (int t = tid; t < Kn * NH * 16; t += NM_THREADS) {
+    const int xi = t / (NH * 16), h = (t / 16) % NH, v = t % 16;
+    unsigned o[3] = {0u, 0u, 0u};
+    for (int q = 0; q < 4; ++q) {
+      const int k = 4 * h + q;
+      if (k < M && ((v >> q) & 1)) {
+        const int d = sm.dest[xi][k];
+        const int dx = d >> 4, dk = d & 15;
+        o[dx >> 2] |= (1u << dk) << ((dx & 3) * 8);
+      }
+    }
+    bitmove[xi][h][v] = make_uint4(o[0], o[1], o[2], 0u);
+  }
+  __syncthreads();
   for_rows_warp<M>(sm, J, sl, [&](int r, const uint4& w, bool valid) {
-    // the row's groups after the swaps, packed like the record (4 segments
-    // per word)
+    // the row's groups after the swaps, packed like the record
     unsigned n0 = 0, n1 = 0, n2 = 0;
 #pragma unroll 1
     for (int xi = 0; xi < Kn; ++xi) {
-      unsigned bb = valid ? rec_byte(w, xi) : 0u;
-      while (bb) {
-        const int k = __ffs(bb) - 1;
-        bb &= bb - 1;
-        const int d = sm.dest[xi][k];
-        const int dx = d >> 4, dk = d & 15;
-        const unsigned bit = (1u << dk) << ((dx & 3) * 8);
-        if (dx < 4) n0 |= bit;
-        else if (dx < 8) n1 |= bit;
-        else n2 |= bit;
+      const unsigned bb = valid ? rec_byte(w, xi) : 0u;
+#pragma unroll
+      for (int h = 0; h < NH; ++h) {
+        const unsigned nib = (bb >> (4 * h)) & 15u;
+        if (nib) {
+          const uint4 m = bitmove[xi][h][nib];
+          n0 |= m.x;
+          n1 |= m.y;
+          n2 |= m.z;
+        }
       }
     }
     // non-empty and invalid groups per segment, one shared add per warp
@@ -1416,8 +1436,10 @@ static vnm_status make_job(vnm_ctx* ctx, const Pattern& P, int sched, int maxite
 
 // Shared memory beyond RoundSmem: the swap-heap scratch, the segment counts when
 // they are small (<= 64 KB), and a row-record table of up to 8192 16-byte
-// slots in what is left of a 200 KB budget.
-constexpr size_t NM_SMEM_BUDGET = 200u << 10;
+// slots in what is left of a 150 KB budget (the rest of the SM's 256 KB is L1,
+// which the gather phase's reads of the column pattern live on: 200 KB ran the
+// 256-matrix 2:8 batch 4 % slower).
+constexpr size_t NM_SMEM_BUDGET = 150u << 10;
 
 template <int M>
 static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, int N, int max_nseg, int cs) {
