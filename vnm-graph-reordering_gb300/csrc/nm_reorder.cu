@@ -1167,13 +1167,18 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
   // cycles spent in each phase of a round, measured by thread 0 of the
   // leader at the barriers that end the phases: select, choose, gather,
   // process, heap, walk, apply
-  unsigned long long tph[7] = {0, 0, 0, 0, 0, 0, 0};
-  long long t0 = clock64(), t1;
-#define VNM_PHASE(i)                         \
-  if (tid == 0) {                            \
-    t1 = clock64();                          \
-    tph[i] += (unsigned long long)(t1 - t0); \
-    t0 = t1;                                 \
+  // (in shared memory: only thread 0 uses them, and registers are scarce)
+  __shared__ unsigned long long tph[7];
+  __shared__ long long t0;
+  if (tid == 0) {
+    for (int q = 0; q < 7; ++q) tph[q] = 0;
+    t0 = clock64();
+  }
+#define VNM_PHASE(i)                                     \
+  if (tid == 0) {                                        \
+    const long long t1 = clock64();                      \
+    tph[i] += (unsigned long long)(t1 - t0);             \
+    t0 = t1;                                             \
   }
   if (cs > 1) cl.sync();  // every block's shared memory is set up before any remote access
   for (;;) {
