@@ -60,6 +60,7 @@ constexpr unsigned FULL = 0xffffffffu;
 constexpr int JOB_OK = 0;
 constexpr int JOB_EMPTY_HEAP = 1;   // reference would call top() on an empty queue
 constexpr int JOB_BAD_STATE = 2;    // a count went out of range
+constexpr int JOB_WAIT_LIMIT = 4;   // the walk waited too long for a swap heap's pops
 
 // The part of a job's row work one thread block does: block `rank` of the
 // `cs` blocks (a thread-block cluster) that share the job.
@@ -198,6 +199,8 @@ struct RoundSmem {
   int use_table;    // this round's records are in `table` (else in J.rec)
   int status;
   int nswaps;
+  int hprog[K * K];  // pops of each ordered pair's heap written to ord so far
+  int hstop;         // the walk is done: the heaps may stop
   int go;           // the leader's decision to run another round (copied to every block)
   int S[K][M];                 // S_x(k): rows with bit k set and popcount == N+1
   int CL[NPAIR][MM];           // per unordered pair (a < b): left-side corrections
@@ -782,14 +785,16 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
 //    lane reads and writes its own bank whatever slot it is at;
 //  - the steps are latency chains of dependent loads, so a push loads the
 //    whole ancestor path at once, and a pop walks down on children loaded a
-//    level ahead and writes its path back once (below).
+//    level ahead and writes its path back once (heap_sift);
+//  - the walk rarely needs more than the first few pops of a heap, so the
+//    sift steps run alongside it and stop when it is done.
+// This part ranks the keys (all warps).
 template <int M>
-__device__ void heap_phase(RoundSmem<M>& sm) {
+__device__ void rank_phase(RoundSmem<M>& sm) {
   constexpr int K = M + 1, MM = M * M, SL = (MM + 31) / 32;
   constexpr int HS = RoundSmem<M>::HSTR;
   constexpr int NW = NM_THREADS / 32;
   static_assert(MM <= 64, "swap index in 8 bits, rank in 8 bits");
-  constexpr int D = MM <= 4 ? 2 : MM <= 8 ? 3 : MM <= 16 ? 4 : MM <= 32 ? 5 : 6;  // ceil(log2(MM))
   const int Kn = sm.K_, np = Kn * Kn;
   const int tid = threadIdx.x, lane = tid & 31;
   // the scratch heads the kernel's dynamic shared memory (declared here too so
@@ -829,7 +834,27 @@ __device__ void heap_phase(RoundSmem<M>& sm) {
     for (int q = 0; q < SL; ++q)
       if (lane + 32 * q < MM) rk8[(lane + 32 * q) * HS + c] = (uint8_t)rk[q];
   }
+  if (tid < K * K) sm.hprog[tid] = 0;
+  if (tid == 0) sm.hstop = 0;
   __syncthreads();
+}
+
+// The sift steps of every heap, one thread each (threads 0 .. Kn*Kn - 1),
+// running while the walk warp consumes the pops: after writing pop k of
+// its pair to ord, a thread publishes k + 1 in hprog; it stops early once
+// the walk has set hstop.
+template <int M>
+__device__ void heap_sift(RoundSmem<M>& sm) {
+  constexpr int K = M + 1, MM = M * M;
+  constexpr int HS = RoundSmem<M>::HSTR;
+  constexpr int D = MM <= 4 ? 2 : MM <= 8 ? 3 : MM <= 16 ? 4 : MM <= 32 ? 5 : 6;  // ceil(log2(MM))
+  const int Kn = sm.K_, np = Kn * Kn;
+  const int tid = threadIdx.x;
+  extern __shared__ uint4 smem_heap[];
+  unsigned* slot = reinterpret_cast<unsigned*>(smem_heap);    // [MM][HS]
+  uint8_t* rk8 = reinterpret_cast<uint8_t*>(slot + MM * HS);  // [MM][HS]
+  volatile int* prog = sm.hprog;
+  volatile int* stop = &sm.hstop;
   const int a = tid / Kn, b = tid % Kn, pq = a * K + b;
   if (tid < np && (a != b || sm.mode == 2)) {
     unsigned* hs = slot + pq;
@@ -864,7 +889,10 @@ __device__ void heap_phase(RoundSmem<M>& sm) {
     // loaded one level ahead, keeps the path in registers, finishes the
     // __push_heap of the old last entry there, and writes the path once.
     for (int len = MM, k = 0; len > 0; --len, ++k) {
+      if (*stop) break;
       ord[k * HS] = (uint8_t)(hs[0] & 255u);
+      __threadfence_block();
+      prog[pq] = k + 1;
       if (len == 1) break;
       const int last = len - 1, lim = (last - 1) / 2;
       const unsigned kv = hs[last * HS];
@@ -907,7 +935,6 @@ __device__ void heap_phase(RoundSmem<M>& sm) {
       }
     }
   }
-  __syncthreads();
 }
 
 // The greedy walk of run_onepair* over this round's segments, on warp 0.
@@ -928,13 +955,29 @@ __device__ __forceinline__ unsigned order_key_lo(int s, bool rev) {  // segment:
   return rev ? (unsigned)s : ~(unsigned)s;
 }
 
+// Runs on the block's last warp while heap_sift fills ord: a pair's pops
+// are read as far as its heap has published them, waiting (with a limit)
+// only when the first unvisited swap lies beyond.
+constexpr int WALK_WAIT_LIMIT = 1 << 20;
+
 template <int M>
 __device__ void walk_phase(RoundSmem<M>& sm, int sched) {
   constexpr int K = M + 1, MM = M * M;
   constexpr int HS = RoundSmem<M>::HSTR;
   constexpr unsigned FULLM = (1u << M) - 1u;
-  if (threadIdx.x >= 32) return;
-  const int lane = threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  volatile int* prog = sm.hprog;
+  bool dead = false;  // a wait ran out: the job is failed, finish without reading ord
+  // pops of pair column `col` published so far, once at least `need`; -1 at the limit
+  auto wait_pops = [&](int col, int need) -> int {
+    int avail = __shfl_sync(FULL, prog[col], 0);
+    for (int spin = 0; avail < need; ++spin) {
+      if (spin >= WALK_WAIT_LIMIT) return -1;
+      avail = __shfl_sync(FULL, prog[col], 0);
+    }
+    __threadfence_block();
+    return avail;
+  };
   // bit moves of the swaps for the recount (identity elsewhere)
   for (int t = lane; t < K * M; t += 32) (&sm.dest[0][0])[t] = (uint8_t)(((t / M) << 4) | (t % M));
   __syncwarp();
@@ -953,7 +996,10 @@ __device__ void walk_phase(RoundSmem<M>& sm, int sched) {
   if (sm.mode != 0) {
     // |L| == 1: best pair of (top, minseg) with no visited filter (:1837-1860)
     const int b = sm.mode == 2 ? 0 : 1;
-    commit(0, b, ord0[0 * K + b]);
+    int pick = 0;
+    if (wait_pops(0 * K + b, 1) < 0) dead = true;
+    else pick = ord0[0 * K + b];
+    commit(0, b, pick);
   } else {
     const bool rev_list = sched >= 2;                  // inv_seg_list / updatePQ comparator
     const bool trav_rev = (sched == 1 || sched == 2);  // traversal comparator is cmp_reverse
@@ -987,22 +1033,32 @@ __device__ void walk_phase(RoundSmem<M>& sm, int sched) {
         const int txi = __ffs(__ballot_sync(FULL, isT && pos == x)) - 1;
         const unsigned vt = __shfl_sync(FULL, vis, txi);
         int tc = __shfl_sync(FULL, cnt, txi);
-        // first pop of the pair whose two nodes are both unvisited
-        const uint8_t* ord = ord0 + pxi * K + txi;
-        int pick = -1;
-#pragma unroll
-        for (int k0 = 0; k0 < MM; k0 += 32) {
-          const int k = k0 + lane;
-          const int e = k < MM ? ord[k * HS] : 0;
-          const bool ok = k < MM && !((vp >> (e / M)) & 1u) && !((vt >> (e % M)) & 1u);
-          const unsigned bal = __ballot_sync(FULL, ok);
-          const int first = __shfl_sync(FULL, e, __ffs(bal | (bal == 0u ? 1u : 0u)) - 1);
-          if (pick < 0 && bal != 0u) pick = first;
+        // first pop of the pair whose two nodes are both unvisited, over the
+        // pops published so far, waiting for more while none qualifies
+        const int col = pxi * K + txi;
+        const uint8_t* ord = ord0 + col;
+        int pick = -1, seen = 0;
+        while (pick < 0 && !dead) {
+          if (seen >= MM) {  // unreachable: a scored target always has an unvisited node
+            if (lane == 0) sm.status |= JOB_EMPTY_HEAP;
+            pick = ord[(MM - 1) * HS];
+            break;
+          }
+          const int avail = wait_pops(col, seen + 1);
+          if (avail < 0) {
+            dead = true;
+            break;
+          }
+          for (int k0 = seen; k0 < avail && pick < 0; k0 += 32) {
+            const int k = k0 + lane;
+            const int e = k < avail ? ord[k * HS] : 0;
+            const bool ok = k < avail && !((vp >> (e / M)) & 1u) && !((vt >> (e % M)) & 1u);
+            const unsigned bal = __ballot_sync(FULL, ok);
+            if (bal) pick = __shfl_sync(FULL, e, __ffs(bal) - 1);
+          }
+          seen = avail;
         }
-        if (pick < 0) {  // unreachable: a scored target always has an unvisited node
-          if (lane == 0) sm.status |= JOB_EMPTY_HEAP;
-          pick = ord[(MM - 1) * HS];
-        }
+        if (dead) pick = 0;
         int l, r;
         pair_gains<M>(sm, pxi, txi, pick, l, r);
         commit(pxi, txi, pick);
@@ -1016,7 +1072,11 @@ __device__ void walk_phase(RoundSmem<M>& sm, int sched) {
       Wm = Um;
     }
   }
-  if (lane == 0) sm.nswaps = nsw;
+  if (lane == 0) {
+    sm.nswaps = nsw;
+    if (dead) sm.status |= JOB_WAIT_LIMIT;
+    *(volatile int*)&sm.hstop = 1;
+  }
 }
 
 // Apply the swaps to orig[] (the leader block) and recount this block's
@@ -1228,9 +1288,10 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     }
     VNM_PHASE(3);
     if (lead) {
-      heap_phase<M>(sm);
+      rank_phase<M>(sm);
       VNM_PHASE(4);
-      walk_phase<M>(sm, J.sched);
+      if (tid >= NM_THREADS - 32) walk_phase<M>(sm, J.sched);  // the last warp walks ...
+      else heap_sift<M>(sm);                                   // ... while the heaps pop
       __syncthreads();
       VNM_PHASE(5);
       if (tid == 0 && J.trace_pairs) {
