@@ -145,3 +145,31 @@ def test_cluster_sizes_agree(ctx, M):
             os.environ.pop("VNM_NM_CLUSTER", None)
         else:
             os.environ["VNM_NM_CLUSTER"] = old
+
+
+def _large_gain_matrix():
+    # segments 0..3 at 2:4 each with 3000 rows holding three of their nodes
+    rng = np.random.default_rng(5)
+    n = 8192
+    rs, cs = [rng.integers(0, n, 20000)], [rng.integers(0, n, 20000)]
+    for s in range(4):
+        hub_rows = rng.choice(np.arange(16, n), 3000, replace=False)
+        rs.append(np.repeat(hub_rows, 3))
+        cs.append(np.tile([4 * s, 4 * s + 1, 4 * s + 2], 3000))
+    r, c = np.concatenate(rs), np.concatenate(cs)
+    key = np.unique(r.astype(np.int64) * n + c)
+    r, c = (key // n).astype(np.int32), (key % n).astype(np.int32)
+    return n, r, c, rng.uniform(0.5, 1.0, len(r)).astype(np.float32)
+
+
+def test_large_gains_match_oracle(ctx):
+    """Swap gains beyond +-2047 (four segments with 3000 rows holding three
+    of their nodes, 2:4): the swap heaps order such keys by rank instead of
+    packing them directly; the result is still the oracle's, for every
+    schedule."""
+    n, r, c, v = _large_gain_matrix()
+    for sched in range(4):
+        ores, _, _, opos = oracle.nm_run(n, r, c, v, 2, 4, sched)
+        res, newpos = ctx.nm_reorder(n, r, c, v, 2, 4, sched)
+        assert np.array_equal(res, ores), sched
+        assert np.array_equal(newpos, opos), sched

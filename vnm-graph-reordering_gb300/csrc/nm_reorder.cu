@@ -208,11 +208,11 @@ struct RoundSmem {
   static constexpr int HSTR = (K * K + 31) / 32 * 32;  // heaps, rounded up to whole warps
   // Scratch at the head of dynamic shared memory, used by three phases in
   // turn: the process phase's per-warp row masks (2 x K x M words a warp),
-  // the heap phase's slots [MM][HSTR] (4 B) and ranks [MM][HSTR] (1 B), and
+  // the heap phase's slots [MM][HSTR] and entries [MM][HSTR] (4 B each), and
   // the apply phase's bit-move table (K x ceil(M/4) x 16 x 16 B, less than
   // the row masks).
   static constexpr int PROC_BYTES = NW * 2 * K * M * 4;
-  static constexpr int HEAP_BYTES = MM * HSTR * 5;
+  static constexpr int HEAP_BYTES = MM * HSTR * 8;
   static constexpr int SCR_U4 = ((PROC_BYTES > HEAP_BYTES ? PROC_BYTES : HEAP_BYTES) + 15) / 16;
   uint8_t ord[MM][HSTR];       // pop order: ord[k][a * K + b] is the k-th pop of ordered pair (a, b)
   int colstart[K * M];
@@ -776,10 +776,11 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
 
 // Pop order of every ordered pair's swap heap (fact 4).  The sift steps are
 // those of swap_heap_pop_order; what differs is how a heap is held:
-//  - a comparison needs only the order of two keys, so each swap's 64-bit
-//    key is first replaced by its rank among its heap's keys (how many are
-//    smaller; equal keys get equal ranks), one warp per heap, and a heap
-//    entry becomes one word, rank << 8 | swap index;
+//  - a comparison needs only the order of two keys, so a heap entry is one
+//    word, key << 8 | swap index, where the key is (l + r, r) packed in
+//    12 + 12 bits when every gain of the heap fits, else the 64-bit key's
+//    rank among the heap's keys (how many are smaller; equal keys get equal
+//    ranks), computed by one warp per heap;
 //  - then one thread per heap runs the sift steps on slots kept in shared
 //    memory as [slot][heap], a row being a multiple of 32 words, so every
 //    lane reads and writes its own bank whatever slot it is at;
@@ -788,7 +789,7 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
 //    level ahead and writes its path back once (heap_sift);
 //  - the walk rarely needs more than the first few pops of a heap, so the
 //    sift steps run alongside it and stop when it is done.
-// This part ranks the keys (all warps).
+// This part makes the entries (all warps).
 template <int M>
 __device__ void rank_phase(RoundSmem<M>& sm) {
   constexpr int K = M + 1, MM = M * M, SL = (MM + 31) / 32;
@@ -800,21 +801,38 @@ __device__ void rank_phase(RoundSmem<M>& sm) {
   // the scratch heads the kernel's dynamic shared memory (declared here too so
   // that accesses compile as shared-memory ones)
   extern __shared__ uint4 smem_heap[];
-  unsigned* slot = reinterpret_cast<unsigned*>(smem_heap);    // [MM][HS]
-  uint8_t* rk8 = reinterpret_cast<uint8_t*>(slot + MM * HS);  // [MM][HS]
-  for (int pq = tid >> 5; pq < np; pq += NW) {  // ranks, one warp per heap
+  unsigned* slot = reinterpret_cast<unsigned*>(smem_heap);  // [MM][HS]
+  unsigned* ent = slot + MM * HS;                           // [MM][HS]
+  for (int pq = tid >> 5; pq < np; pq += NW) {  // entries, one warp per heap
     const int a = pq / Kn, b = pq % Kn;
     if (a == b && sm.mode != 2) continue;
+    const int c = a * K + b;  // column of the ordered pair in ord, slots and entries
     long long key[SL];
+    bool small = true;  // every gain of the heap within +-2047
+    int lr[SL], rr[SL];
 #pragma unroll
     for (int q = 0; q < SL; ++q) {
       const int idx = lane + 32 * q;
       key[q] = 0;
+      lr[q] = 0;
+      rr[q] = 0;
       if (idx < MM) {
         int l, r;
         pair_gains<M>(sm, a, b, idx, l, r);
         key[q] = swap_key(l, r);
+        lr[q] = l + r;
+        rr[q] = r;
+        small = small && lr[q] >= -2047 && lr[q] <= 2047 && r >= -2047 && r <= 2047;
       }
+    }
+    if (__all_sync(FULL, small)) {
+      // the key itself, (l + r, r) in 12 + 12 bits, orders like swap_key
+#pragma unroll
+      for (int q = 0; q < SL; ++q)
+        if (lane + 32 * q < MM)
+          ent[(lane + 32 * q) * HS + c] =
+              ((((unsigned)(lr[q] + 2048) << 12) | (unsigned)(rr[q] + 2048)) << 8) | (unsigned)(lane + 32 * q);
+      continue;
     }
     unsigned rk[SL];
 #pragma unroll
@@ -829,10 +847,9 @@ __device__ void rank_phase(RoundSmem<M>& sm) {
 #pragma unroll
       for (int q = 0; q < SL; ++q) rk[q] += kj < key[q] ? 1u : 0u;
     }
-    const int c = a * K + b;  // column of the ordered pair in ord, slots and ranks
 #pragma unroll
     for (int q = 0; q < SL; ++q)
-      if (lane + 32 * q < MM) rk8[(lane + 32 * q) * HS + c] = (uint8_t)rk[q];
+      if (lane + 32 * q < MM) ent[(lane + 32 * q) * HS + c] = (rk[q] << 8) | (unsigned)(lane + 32 * q);
   }
   if (tid < K * K) sm.hprog[tid] = 0;
   if (tid == 0) sm.hstop = 0;
@@ -851,8 +868,8 @@ __device__ void heap_sift(RoundSmem<M>& sm) {
   const int Kn = sm.K_, np = Kn * Kn;
   const int tid = threadIdx.x;
   extern __shared__ uint4 smem_heap[];
-  unsigned* slot = reinterpret_cast<unsigned*>(smem_heap);    // [MM][HS]
-  uint8_t* rk8 = reinterpret_cast<uint8_t*>(slot + MM * HS);  // [MM][HS]
+  unsigned* slot = reinterpret_cast<unsigned*>(smem_heap);  // [MM][HS]
+  const unsigned* ent = slot + MM * HS;                     // [MM][HS]
   volatile int* prog = sm.hprog;
   volatile int* stop = &sm.hstop;
   const int a = tid / Kn, b = tid % Kn, pq = a * K + b;
@@ -864,7 +881,7 @@ __device__ void heap_sift(RoundSmem<M>& sm) {
     // ancestors of `len` are loaded together; keys do not decrease going up
     // a path, so the entry rises past exactly the ancestors with key <= its own.
     for (int len = 0; len < MM; ++len) {
-      const unsigned kv = ((unsigned)rk8[len * HS + pq] << 8) | (unsigned)len;
+      const unsigned kv = ent[len * HS + pq];
       int pn[D + 1];
       unsigned av[D];
       pn[0] = len;
