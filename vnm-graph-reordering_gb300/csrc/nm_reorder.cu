@@ -621,10 +621,11 @@ __device__ __forceinline__ void for_touched_warp(const RoundSmem<M>& sm, const N
   constexpr int TOUCH_U = 4;
   constexpr int NW = NM_THREADS / 32;
   const int nt = sm.ntouched;
-  // 32-row chunks dealt round-robin over every warp of the job's blocks, so
-  // a round with few touched rows still spreads over all of them
+  // 32-row chunks dealt round-robin over the job's blocks first, then over
+  // their warps, so a round with few touched rows still spreads over every
+  // SM of the cluster (the phases are issue-bound per SM)
   const int NWt = sl.cs * NW;
-  const int lane = threadIdx.x & 31, w = sl.rank * NW + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31, w = (threadIdx.x >> 5) * sl.cs + sl.rank;
   for (int c0 = w; c0 * 32 < nt; c0 += NWt * TOUCH_U) {
     int rv[TOUCH_U];
     uint4 wv[TOUCH_U];
