@@ -983,8 +983,11 @@ __device__ void walk_phase(RoundSmem<M>& sm, int sched) {
   constexpr int K = M + 1, MM = M * M;
   constexpr int HS = RoundSmem<M>::HSTR;
   constexpr unsigned FULLM = (1u << M) - 1u;
+  constexpr int U = (MM + 31) / 32;  // swaps per lane
   const int lane = threadIdx.x & 31;
   volatile int* prog = sm.hprog;
+  extern __shared__ uint4 smem_heap[];
+  const unsigned* ent = reinterpret_cast<const unsigned*>(smem_heap) + MM * HS;  // [MM][HS], as rank_phase wrote
   bool dead = false;  // a wait ran out: the job is failed, finish without reading ord
   // pops of pair column `col` published so far, once at least `need`; -1 at the limit
   auto wait_pops = [&](int col, int need) -> int {
@@ -1051,11 +1054,35 @@ __device__ void walk_phase(RoundSmem<M>& sm, int sched) {
         const int txi = __ffs(__ballot_sync(FULL, isT && pos == x)) - 1;
         const unsigned vt = __shfl_sync(FULL, vis, txi);
         int tc = __shfl_sync(FULL, cnt, txi);
-        // first pop of the pair whose two nodes are both unvisited, over the
-        // pops published so far, waiting for more while none qualifies
+        // First pop of the pair whose two nodes are both unvisited.  A heap
+        // pops in non-increasing key order, so that is the qualifying swap of
+        // largest key when only one has it (read off the entries); on a tie
+        // it is the first of them in the pops published so far, waiting for
+        // more while none qualifies.
         const int col = pxi * K + txi;
         const uint8_t* ord = ord0 + col;
         int pick = -1, seen = 0;
+        {
+          unsigned kq[U];  // key + 1 of this lane's qualifying swaps, else 0
+          unsigned best = 0;
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            const int k = lane + 32 * u;
+            const unsigned e = k < MM ? ent[k * HS + col] : 0u;
+            const int idx = (int)(e & 255u);
+            const bool ok = k < MM && !((vp >> (idx / M)) & 1u) && !((vt >> (idx % M)) & 1u);
+            kq[u] = ok ? (e >> 8) + 1u : 0u;
+            best = max(best, __reduce_max_sync(FULL, kq[u]));
+          }
+          int nbest = 0, who = -1;
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            const unsigned bb = __ballot_sync(FULL, best != 0u && kq[u] == best);
+            nbest += __popc(bb);
+            if (bb && who < 0) who = 32 * u + __ffs(bb) - 1;
+          }
+          if (nbest == 1) pick = who;  // swap index == entry position
+        }
         while (pick < 0 && !dead) {
           if (seen >= MM) {  // unreachable: a scored target always has an unvisited node
             if (lane == 0) sm.status |= JOB_EMPTY_HEAP;
