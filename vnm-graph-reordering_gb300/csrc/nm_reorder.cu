@@ -517,24 +517,44 @@ __device__ void clear_round_smem(RoundSmem<M>& sm) {
 // OR the bitmaps of the round's segments into per-row records.
 template <int M>
 __device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J, Slice sl = Slice{0, 1}, int* ntp = nullptr) {
+  constexpr int K = M + 1;
   const int tid = threadIdx.x;
   if (!ntp) ntp = &sm.ntouched;
   const int KM = sm.K_ * M;
-  if (tid < KM) {
-    const int xi = tid / M, k = tid % M;
-    const int u = J.orig[sm.xseg[xi] * M + k];
-    const int b = J.cptr[u];
-    sm.colstart[tid] = b;
-    sm.colpre[tid + 1] = J.cptr[u + 1] - b;
+  if (tid < 32) {  // columns of the round and their prefix sums, on one warp
+    constexpr int CPL = (K * M + 31) / 32;  // columns per lane
+    int len[CPL], tot = 0;
+#pragma unroll
+    for (int q = 0; q < CPL; ++q) {
+      const int col = tid * CPL + q;
+      len[q] = 0;
+      if (col < KM) {
+        const int u = J.orig[sm.xseg[col / M] * M + col % M];
+        const int b = J.cptr[u];
+        sm.colstart[col] = b;
+        len[q] = J.cptr[u + 1] - b;
+      }
+      tot += len[q];
+    }
+    int incl = tot;  // inclusive scan of the lanes' totals
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(FULL, incl, o);
+      if (tid >= o) incl += t;
+    }
+    int run = incl - tot;
+#pragma unroll
+    for (int q = 0; q < CPL; ++q) {
+      const int col = tid * CPL + q;
+      if (col < KM) sm.colpre[col] = run;
+      run += len[q];
+    }
+    if (tid == 31) {
+      sm.colpre[KM] = incl;
+      sm.E = incl;
+      sm.use_table = sm.ts_max > 0 && incl <= (sm.ts_max >> 2) * 3;
+    }
   }
-  __syncthreads();
-  if (tid == 0) {
-    sm.colpre[0] = 0;
-    for (int q = 0; q < KM; ++q) sm.colpre[q + 1] += sm.colpre[q];
-    sm.E = sm.colpre[KM];
-  }
-  __syncthreads();
-  if (tid == 0) sm.use_table = sm.ts_max > 0 && sm.E <= (sm.ts_max >> 2) * 3;
   __syncthreads();
   const int E = sm.E;
   if (sm.use_table) {
