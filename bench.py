@@ -369,13 +369,14 @@ def run_ours(args, rank, world, local):
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                      # dram__bytes_read.sum + dram__bytes_write.sum of one launch, from the ncu
                      # capture summarised in profiles/k_nm_rounds_c2_rmat16384_m4.md
-                     "traffic": 2.06e6, "traffic_unit": "bytes per launch",
+                     "traffic": 2.08e6, "traffic_unit": "bytes per launch",
                      "alg_bytes_per_launch": alg_bytes / args.steps,
                      "kernel_ms_per_launch": tot["rounds_kernel_ms"] / args.steps,
                      "note": "latency-bound sequential greedy (4 jobs x cluster of 8 blocks); see profiles/",
                      "round_phase_share": {k: round(vv / max(1, sum(phase_sum.values())), 4)
                                            for k, vv in phase_sum.items()}},
-        "spmm": {"kernel": "k_spmm_vnm<128>", "useful_tflops": useful / sk / 1e12,
+        "spmm": {"kernel": "k_spmm_vnm<64|128|256> (column-block width picked by timing on the first call)",
+                 "useful_tflops": useful / sk / 1e12,
                  "issued_tflops": issued / sk / 1e12, "bound": "tensor", "peak_tflops": tflops_peak,
                  "peak_kind": tkind, "issued_frac": issued / sk / 1e12 / tflops_peak,
                  "max_rel_err_vs_fp64": spmm_err, "slices": info["slices"], "ksteps": info["ksteps"],
