@@ -73,8 +73,9 @@ float vnm_last_main_kernel_ms(const vnm_ctx* ctx);
  * out[2] row records touched, out[3] segments per job, out[4] jobs,
  * out[5] nonzero-valued entries of the pattern, out[6] thread blocks per
  * job (the cluster size the launch used), out[8..14] kilocycles
- * spent per round phase (select, choose, gather, process, heap, walk,
- * apply) summed over jobs.  n <= 16 values. */
+ * spent per round phase (select, choose, gather, process, heap entries,
+ * swap heaps and walk overlapped, apply) summed over jobs.  n <= 16
+ * values. */
 vnm_status vnm_last_stats(const vnm_ctx* ctx, long long* out, int n);
 
 /* ---------------------------------------------------------------------------

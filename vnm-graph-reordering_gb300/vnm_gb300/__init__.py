@@ -155,7 +155,7 @@ class Context:
         _check(lib().vnm_last_stats(self.h, out, 16), "vnm_last_stats")
         keys = ("rounds", "gathered", "touched", "nseg", "jobs", "pattern_nnz", "blocks_per_job")
         d = dict(zip(keys, list(out)[:7]))
-        d["phase_kcycles"] = dict(zip(("select", "choose", "gather", "process", "heap", "walk", "apply"),
+        d["phase_kcycles"] = dict(zip(("select", "choose", "gather", "process", "heap_entries", "heaps_and_walk", "apply"),
                                       list(out)[8:15]))
         return d
 
