@@ -372,7 +372,8 @@ def run_ours(args, rank, world, local):
                      "traffic": 2.08e6, "traffic_unit": "bytes per launch",
                      "alg_bytes_per_launch": alg_bytes / args.steps,
                      "kernel_ms_per_launch": tot["rounds_kernel_ms"] / args.steps,
-                     "note": "latency-bound sequential greedy (4 jobs x cluster of 8 blocks); see profiles/",
+                     "note": "latency-bound sequential greedy (4 jobs x cluster of %d blocks); see profiles/"
+                             % int(t["stats"]["blocks_per_job"]),
                      "round_phase_share": {k: round(vv / max(1, sum(phase_sum.values())), 4)
                                            for k, vv in phase_sum.items()}},
         "spmm": {"kernel": "k_spmm_vnm<64|128|256> (column-block width picked by timing on the first call)",

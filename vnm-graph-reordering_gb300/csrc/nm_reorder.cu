@@ -1225,20 +1225,14 @@ __device__ void apply_finish(RoundSmem<M>& sm, const NMJob& J, int* cnt) {
   __syncthreads();
 }
 
-// Leader block: add the other blocks' partial sums of n ints at `mine`.
-template <int M>
-__device__ void cluster_reduce(cg::cluster_group& cl, int cs, int* mine, int n) {
+// Helper block: add its nonzero partial sums of n ints at `mine` into the
+// leader's copy (remote atomics, complete at the next cluster barrier).
+__device__ void cluster_push(cg::cluster_group& cl, int* mine, int n) {
+  int* lead_arr = cl.map_shared_rank(mine, 0);
   for (int i = threadIdx.x; i < n; i += NM_THREADS) {
-    int v = 0, r = 1;
-    for (; r + 3 < cs; r += 4) {  // four remote loads in flight at a time
-      const int a0 = cl.map_shared_rank(mine, r)[i], a1 = cl.map_shared_rank(mine, r + 1)[i];
-      const int a2 = cl.map_shared_rank(mine, r + 2)[i], a3 = cl.map_shared_rank(mine, r + 3)[i];
-      v += (a0 + a1) + (a2 + a3);
-    }
-    for (; r < cs; ++r) v += cl.map_shared_rank(mine, r)[i];
-    mine[i] += v;
+    const int v = mine[i];
+    if (v) atomicAdd(lead_arr + i, v);
   }
-  __syncthreads();
 }
 
 // All rounds of a job.  With cs == 1 one thread block runs the job; with
@@ -1329,7 +1323,7 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     }
     if (cs > 1) cl.sync();
     if (!sm.go) break;  // the same decision in every block of the job
-    if (!lead) {        // the leader read last round's partial sums before the barrier
+    if (!lead) {        // the block pushed last round's partial sums before the last barrier
       clear_round_smem<M>(sm);
       __syncthreads();
     }
@@ -1342,10 +1336,9 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     VNM_PHASE(2);
     process_phase<M>(sm, J, N, sl);
     if (cs > 1) {
+      if (!lead) cluster_push(cl, &sm.S[0][0], NSUM);
       cl.sync();
-      if (lead) {
-        cluster_reduce<M>(cl, cs, &sm.S[0][0], NSUM);
-      } else {  // while the leader runs the heaps and the walk: next round's scan
+      if (!lead) {  // while the leader runs the heaps and the walk: next round's scan
         const int nh = cs - 1, hr = rank - 1;
         const int sb = (int)((long long)J.nseg * hr / nh), se = (int)((long long)J.nseg * (hr + 1) / nh);
         select_range<M>(sm, cnt_in_smem ? cl.map_shared_rank(smem_cnt, 0) : J.cnt, sb, se, sm.xseg, sm.K_);
@@ -1379,8 +1372,8 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     if (cs > 1) cl.sync();
     apply_recount<M>(sm, J, N, sl);
     if (cs > 1) {
+      if (!lead) cluster_push(cl, &sm.newinv[0], 2 * K);
       cl.sync();
-      if (lead) cluster_reduce<M>(cl, cs, &sm.newinv[0], 2 * K);
     }
     if (lead) {
       apply_finish<M>(sm, J, cnt);
@@ -1643,17 +1636,17 @@ static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, 
 
 // Blocks per job for calls with few jobs (one matrix, or its four
 // schedules); batches run one block per job.  Measured on GB300 (find_best,
-// four jobs): R-MAT 16384 2:4 (228 K entries) 59 / 40 / 32 / 27 / 27 ms and
-// R-MAT 65536 2:8 (1.8 M entries) 4111 / 2204 / 1323 / 880 / 709 ms with 1 /
-// 2 / 4 / 8 / 16 blocks, so 16 (a non-portable cluster size) from 1 M
-// pattern entries on, 8 below.  VNM_NM_CLUSTER (1..16) in the environment
-// overrides the choice.
+// four jobs) with 4 / 8 / 16 blocks: R-MAT 2048 2:8 (26 K entries) 6.7 /
+// 6.8 / 7.3 ms, R-MAT 16384 2:4 (228 K entries) 17.1 / 12.9 / 12.4 ms,
+// R-MAT 65536 2:8 (1.8 M entries) 472 / 295 / 209 ms; so 16 (a non-portable
+// cluster size) from 128 K pattern entries on, 8 below.  VNM_NM_CLUSTER
+// (1..16) in the environment overrides the choice.
 static int nm_cluster_size(long long np) {
   if (const char* e = getenv("VNM_NM_CLUSTER")) {
     const int v = atoi(e);
     if (v >= 1 && v <= 16) return v;
   }
-  return np >= (1ll << 20) ? 16 : 8;
+  return np >= (1ll << 17) ? 16 : 8;
 }
 
 static vnm_status launch_rounds(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, int N, int M, int max_nseg,
