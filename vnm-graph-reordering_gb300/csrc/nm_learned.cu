@@ -102,9 +102,8 @@ __global__ void k_l_colh(LMat L, const int* positions, const int* npos_p, int np
     }
 #pragma unroll
     for (int z = 0; z < 9; ++z) {
-      int v = h[z];
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) L.colh[u * 9 + z] = v;
+      const int v = __reduce_add_sync(0xffffffffu, h[z]);
+      if (lane == z) L.colh[u * 9 + z] = v;
     }
   }
 }
@@ -489,7 +488,9 @@ __global__ void k_l_accept(LMat L, const int* active, const int* nactive_p, int 
 }
 
 // Apply accepted swaps: flip the two bits of every row that holds exactly one
-// of the two columns, keep hist / cnt in step, and exchange the nodes.
+// of the two columns, keep hist / cnt in step, and exchange the nodes.  A
+// swap's hist / cnt changes are summed over its rows in registers and added
+// once per warp (per-row atomics on those few counters serialised).
 __global__ void k_l_apply(LMat L, const int4* acc, const int* nacc) {
   const int n = *nacc;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
@@ -500,6 +501,8 @@ __global__ void k_l_apply(LMat L, const int4* acc, const int* nacc) {
     const int p = sw.x, i = sw.y, t = sw.z, j = sw.w;
     const int u = L.orig[p * L.M + i], w = L.orig[t * L.M + j];
     const unsigned bi = 1u << i, bj = 1u << j;
+    int dp[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, dt[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    int dcp = 0, dct = 0;
     for (int side = 0; side < 2; ++side) {
       const int col = side == 0 ? u : w;
       for (int e = L.cptr[col] + lane; e < L.cptr[col + 1]; e += 32) {
@@ -513,15 +516,25 @@ __global__ void k_l_apply(LMat L, const int4* acc, const int* nacc) {
         atomicXor(&Gw[cp >> 2], (gp ^ np_) << ((cp & 3) * 8));
         atomicXor(&Gw[ct >> 2], (gt ^ nt_) << ((ct & 3) * 8));
         const int a0 = __popc(gp), a1 = __popc(np_), c0 = __popc(gt), c1 = __popc(nt_);
-        atomicAdd(&L.hist[p * 9 + a0], -1);
-        atomicAdd(&L.hist[p * 9 + a1], 1);
-        atomicAdd(&L.hist[t * 9 + c0], -1);
-        atomicAdd(&L.hist[t * 9 + c1], 1);
-        atomicAdd(&L.cnt[p], (a1 > L.N) - (a0 > L.N));
-        atomicAdd(&L.cnt[t], (c1 > L.N) - (c0 > L.N));
+#pragma unroll
+        for (int z = 0; z < 9; ++z) {
+          dp[z] += (z == a1) - (z == a0);
+          dt[z] += (z == c1) - (z == c0);
+        }
+        dcp += (a1 > L.N) - (a0 > L.N);
+        dct += (c1 > L.N) - (c0 > L.N);
       }
       __syncwarp();
     }
+#pragma unroll
+    for (int z = 0; z < 9; ++z) {
+      const int vp = __reduce_add_sync(0xffffffffu, dp[z]), vt = __reduce_add_sync(0xffffffffu, dt[z]);
+      if (lane == z && vp) atomicAdd(&L.hist[p * 9 + z], vp);
+      if (lane == z && vt) atomicAdd(&L.hist[t * 9 + z], vt);
+    }
+    const int vcp = __reduce_add_sync(0xffffffffu, dcp), vct = __reduce_add_sync(0xffffffffu, dct);
+    if (lane == 0 && vcp) atomicAdd(&L.cnt[p], vcp);
+    if (lane == 0 && vct) atomicAdd(&L.cnt[t], vct);
     if (lane == 0) {
       L.orig[p * L.M + i] = w;
       L.orig[t * L.M + j] = u;
