@@ -85,16 +85,52 @@ __global__ void k_l_hist_zero(int* hist, int nseg, int R) {
   }
 }
 
-// colh of the columns at the given positions (one warp per column)
-__global__ void k_l_colh(LMat L, const int* positions, const int* npos_p, int npos_fixed) {
+// colh of the columns at the given positions.  A column's rows are cut into
+// chunks of L_CHUNK, one warp per chunk, so a hub column spreads over many
+// warps: k_l_colh_prep zeroes each column's histogram and counts its
+// chunks, an exclusive scan turns the counts into offsets, and
+// k_l_colh_rows adds each chunk's histogram.
+constexpr int L_CHUNK = 256;
+
+__global__ void k_l_colh_prep(LMat L, const int* positions, const int* npos_p, int npos_fixed, int cap,
+                              int* nchunk) {
+  const int npos = npos_p ? *npos_p : npos_fixed;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cap; q += gridDim.x * blockDim.x) {
+    int c = 0;
+    if (q < npos) {
+      const int u = L.orig[positions ? positions[q] : q];
+#pragma unroll
+      for (int z = 0; z < 9; ++z) L.colh[u * 9 + z] = 0;
+      c = (L.cptr[u + 1] - L.cptr[u] + L_CHUNK - 1) / L_CHUNK;
+    }
+    nchunk[q] = c;
+  }
+}
+
+// the entry of a sorted offset table that holds `item`: last q with offs[q] <= item
+__device__ __forceinline__ int chunk_owner(const int* offs, int n, int item) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (offs[mid] <= item) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void k_l_colh_rows(LMat L, const int* positions, const int* npos_p, int npos_fixed, const int* offs,
+                              const int* ntot) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int nw = (gridDim.x * blockDim.x) >> 5;
-  const int npos = npos_p ? *npos_p : npos_fixed;
-  for (int q = warp; q < npos; q += nw) {
+  const int npos = npos_p ? *npos_p : npos_fixed, tot = *ntot;
+  for (int item = warp; item < tot; item += nw) {
+    const int q = chunk_owner(offs, npos, item);
     const int a = positions ? positions[q] : q;
     const int u = L.orig[a], s = a / L.M;
+    const int beg = L.cptr[u] + (item - offs[q]) * L_CHUNK;
+    const int end = min(beg + L_CHUNK, L.cptr[u + 1]);
     int h[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int e = L.cptr[u] + lane; e < L.cptr[u + 1]; e += 32) {
+    for (int e = beg + lane; e < end; e += 32) {
       const int r = L.crow[e];
       const int k = __popc(L.G[(long long)r * L.nseg + s]);
 #pragma unroll
@@ -103,7 +139,7 @@ __global__ void k_l_colh(LMat L, const int* positions, const int* npos_p, int np
 #pragma unroll
     for (int z = 0; z < 9; ++z) {
       const int v = __reduce_add_sync(0xffffffffu, h[z]);
-      if (lane == z) L.colh[u * 9 + z] = v;
+      if (lane == z && v) atomicAdd(&L.colh[u * 9 + z], v);
     }
   }
 }
@@ -488,43 +524,69 @@ __global__ void k_l_accept(LMat L, const int* active, const int* nactive_p, int 
 }
 
 // Apply accepted swaps: flip the two bits of every row that holds exactly one
-// of the two columns, keep hist / cnt in step, and exchange the nodes.  A
-// swap's hist / cnt changes are summed over its rows in registers and added
-// once per warp (per-row atomics on those few counters serialised).
-__global__ void k_l_apply(LMat L, const int4* acc, const int* nacc) {
+// of the two columns, keep hist / cnt in step, and exchange the nodes.
+// Accepted swaps touch disjoint segments, and a row holding both columns
+// moves nothing, so the rows of the two columns are independent: they are
+// cut into chunks of L_CHUNK, one warp per chunk.  k_l_apply_prep records
+// each swap's two nodes, counts their chunks and exchanges the nodes;
+// k_l_apply_rows moves the bits, summing a chunk's hist / cnt changes in
+// registers and adding them once per warp.
+__global__ void k_l_apply_prep(LMat L, const int4* acc, const int* nacc, int cap, int2* uw, int* nchunk) {
   const int n = *nacc;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < cap; s += gridDim.x * blockDim.x) {
+    int c = 0;
+    if (s < n) {
+      const int4 sw = acc[s];
+      const int a = sw.x * L.M + sw.y, b = sw.z * L.M + sw.w;
+      const int u = L.orig[a], w = L.orig[b];
+      uw[s] = make_int2(u, w);
+      c = (L.cptr[u + 1] - L.cptr[u] + L_CHUNK - 1) / L_CHUNK + (L.cptr[w + 1] - L.cptr[w] + L_CHUNK - 1) / L_CHUNK;
+      L.orig[a] = w;
+      L.orig[b] = u;
+      L.pos[w] = a;
+      L.pos[u] = b;
+    }
+    nchunk[s] = c;
+  }
+}
+
+__global__ void k_l_apply_rows(LMat L, const int4* acc, const int* nacc, const int2* uw, const int* offs,
+                               const int* ntot) {
+  const int n = *nacc, tot = *ntot;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int nw = (gridDim.x * blockDim.x) >> 5;
   unsigned* Gw = reinterpret_cast<unsigned*>(L.G);
-  for (int s = warp; s < n; s += nw) {
+  for (int item = warp; item < tot; item += nw) {
+    const int s = chunk_owner(offs, n, item);
     const int4 sw = acc[s];
     const int p = sw.x, i = sw.y, t = sw.z, j = sw.w;
-    const int u = L.orig[p * L.M + i], w = L.orig[t * L.M + j];
+    const int u = uw[s].x, w = uw[s].y;
     const unsigned bi = 1u << i, bj = 1u << j;
+    const int cu = (L.cptr[u + 1] - L.cptr[u] + L_CHUNK - 1) / L_CHUNK;
+    int k = item - offs[s];
+    const int col = k < cu ? u : w;
+    if (k >= cu) k -= cu;
+    const int beg = L.cptr[col] + k * L_CHUNK, end = min(beg + L_CHUNK, L.cptr[col + 1]);
     int dp[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, dt[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     int dcp = 0, dct = 0;
-    for (int side = 0; side < 2; ++side) {
-      const int col = side == 0 ? u : w;
-      for (int e = L.cptr[col] + lane; e < L.cptr[col + 1]; e += 32) {
-        const int r = L.crow[e];
-        const long long cp = (long long)r * L.nseg + p, ct = (long long)r * L.nseg + t;
-        const unsigned gp = L.G[cp], gt = L.G[ct];
-        const bool inU = gp & bi, inW = gt & bj;
-        if (inU == inW) continue;  // both or neither: nothing moves (and side 1 skips rows side 0 handled)
-        const unsigned np_ = inW ? (gp | bi) : (gp & ~bi);
-        const unsigned nt_ = inU ? (gt | bj) : (gt & ~bj);
-        atomicXor(&Gw[cp >> 2], (gp ^ np_) << ((cp & 3) * 8));
-        atomicXor(&Gw[ct >> 2], (gt ^ nt_) << ((ct & 3) * 8));
-        const int a0 = __popc(gp), a1 = __popc(np_), c0 = __popc(gt), c1 = __popc(nt_);
+    for (int e = beg + lane; e < end; e += 32) {
+      const int r = L.crow[e];
+      const long long cp = (long long)r * L.nseg + p, ct = (long long)r * L.nseg + t;
+      const unsigned gp = L.G[cp], gt = L.G[ct];
+      const bool inU = gp & bi, inW = gt & bj;
+      if (inU == inW) continue;  // both columns or neither: nothing moves
+      const unsigned np_ = inW ? (gp | bi) : (gp & ~bi);
+      const unsigned nt_ = inU ? (gt | bj) : (gt & ~bj);
+      atomicXor(&Gw[cp >> 2], (gp ^ np_) << ((cp & 3) * 8));
+      atomicXor(&Gw[ct >> 2], (gt ^ nt_) << ((ct & 3) * 8));
+      const int a0 = __popc(gp), a1 = __popc(np_), c0 = __popc(gt), c1 = __popc(nt_);
 #pragma unroll
-        for (int z = 0; z < 9; ++z) {
-          dp[z] += (z == a1) - (z == a0);
-          dt[z] += (z == c1) - (z == c0);
-        }
-        dcp += (a1 > L.N) - (a0 > L.N);
-        dct += (c1 > L.N) - (c0 > L.N);
+      for (int z = 0; z < 9; ++z) {
+        dp[z] += (z == a1) - (z == a0);
+        dt[z] += (z == c1) - (z == c0);
       }
-      __syncwarp();
+      dcp += (a1 > L.N) - (a0 > L.N);
+      dct += (c1 > L.N) - (c0 > L.N);
     }
 #pragma unroll
     for (int z = 0; z < 9; ++z) {
@@ -535,12 +597,6 @@ __global__ void k_l_apply(LMat L, const int4* acc, const int* nacc) {
     const int vcp = __reduce_add_sync(0xffffffffu, dcp), vct = __reduce_add_sync(0xffffffffu, dct);
     if (lane == 0 && vcp) atomicAdd(&L.cnt[p], vcp);
     if (lane == 0 && vct) atomicAdd(&L.cnt[t], vct);
-    if (lane == 0) {
-      L.orig[p * L.M + i] = w;
-      L.orig[t * L.M + j] = u;
-      L.pos[w] = p * L.M + i;
-      L.pos[u] = t * L.M + j;
-    }
   }
 }
 
@@ -943,7 +999,10 @@ vnm_status vnm_nm_learned(vnm_ctx* ctx, int nrows, int nnz, const int* row, cons
                 arena_bytes((size_t)nseg * 9, 4) + arena_bytes(nseg, 4) + arena_bytes((size_t)R * 9, 4) +
                 3 * arena_bytes(R, 4) + 3 * arena_bytes(nseg + 1, 4) + arena_bytes((size_t)nseg * LTOP, 4) +
                 2 * arena_bytes(nseg, 8) + arena_bytes(nseg, 16) + arena_bytes(2 * (size_t)R, 4) +
-                arena_bytes(16, 4) + arena_bytes(8, 8) + scan_scratch_bytes(nseg + 1) +
+                arena_bytes(16, 4) + arena_bytes(8, 8) + arena_bytes(R + 1, 4) + arena_bytes(nseg + 1, 8) +
+                // scratch of the scans, given back every round: the active list, the applied
+                // swaps and the column histograms (the first histograms' scan before the loop)
+                scan_scratch_bytes(R + 1) + 2 * scan_scratch_bytes(nseg + 1) +
                 arena_bytes((size_t)dcap * LF, 4) + arena_bytes(dcap, 4) + 8192;
   VNM_TRY(arena_reserve(ctx, need));
   VNM_TRY(pinned_reserve(ctx, 256));
@@ -976,13 +1035,15 @@ vnm_status vnm_nm_learned(vnm_ctx* ctx, int nrows, int nnz, const int* row, cons
   unsigned long long* claim = arena_take<unsigned long long>(ctx, nseg + 1);
   int4* acc = arena_take<int4>(ctx, nseg + 1);
   int* cols = arena_take<int>(ctx, 2 * (size_t)R + 1);
-  int* ci = arena_take<int>(ctx, 16);  // [0] nactive [1] nacc [2] ncols [3] ndump [4] err
+  int* chunks = arena_take<int>(ctx, R + 1);     // per column (or swap) chunk counts, then their offsets
+  int2* uw = arena_take<int2>(ctx, nseg + 1);    // the two nodes of each accepted swap
+  int* ci = arena_take<int>(ctx, 16);  // [0] nactive [1] nacc [2] ncols [3] ndump [4] err [5..6] chunk totals
   unsigned long long* cu = arena_take<unsigned long long>(ctx, 8);  // [0] gain [1] scored [2..3] totals
   float* dx = dcap ? arena_take<float>(ctx, (size_t)dcap * LF) : nullptr;
   float* dy = dcap ? arena_take<float>(ctx, dcap) : nullptr;
   int* d_newpos = arena_take<int>(ctx, R + 1);
   if (!L.G || !L.hist || !L.cnt || !L.colh || !L.orig || !L.pos || !flags || !active || !top || !best || !claim ||
-      !acc || !cols || !ci || !cu || !d_newpos || (dcap && (!dx || !dy)))
+      !acc || !cols || !chunks || !uw || !ci || !cu || !d_newpos || (dcap && (!dx || !dy)))
     return VNM_ERR_NOMEM;
   cudaStream_t st = ctx->stream;
   VNM_CUDA_TRY(cudaMemsetAsync(L.G, 0, gbytes > 0 ? gbytes : 4, st));
@@ -1000,7 +1061,12 @@ vnm_status vnm_nm_learned(vnm_ctx* ctx, int nrows, int nnz, const int* row, cons
     VNM_LAUNCH(ctx, k_l_hist_zero, lgrid(ctx, nseg), 256, 0, L.hist, nseg, R);
     VNM_LAUNCH(ctx, k_l_totals, lgrid(ctx, nseg), 256, 0, L.hist, nseg, N, cu + 2);
   }
-  if (R > 0) VNM_LAUNCH(ctx, k_l_colh, lgrid(ctx, (long long)R * 32), 256, 0, L, nullptr, nullptr, R);
+  const size_t round_mark = ctx->arena.used;  // scan scratch from here on is given back every round
+  if (R > 0) {  // every column's histogram
+    VNM_LAUNCH(ctx, k_l_colh_prep, lgrid(ctx, R), 256, 0, L, nullptr, nullptr, R, R, chunks);
+    VNM_TRY(exclusive_scan(ctx, chunks, chunks, R, ci + 5));
+    VNM_LAUNCH(ctx, k_l_colh_rows, lgrid(ctx, (long long)R * 32), 256, 0, L, nullptr, nullptr, R, chunks, ci + 5);
+  }
   unsigned long long* hcu = reinterpret_cast<unsigned long long*>(ctx->h_pinned);  // 8 words
   int* hci = ctx->h_pinned + 32;                                                    // 16 ints
   VNM_CUDA_TRY(cudaMemcpyAsync(hcu, cu, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, st));
@@ -1015,6 +1081,7 @@ vnm_status vnm_nm_learned(vnm_ctx* ctx, int nrows, int nnz, const int* row, cons
   int idle = 0, rounds = 0, swaps = 0;
   VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main0, st));
   for (int round = 0; round < prm->max_rounds && nseg >= 2 && P.np > 0; ++round) {
+    ctx->arena.used = round_mark;
     VNM_CUDA_TRY(cudaMemsetAsync(ci + 1, 0, sizeof(int) * 2, st));
     VNM_CUDA_TRY(cudaMemsetAsync(best, 0, sizeof(unsigned long long) * nseg, st));
     VNM_CUDA_TRY(cudaMemsetAsync(claim, 0, sizeof(unsigned long long) * nseg, st));
@@ -1029,9 +1096,13 @@ vnm_status vnm_nm_learned(vnm_ctx* ctx, int nrows, int nnz, const int* row, cons
     VNM_LAUNCH(ctx, k_l_claim, lgrid(ctx, nseg), 256, 0, L, active, ci, round, prm->seed, best, claim);
     VNM_LAUNCH(ctx, k_l_accept, lgrid(ctx, nseg), 256, 0, L, active, ci, round, prm->seed, best, claim, acc, ci + 1,
                cu);
-    VNM_LAUNCH(ctx, k_l_apply, egrid, 256, 0, L, acc, ci + 1);
+    VNM_LAUNCH(ctx, k_l_apply_prep, lgrid(ctx, nseg), 256, 0, L, acc, ci + 1, nseg, uw, chunks);
+    VNM_TRY(exclusive_scan(ctx, chunks, chunks, nseg, ci + 6));
+    VNM_LAUNCH(ctx, k_l_apply_rows, egrid, 256, 0, L, acc, ci + 1, uw, chunks, ci + 6);
     VNM_LAUNCH(ctx, k_l_touched_cols, lgrid(ctx, 2 * (long long)R), 256, 0, acc, ci + 1, M, cols, ci + 2);
-    VNM_LAUNCH(ctx, k_l_colh, egrid, 256, 0, L, cols, ci + 2, 0);
+    VNM_LAUNCH(ctx, k_l_colh_prep, lgrid(ctx, R), 256, 0, L, cols, ci + 2, 0, R, chunks);
+    VNM_TRY(exclusive_scan(ctx, chunks, chunks, R, ci + 5));
+    VNM_LAUNCH(ctx, k_l_colh_rows, egrid, 256, 0, L, cols, ci + 2, 0, chunks, ci + 5);
     VNM_CUDA_TRY(cudaMemcpyAsync(hci, ci, sizeof(int) * 8, cudaMemcpyDeviceToHost, st));
     VNM_CUDA_TRY(cudaMemcpyAsync(hcu, cu, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     VNM_CUDA_TRY(cudaStreamSynchronize(st));
