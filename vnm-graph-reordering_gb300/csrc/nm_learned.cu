@@ -204,24 +204,36 @@ __device__ __forceinline__ int move_gain(int obj, int N, int from, int to) {  //
 }
 
 __device__ int exact_gain_warp(const LMat& L, int p, int i, int t, int j) {
+  constexpr int U = 4;  // rows per lane in flight: a hub column is a long chain of dependent loads
   const int lane = threadIdx.x & 31;
   const int u = L.orig[p * L.M + i], w = L.orig[t * L.M + j];
   const unsigned bi = 1u << i, bj = 1u << j;
   int g = 0;
-  for (int e = L.cptr[u] + lane; e < L.cptr[u + 1]; e += 32) {
-    const int r = L.crow[e];
-    const unsigned gp = L.G[(long long)r * L.nseg + p], gt = L.G[(long long)r * L.nseg + t];
-    if (gt & bj) continue;  // w is in this row too: nothing moves
-    g += move_gain(L.obj, L.N, __popc(gp), __popc(gt));
+  for (int side = 0; side < 2; ++side) {
+    const int col = side == 0 ? u : w;
+    const int end = L.cptr[col + 1];
+    for (int e0 = L.cptr[col] + lane; e0 < end; e0 += 32 * U) {
+      int r[U];
+#pragma unroll
+      for (int k = 0; k < U; ++k) r[k] = e0 + 32 * k < end ? L.crow[e0 + 32 * k] : -1;
+      unsigned gp[U], gt[U];
+#pragma unroll
+      for (int k = 0; k < U; ++k) {
+        gp[k] = r[k] >= 0 ? L.G[(long long)r[k] * L.nseg + p] : 0u;
+        gt[k] = r[k] >= 0 ? L.G[(long long)r[k] * L.nseg + t] : 0u;
+      }
+#pragma unroll
+      for (int k = 0; k < U; ++k) {
+        if (r[k] < 0) continue;
+        if (side == 0) {
+          if (!(gt[k] & bj)) g += move_gain(L.obj, L.N, __popc(gp[k]), __popc(gt[k]));  // else w is here too
+        } else {
+          if (!(gp[k] & bi)) g += move_gain(L.obj, L.N, __popc(gt[k]), __popc(gp[k]));
+        }
+      }
+    }
   }
-  for (int e = L.cptr[w] + lane; e < L.cptr[w + 1]; e += 32) {
-    const int r = L.crow[e];
-    const unsigned gp = L.G[(long long)r * L.nseg + p], gt = L.G[(long long)r * L.nseg + t];
-    if (gp & bi) continue;
-    g += move_gain(L.obj, L.N, __popc(gt), __popc(gp));
-  }
-  for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
-  return g;
+  return __reduce_add_sync(0xffffffffu, g);
 }
 
 // ---------------------------------------------------------------------------
