@@ -369,7 +369,7 @@ def run_ours(args, rank, world, local):
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                      # dram__bytes_read.sum + dram__bytes_write.sum of one launch, from the ncu
                      # capture summarised in profiles/k_nm_rounds_c2_rmat16384_m4.md
-                     "traffic": 2.08e6, "traffic_unit": "bytes per launch",
+                     "traffic": 2.04e6, "traffic_unit": "bytes per launch",
                      "alg_bytes_per_launch": alg_bytes / args.steps,
                      "kernel_ms_per_launch": tot["rounds_kernel_ms"] / args.steps,
                      "note": "latency-bound sequential greedy (4 jobs x cluster of %d blocks); see profiles/"
