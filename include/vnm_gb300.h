@@ -285,7 +285,8 @@ typedef struct vnm_spmm_matrix vnm_spmm_matrix;
  * values are divided by their V-block row's largest magnitude and stored
  * as `dtype` (1 = BF16, 0 = FP16).  Requires 128 % V == 0, 2 <= M <= 8.
  * COO in any order.  The result lives in device memory of the context's
- * GPU until vnm_spmm_free. */
+ * GPU until vnm_spmm_free; its storage is taken from the last operand this
+ * context's operands freed when that is large enough, else allocated. */
 vnm_status vnm_spmm_compress(vnm_ctx* ctx, int nrows, int nnz, const int* row, const int* col, const float* val,
                              int mem, int M, int V, int dtype, vnm_spmm_matrix** out);
 
@@ -302,6 +303,10 @@ vnm_status vnm_spmm_info(const vnm_spmm_matrix* A, long long* info, int n);
  * the environment fixes the width where it divides n. */
 vnm_status vnm_spmm_run(vnm_ctx* ctx, const vnm_spmm_matrix* A, const void* B, int n, float* C, int mem);
 
+/* Release an operand.  While its context lives, the context keeps the
+ * largest freed operand's device storage for its next vnm_spmm_compress
+ * (no cudaMalloc there, no device-wide synchronisation here) and releases
+ * it in vnm_destroy; an operand may outlive its context. */
 vnm_status vnm_spmm_free(vnm_spmm_matrix* A);
 
 /* ---------------------------------------------------------------------------

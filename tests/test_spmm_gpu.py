@@ -75,3 +75,27 @@ def test_spmm_every_column_block_width(ctx, width):
             os.environ.pop("VNM_SPMM_WIDTH", None)
         else:
             os.environ["VNM_SPMM_WIDTH"] = old
+
+
+def test_storage_reuse_and_operand_outliving_its_context():
+    """A freed operand's storage serves the context's next compression (a
+    smaller matrix in a larger block, results still the oracle's), and an
+    operand freed after its context is destroyed is released cleanly."""
+    import torch
+    import vnm_gb300
+    from vnm_gb300 import synth
+    c2 = vnm_gb300.Context(0)
+    big = synth.uniform(2048, 0.01, 11)
+    small = synth.uniform(384, 0.03, 12)
+    nr, r, c, v = big
+    vnm_gb300.SpmmMatrix(c2, nr, r, c, v, 8, 32, "bf16").close()
+    err, _ = _run(c2, *small, 8, 32, 128, "bf16")
+    assert err <= TOL, err
+    nr, r, c, v = small
+    A = vnm_gb300.SpmmMatrix(c2, nr, r, c, v, 8, 32, "bf16")
+    B = torch.randn((nr, 64)).to(torch.bfloat16).cuda()
+    C = A.run(B).cpu().numpy().astype(np.float64)
+    c2.close()
+    ref = oracle.spmm_f64(nr, r, c, v.astype(np.float64), B.float().cpu().numpy().astype(np.float64))
+    assert np.abs(C - ref).max() / max(np.abs(ref).max(), 1e-30) <= TOL
+    A.close()

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
 #include <vector>
 
 #include "../../include/vnm_gb300.h"
@@ -43,6 +44,19 @@ struct DeviceArena {
   size_t used = 0;
 };
 
+// Device storage of a freed SpMM operand, kept for the next compression on
+// the same context (a compression then skips cudaMalloc, a free skips the
+// device-wide synchronisation of cudaFree).  Shared by the context and every
+// operand it compressed; whichever of them goes last frees it.
+struct vnm_spmm_spare {
+  std::mutex m;
+  int device = 0;
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  int refs = 1;  // the context and its live operands
+  bool ctx_alive = true;
+};
+
 struct vnm_ctx {
   int device = 0;
   int num_sms = 0;
@@ -59,6 +73,7 @@ struct vnm_ctx {
   int spmm_tune_nt[8] = {};
   int spmm_tune_next = 0;
   DeviceArena arena;
+  vnm_spmm_spare* spare = nullptr;
   // pinned staging for small results
   int* h_pinned = nullptr;
   size_t h_pinned_cap = 0;

@@ -190,6 +190,8 @@ vnm_status vnm_create(vnm_ctx** out, int device) {
     return VNM_ERR_CUDA;
   }
   c->num_sms = prop.multiProcessorCount;
+  c->spare = new vnm_spmm_spare();
+  c->spare->device = device;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&c->ev_start) != cudaSuccess || cudaEventCreate(&c->ev_stop) != cudaSuccess ||
       cudaEventCreate(&c->ev_main0) != cudaSuccess || cudaEventCreate(&c->ev_main1) != cudaSuccess) {
@@ -211,6 +213,18 @@ vnm_status vnm_destroy(vnm_ctx* c) {
   if (c->ev_main0) cudaEventDestroy(c->ev_main0);
   if (c->ev_main1) cudaEventDestroy(c->ev_main1);
   if (c->stream) cudaStreamDestroy(c->stream);
+  if (c->spare) {
+    bool last;
+    {
+      std::lock_guard<std::mutex> g(c->spare->m);
+      if (c->spare->ptr) cudaFree(c->spare->ptr);
+      c->spare->ptr = nullptr;
+      c->spare->bytes = 0;
+      c->spare->ctx_alive = false;
+      last = --c->spare->refs == 0;
+    }
+    if (last) delete c->spare;
+  }
   delete c;
   return VNM_OK;
 }

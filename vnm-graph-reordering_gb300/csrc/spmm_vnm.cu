@@ -49,6 +49,8 @@ struct vnm_spmm_matrix {
   unsigned char* a = nullptr;  // [nsteps * 4096]
   float* rscale = nullptr;   // [ntiles * 128]
   void* base = nullptr;      // one allocation for all of the above
+  size_t bytes = 0;          // its size
+  vnm_spmm_spare* spare = nullptr;  // the compressing context's spare storage
 };
 
 namespace vnm {
@@ -504,9 +506,24 @@ static vnm_status compress_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, con
   const size_t b_step = arena_bytes(ntiles + 1, 4), b_cols = arena_bytes((size_t)out->nsteps * 16 + 1, 4),
                b_a = arena_bytes((size_t)out->nsteps * SP_KSTEP_BYTES + 16, 1),
                b_sc = arena_bytes((size_t)ntiles * SP_TM, 4);
+  const size_t need = b_step + b_cols + b_a + b_sc;
   void* base = nullptr;
-  VNM_CUDA_TRY(cudaMalloc(&base, b_step + b_cols + b_a + b_sc));
+  size_t have = 0;
+  if (ctx->spare) {  // a freed operand's storage, when large enough
+    std::lock_guard<std::mutex> g(ctx->spare->m);
+    if (ctx->spare->ptr && ctx->spare->bytes >= need) {
+      base = ctx->spare->ptr;
+      have = ctx->spare->bytes;
+      ctx->spare->ptr = nullptr;
+      ctx->spare->bytes = 0;
+    }
+  }
+  if (!base) {
+    VNM_CUDA_TRY(cudaMalloc(&base, need));
+    have = need;
+  }
   out->base = base;
+  out->bytes = have;
   char* pb = static_cast<char*>(base);
   out->tile_step = reinterpret_cast<int*>(pb);
   out->cols = reinterpret_cast<int*>(pb + b_step);
@@ -577,6 +594,11 @@ vnm_status vnm_spmm_compress(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
     delete A;
     return st;
   }
+  if (ctx->spare) {
+    std::lock_guard<std::mutex> g(ctx->spare->m);
+    ctx->spare->refs++;
+    A->spare = ctx->spare;
+  }
   *out = A;
   return VNM_OK;
 }
@@ -591,10 +613,22 @@ vnm_status vnm_spmm_info(const vnm_spmm_matrix* A, long long* info, int n) {
 
 vnm_status vnm_spmm_free(vnm_spmm_matrix* A) {
   if (!A) return VNM_ERR_ARG;
-  if (A->base) {
-    cudaSetDevice(A->device);
-    cudaFree(A->base);
+  cudaSetDevice(A->device);
+  bool last = false;
+  if (A->spare) {
+    // keep the storage for the context's next compression (the larger of
+    // this block and the one kept, while the context lives)
+    std::lock_guard<std::mutex> g(A->spare->m);
+    if (A->base && A->spare->ctx_alive && A->bytes > A->spare->bytes) {
+      if (A->spare->ptr) cudaFree(A->spare->ptr);
+      A->spare->ptr = A->base;
+      A->spare->bytes = A->bytes;
+      A->base = nullptr;
+    }
+    last = --A->spare->refs == 0;
   }
+  if (A->base) cudaFree(A->base);
+  if (last) delete A->spare;
   delete A;
   return VNM_OK;
 }
