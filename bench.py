@@ -280,12 +280,18 @@ def run_ours(args, rank, world, local):
         A.close()
         return t
 
+    # pinned host buffers of the pass through the public API, made once as a
+    # caller running many steps would: the relabelled COO and the result
+    hpr = torch.empty(len(r), dtype=torch.int32).pin_memory()
+    hpc = torch.empty(len(c), dtype=torch.int32).pin_memory()
+    hC = torch.empty((nr, N_B), dtype=torch.float32).pin_memory()
+
     def step_host():
         """The same pass through the public API with host buffers."""
         best, res, newpos = ctx.nm_search(nr, hr.numpy(), hc.numpy(), hv.numpy(), N_NM, M_NM, want_newpos=True)
-        pr, pc = ctx.permute_coo(nr, hr.numpy(), hc.numpy(), newpos)
+        pr, pc = ctx.permute_coo(nr, hr.numpy(), hc.numpy(), newpos, out=(hpr.numpy(), hpc.numpy()))
         A = vnm_gb300.SpmmMatrix(ctx, nr, pr, pc, hv.numpy(), M_NM, V, "bf16")
-        C = A.run(hB.numpy())
+        C = A.run(hB.numpy(), C=hC.numpy())
         A.close()
         return C
 

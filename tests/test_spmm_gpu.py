@@ -99,3 +99,26 @@ def test_storage_reuse_and_operand_outliving_its_context():
     ref = oracle.spmm_f64(nr, r, c, v.astype(np.float64), B.float().cpu().numpy().astype(np.float64))
     assert np.abs(C - ref).max() / max(np.abs(ref).max(), 1e-30) <= TOL
     A.close()
+
+
+def test_host_outputs_given_by_the_caller(ctx):
+    """permute_coo and SpmmMatrix.run fill caller-given (pinned) host arrays
+    with the same results they return otherwise."""
+    import torch
+    import vnm_gb300
+    from vnm_gb300 import synth
+    nr, r, c, v = synth.uniform(512, 0.02, 21)
+    newpos = np.random.default_rng(3).permutation(nr).astype(np.int32)
+    pr, pc = ctx.permute_coo(nr, r, c, newpos)
+    orow = torch.empty(len(r), dtype=torch.int32).pin_memory().numpy()
+    ocol = torch.empty(len(c), dtype=torch.int32).pin_memory().numpy()
+    qr, qc = ctx.permute_coo(nr, r, c, newpos, out=(orow, ocol))
+    assert qr is orow and qc is ocol
+    assert np.array_equal(qr, pr) and np.array_equal(qc, pc) and np.array_equal(pr, newpos[r])
+    B = torch.randn((nr, 64)).to(torch.bfloat16).view(torch.int16).numpy()
+    A = vnm_gb300.SpmmMatrix(ctx, nr, pr, pc, v, 8, 32, "bf16")
+    C0 = A.run(B)
+    hC = torch.full((nr, 64), float("nan")).pin_memory().numpy()
+    C1 = A.run(B, C=hC)
+    assert C1 is hC and np.array_equal(C0, C1)
+    A.close()

@@ -212,14 +212,26 @@ class Context:
             start = e
         return out
 
-    def permute_coo(self, nrows, row, col, newpos):
+    def permute_coo(self, nrows, row, col, newpos, out=None):
+        """Relabel a COO by newpos.  CUDA tensors are relabelled in place; host
+        arrays are copied first, into `out` = (row_out, col_out) when given
+        (int32 host arrays of the same length, e.g. pinned), else into new
+        arrays."""
         if hasattr(row, "is_cuda") and row.is_cuda:
             _check(lib().vnm_permute_coo(self.h, nrows, int(row.numel()), ctypes.c_void_p(row.data_ptr()),
                                          ctypes.c_void_p(col.data_ptr()), MEM_DEVICE,
                                          ctypes.c_void_p(newpos.data_ptr())), "vnm_permute_coo")
             return row, col
-        r = np.array(row, np.int32)
-        c = np.array(col, np.int32)
+        if out is not None:
+            r, c = out
+            if r.dtype != np.int32 or c.dtype != np.int32 or len(r) != len(row) or len(c) != len(col) \
+                    or not r.flags["C_CONTIGUOUS"] or not c.flags["C_CONTIGUOUS"]:
+                raise ValueError("out must be two C-contiguous int32 arrays as long as the COO")
+            np.copyto(r, row, casting="same_kind")
+            np.copyto(c, col, casting="same_kind")
+        else:
+            r = np.array(row, np.int32)
+            c = np.array(col, np.int32)
         p = _host(newpos, np.int32)
         _check(lib().vnm_permute_coo(self.h, nrows, len(r), _ptr(r, None), _ptr(c, None), MEM_HOST,
                                      _ptr(p, None)), "vnm_permute_coo")
@@ -315,7 +327,10 @@ class SpmmMatrix:
         return dict(zip(keys, list(out)))
 
     def run(self, B, C=None):
-        """B: torch CUDA tensor (nrows x n, bf16/f16) or numpy uint16 view; returns C (fp32)."""
+        """B: torch CUDA tensor (nrows x n, bf16/f16) or host array of the 16-bit
+        words; returns C (nrows x n fp32) on B's side.  C may be given: a CUDA
+        tensor, or for host B a C-contiguous float32 host array (pinned memory
+        makes the device-to-host copy direct)."""
         if hasattr(B, "is_cuda") and B.is_cuda:
             import torch
             n = B.shape[1]
@@ -326,7 +341,10 @@ class SpmmMatrix:
             return C
         B = np.ascontiguousarray(B)
         n = B.shape[1]
-        C = np.zeros((self.nrows, n), np.float32)
+        if C is None:
+            C = np.empty((self.nrows, n), np.float32)
+        elif C.shape != (self.nrows, n) or C.dtype != np.float32 or not C.flags["C_CONTIGUOUS"]:
+            raise ValueError("C must be a C-contiguous float32 array of shape (nrows, n)")
         _check(lib().vnm_spmm_run(self.ctx.h, self.h, ctypes.c_void_p(B.ctypes.data), n,
                                   ctypes.c_void_p(C.ctypes.data), MEM_HOST), "vnm_spmm_run")
         return C
