@@ -448,7 +448,7 @@ def bench_batch_c3(ctx, reps=3):
             "batched_device_ms": _median(bt), "batched_wall_ms": _median(bw),
             "per_matrix_device_ms_sum": loop_ms, "per_matrix_wall_ms_sum": loop_wall,
             "speedup_wall": loop_wall / _median(bw), "bit_exact_vs_per_matrix": bool(same),
-            "launches": "one persistent launch (one thread block per matrix)"}
+            "launches": "one persistent launch (a two-block cluster per matrix)"}
 
 
 def bench_learned_c4(ctx, reps=3):

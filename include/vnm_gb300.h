@@ -115,7 +115,7 @@ vnm_status vnm_nm_search(vnm_ctx* ctx, int nrows, int nnz, const int* row, const
                          int mem, int N, int M, int nm_maxiter, int* best_sched, int* res5x4, int* newpos_best);
 
 /* Many independent matrices, each with one schedule, reordered in one
- * persistent launch (one thread block per matrix).  Matrix b occupies
+ * persistent launch (a two-block cluster per matrix).  Matrix b occupies
  * row/col/val[nnz_offset[b] .. nnz_offset[b+1]) and has nrows[b] rows;
  * newpos (optional) is laid out at row_offset[b] = sum of nrows[0..b).
  * All arrays are host arrays.  res5 is [nmat][5]. */

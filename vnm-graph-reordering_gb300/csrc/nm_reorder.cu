@@ -1562,7 +1562,7 @@ static vnm_status make_job(vnm_ctx* ctx, const Pattern& P, int sched, int maxite
 // they are small (<= 64 KB), and a row-record table of up to 8192 16-byte
 // slots in what is left of a 150 KB budget (the rest of the SM's 256 KB is L1,
 // which the gather phase's reads of the column pattern live on: 200 KB ran the
-// 256-matrix 2:8 batch 4 % slower).
+// 256-matrix 2:8 batch 4 % slower when it used one block per job).
 constexpr size_t NM_SMEM_BUDGET = 150u << 10;
 
 template <int M>
@@ -1635,7 +1635,7 @@ static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, 
 }
 
 // Blocks per job for calls with few jobs (one matrix, or its four
-// schedules); batches run one block per job.  Measured on GB300 (find_best,
+// schedules); batches run clusters of 2 (run_batch).  Measured on GB300 (find_best,
 // four jobs) with 4 / 8 / 16 blocks: R-MAT 2048 2:8 (26 K entries) 6.7 /
 // 6.8 / 7.3 ms, R-MAT 16384 2:4 (228 K entries) 17.1 / 12.9 / 12.4 ms,
 // R-MAT 65536 2:8 (1.8 M entries) 472 / 295 / 209 ms; so 16 (a non-portable
@@ -1922,7 +1922,11 @@ static vnm_status run_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int6
   VNM_CUDA_TRY(cudaMemcpyAsync(d_jobs, hj.data(), sizeof(NMJob) * nmat, cudaMemcpyHostToDevice, ctx->stream));
   VNM_LAUNCH(ctx, k_batch_init, nmat, 256, 0, d_jobs, P.inv0, P.pres0, d_soff);
   VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main0, ctx->stream));
-  VNM_TRY(launch_rounds(ctx, d_jobs, nmat, N, M, max_nseg));
+  // clusters of 2 blocks per job: the batch's time is its largest matrices'
+  // jobs, and two SMs each shorten them more than the extra waves cost
+  // (GB300, 256 R-MAT matrices 256-8192 rows at 2:8: 88 ms with one block
+  // per job, 63 ms with 2, 69 ms with 4)
+  VNM_TRY(launch_rounds(ctx, d_jobs, nmat, N, M, max_nseg, 2));
   VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main1, ctx->stream));
   int* hres = ctx->h_pinned + 256;
   VNM_CUDA_TRY(cudaMemcpyAsync(hres, res, sizeof(int) * 24 * nmat, cudaMemcpyDeviceToHost, ctx->stream));
