@@ -29,13 +29,14 @@
 //      that touch both segments need the per-(i, j) terms.
 //   4. The pop order of the swap-pair heap is fixed once its gains are known;
 //      the visited filter only skips ahead in it.  So each ordered pair's pop
-//      order is computed once per round by one warp (exact libstdc++ sift
-//      steps, swap_heap.h) and the walk reads the first unvisited entry.
+//      order is computed once per round (exact libstdc++ sift steps, one
+//      thread per heap) and the walk reads the first unvisited entry -- or,
+//      since a heap pops in non-increasing key order, takes the qualifying
+//      swap of largest key directly when no other qualifying swap shares it.
 //
-// One thread block runs one job (a matrix and a schedule) for all of its
-// rounds: no host round trips, no atomics on global counters in the loop,
-// no allocation.  Many jobs (four schedules, or a batch of matrices) run in
-// one launch.
+// One thread-block cluster (or one block) runs one job (a matrix and a
+// schedule) for all of its rounds: no host round trips, no allocation.  Many
+// jobs (four schedules, or a batch of matrices) run in one launch.
 
 #include <cooperative_groups.h>
 
