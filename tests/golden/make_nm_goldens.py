@@ -8,7 +8,8 @@ with the binaries that oracle/ref_build.py builds from the reference sources.
            shipped matrices (mtxfile/*.mtx) to oracle/_ref/fixtures/.
   run      (GPU machine, after `ref_build.py compile`): run every input x
            (N, M) x schedule through oracle/_ref/ref_nm_n<N>_m<M>; raw text
-           results go to --out.
+           results go to --out (default oracle/_ref/nm_raw; on a machine
+           whose files do not come back, a folder that is copied back).
   collect  (anywhere): read the raw results and the inputs, write
            tests/golden/nm_ref_goldens.npz.
 
@@ -162,7 +163,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("step", choices=["prepare", "run", "collect"])
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--out", default=os.path.join(REPO, "gpurun_out", "nm_ref"))
+    ap.add_argument("--out", default=os.path.join(REPO, "oracle", "_ref", "nm_raw"))
     a = ap.parse_args()
     if a.step == "prepare":
         prepare(a.ref)
