@@ -173,3 +173,27 @@ def test_large_gains_match_oracle(ctx):
         res, newpos = ctx.nm_reorder(n, r, c, v, 2, 4, sched)
         assert np.array_equal(res, ores), sched
         assert np.array_equal(newpos, opos), sched
+
+
+@pytest.mark.parametrize("M", [2, 3, 5, 6, 7])
+def test_other_group_sizes_match_oracle(ctx, M):
+    """Group sizes besides 4 and 8 (the reference takes M from mtx/Mtx.h):
+    every schedule against the oracle, on a cluster and on one block."""
+    import os
+    from vnm_gb300 import synth
+    nr, r, c, v = synth.uniform(128 * M, 0.04, 30 + M)
+    N = max(1, M // 2)
+    old = os.environ.get("VNM_NM_CLUSTER")
+    try:
+        for cs in ("8", "1"):
+            os.environ["VNM_NM_CLUSTER"] = cs
+            for sched in range(4):
+                ores, _, _, opos = oracle.nm_run(nr, r, c, v, N, M, sched)
+                res, newpos = ctx.nm_reorder(nr, r, c, v, N, M, sched)
+                assert np.array_equal(res, ores), (cs, sched)
+                assert np.array_equal(newpos, opos), (cs, sched)
+    finally:
+        if old is None:
+            os.environ.pop("VNM_NM_CLUSTER", None)
+        else:
+            os.environ["VNM_NM_CLUSTER"] = old
