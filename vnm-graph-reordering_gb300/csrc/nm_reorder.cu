@@ -60,7 +60,6 @@ constexpr unsigned FULL = 0xffffffffu;
 // status bits a job reports in res[5]
 constexpr int JOB_OK = 0;
 constexpr int JOB_EMPTY_HEAP = 1;   // reference would call top() on an empty queue
-constexpr int JOB_BAD_STATE = 2;    // a count went out of range
 constexpr int JOB_WAIT_LIMIT = 4;   // the walk waited too long for a swap heap's pops
 
 // The part of a job's row work one thread block does: block `rank` of the
@@ -692,7 +691,6 @@ template <int M>
 __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl = Slice{0, 1}) {
   constexpr int K = M + 1;
   constexpr int MM = M * M;
-  constexpr unsigned MASK = (1u << M) - 1u;
   const int Kn = sm.K_;
   const bool self = sm.mode == 2;
   const int lane = threadIdx.x & 31;
