@@ -37,7 +37,8 @@ typedef int vnm_status;
 #define VNM_ERR_UNSORTED 3     /* COO not sorted by (row, col) or has repeats */
 #define VNM_ERR_RANGE 4        /* an index outside [0, nrows) */
 #define VNM_ERR_NOMEM 5        /* device allocation failed */
-#define VNM_ERR_INTERNAL 6     /* a kernel reported a broken invariant */
+#define VNM_ERR_INTERNAL 6     /* a kernel reported a broken invariant, or a bounded wait inside a
+                                  kernel ran out (it returns instead of spinning on) */
 #define VNM_ERR_IO 7           /* file could not be read or written */
 #define VNM_ERR_FORMAT 8       /* Matrix Market banner/size/type not supported */
 #define VNM_ERR_NO_DEVICE 9    /* no usable CUDA device */
