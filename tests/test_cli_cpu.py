@@ -32,3 +32,13 @@ def test_refused_parameters(tmp_path, extra):
     args = ["--mtxfile", str(p), "--outmtxfile", "o.mtx", "--maxiter", "1", "--v", "32"]
     r = _run(args + extra if "--v" not in extra else args[:-2] + extra, str(tmp_path))
     assert r.returncode == 1 and "need 1 <= N < M <= 8" in r.stderr
+
+
+def test_bench_flags():
+    """bench.py parses its flags without a GPU (the measured runs need one)."""
+    import sys
+    r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--help"], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    for flag in ("--gpus", "--steps", "--warmup", "--impl", "--no-cpu-baseline", "--no-extended", "--c5-spmm-only"):
+        assert flag in r.stdout
