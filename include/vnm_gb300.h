@@ -143,11 +143,14 @@ vnm_status vnm_nm_get_trace(vnm_ctx* ctx, int* pairs, int cap_pairs, int* npairs
  *   - row, col, val: device memory of the current device, sorted COO as for
  *     vnm_nm_reorder; res5 (5 ints) and newpos (nrows ints): device memory
  *     the caller owns; work is issued on `stream` (a cudaStream_t, NULL for
- *     the default stream) and the call returns when it is done.
+ *     the default stream).  The call reads a status back on the host and
+ *     synchronises `stream` before it returns.
  *   - nrows <= VNM_NOALLOC_MAX_ROWS and nnz <= VNM_NOALLOC_MAX_NNZ, else
  *     VNM_ERR_LIMIT.
- *   - The first call on a device looks up the array's device address with
- *     that device current; make that first call before any stream capture.
+ *   - Each call looks up the array's device address on the current device
+ *     (no stream work), so a device reset between calls does no harm.
+ *   - Each job runs on a thread-block cluster sized as vnm_nm_reorder sizes
+ *     it; results are identical to vnm_nm_reorder's.
  *   - All calls share the array.  Calls that overlap on the GPU (from other
  *     streams or host threads) race; serialise them. */
 #define VNM_NOALLOC_MAX_ROWS 32768

@@ -43,6 +43,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -1564,8 +1565,16 @@ static vnm_status make_job(vnm_ctx* ctx, const Pattern& P, int sched, int maxite
 // 256-matrix 2:8 batch 4 % slower when it used one block per job).
 constexpr size_t NM_SMEM_BUDGET = 150u << 10;
 
+// k_nm_rounds<M>'s dynamic shared-memory ceiling depends on the launch shape
+// (a single-block job keeps a row table on chip, a cluster job does not), and
+// it is a property of the function shared by every host thread: one lock
+// covers each setting of it together with the launch it is for, so that a
+// call on another thread cannot lower it in between.
+static std::mutex g_round_launch_mu;
+
 template <int M>
 static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, int N, int max_nseg, int cs) {
+  std::lock_guard<std::mutex> launch_lock(g_round_launch_mu);
   const size_t cbytes = (size_t)max_nseg * sizeof(int);
   const int in_smem = cbytes <= (64u << 10) ? 1 : 0;
   const size_t hbytes = (size_t)RoundSmem<M>::SCR_U4 * sizeof(uint4);
@@ -2111,7 +2120,6 @@ vnm_status vnm_nm_reorder_batch(vnm_ctx* ctx, int nmat, const int* nrows, const 
 // keeps it until the process exits.  All calls share it: calls that overlap
 // on the GPU (other streams, other host threads) race and must not be made.
 // ---------------------------------------------------------------------------
-#include <mutex>
 
 namespace vnm {
 
@@ -2124,24 +2132,17 @@ constexpr size_t NOALLOC_BYTES = size_t(10) << 20;  // 10 MiB
 // device address instead (noalloc_scratch below).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 
-// Device address of g_noalloc_scratch on `device`, looked up once per device
-// with that device current.
-static vnm_status noalloc_scratch(int device, unsigned char** out) {
-  constexpr int MAXDEV = 64;
-  static unsigned char* addr[MAXDEV] = {nullptr};
-  static std::mutex mu;
-  if (device < 0 || device >= MAXDEV) return VNM_ERR_ARG;
-  std::lock_guard<std::mutex> lock(mu);
-  if (!addr[device]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      (void)cudaGetLastError();
-      return VNM_ERR_CUDA;
-    }
-    addr[device] = static_cast<unsigned char*>(p);
+// Device address of g_noalloc_scratch on the current device.  Looked up on
+// every call (no stream work, no allocation): an address kept from an
+// earlier call would be stale after a device reset, which reloads the module.
+static vnm_status noalloc_scratch(unsigned char** out) {
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
+    (void)cudaGetLastError();
+    return VNM_ERR_CUDA;
   }
-  *out = addr[device];
+  *out = static_cast<unsigned char*>(p);
   return VNM_OK;
 }
 
@@ -2159,7 +2160,7 @@ extern "C" vnm_status vnm_nm_reorder_noalloc(int nrows, int nnz, const int* row,
   int device = 0;
   VNM_CUDA_TRY(cudaGetDevice(&device));
   unsigned char* scratch = nullptr;
-  VNM_TRY(noalloc_scratch(device, &scratch));
+  VNM_TRY(noalloc_scratch(&scratch));
   // a context on the stack: its "arena" is the fixed array, its stream the
   // caller's; no event, stream or memory is created
   vnm_ctx c;
@@ -2178,7 +2179,9 @@ extern "C" vnm_status vnm_nm_reorder_noalloc(int nrows, int nnz, const int* row,
   NMJob* d_job = arena_take<NMJob>(&c, 1);
   if (!d_job) return VNM_ERR_LIMIT;
   VNM_CUDA_TRY(cudaMemcpyAsync(d_job, &hj, sizeof(NMJob), cudaMemcpyHostToDevice, c.stream));
-  VNM_TRY(launch_rounds(&c, d_job, 1, N, M, P.nseg));
+  // the same launch shape as vnm_nm_reorder (a cluster of blocks per job);
+  // the scratch it needs does not depend on the cluster size
+  VNM_TRY(launch_rounds(&c, d_job, 1, N, M, P.nseg, nm_cluster_size(P.np)));
   VNM_CUDA_TRY(cudaMemcpyAsync(hs, hj.res, sizeof(int) * 16, cudaMemcpyDeviceToHost, c.stream));
   VNM_CUDA_TRY(cudaStreamSynchronize(c.stream));
   if (hs[5] != 0) return VNM_ERR_INTERNAL;
