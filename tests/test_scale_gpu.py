@@ -1,0 +1,87 @@
+"""Bit-exact parity at the sizes the benchmark measures.
+
+  c2  R-MAT 16384, 2:4 (the headline step's find_best_2toX): all four
+      schedules against the oracle (tests/golden/scale_oracle_goldens.npz)
+      and against the reference's own GPU code run on the same matrix
+      (tests/golden/scale_ref_c2.npz)
+  c4  R-MAT 65536, 2:8 (the plain reorder the learned mode is compared
+      with): all four schedules against the oracle
+  c3  the 256-matrix batch, one launch: three of its matrices (the
+      smallest, a middle one, the largest) against the oracle run here
+
+The oracle needs minutes per schedule at c4, so its results are committed
+fixtures (tests/golden/make_scale_goldens.py); the input is regenerated from
+its seed and checked against the fixture's SHA-256 first."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _scale():
+    import sys
+    sys.path.insert(0, GOLD)
+    import make_scale_goldens
+    return make_scale_goldens
+
+
+def _check_workload(ctx, name, g):
+    msg = _scale()
+    nr, r, c, v, N, M = msg.load(name)
+    assert msg.coo_digest(nr, r, c, v) == str(g[name + "__sha256"]), "the seeded generator gave another matrix"
+    best, res4, newpos = ctx.nm_search(nr, r, c, v, N, M)
+    assert np.array_equal(res4, g[name + "__res5x4"]), (res4, g[name + "__res5x4"])
+    assert best == int(g[name + "__best"])
+    assert np.array_equal(newpos, g[name + "__newpos4"][best])
+    for s in range(4):
+        res, pos = ctx.nm_reorder(nr, r, c, v, N, M, s)
+        assert np.array_equal(res, g[name + "__res5x4"][s]), s
+        assert np.array_equal(pos, g[name + "__newpos4"][s]), s
+
+
+def test_c2_matches_oracle(ctx):
+    g = np.load(os.path.join(GOLD, "scale_oracle_goldens.npz"))
+    _check_workload(ctx, "c2", g)
+
+
+def test_c4_plain_matches_oracle(ctx):
+    g = np.load(os.path.join(GOLD, "scale_oracle_goldens.npz"))
+    _check_workload(ctx, "c4", g)
+
+
+def test_c2_matches_reference_gpu_code(ctx):
+    """The reference's own reorder (reorder/reorder.h:1805-2474, built from
+    its sources) on the c2 matrix: every schedule's result integers and the
+    final position of every node that carries an entry."""
+    g = np.load(os.path.join(GOLD, "scale_ref_c2.npz"))
+    msg = _scale()
+    nr, r, c, v, N, M = msg.load("c2")
+    assert msg.coo_digest(nr, r, c, v) == str(g["sha256"])
+    best, res4, newpos = ctx.nm_search(nr, r, c, v, N, M)
+    assert np.array_equal(res4, g["res5x4"])
+    assert best == int(g["best"])
+    for s in range(4):
+        _, pos = ctx.nm_reorder(nr, r, c, v, N, M, s)
+        want = g["newpos4"][s]
+        m = want >= 0
+        assert np.array_equal(pos[m], want[m]), s
+
+
+def test_c3_batch_members_match_oracle(ctx):
+    from vnm_gb300 import synth
+    M = 8
+    mats = [((n + M - 1) // M * M, r, c, v) for n, r, c, v in synth.rmat_batch(256)]
+    res, pos = ctx.nm_reorder_batch(mats, 2, M, 0)
+    sizes = np.array([m[0] for m in mats])
+    order = np.argsort(sizes, kind="stable")
+    for b in (int(order[0]), int(order[len(order) // 2]), int(order[-1])):
+        nr, r, c, v = mats[b]
+        ores, _, _, opos = oracle.nm_run(nr, r, c, v, 2, M, 0)
+        assert np.array_equal(res[b], ores), (b, nr)
+        assert np.array_equal(pos[b], opos), (b, nr)
