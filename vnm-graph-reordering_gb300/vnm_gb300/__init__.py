@@ -321,9 +321,10 @@ class SpmmMatrix:
         self.h = h
 
     def info(self):
-        out = (ctypes.c_longlong * 8)()
-        _check(lib().vnm_spmm_info(self.h, out, 8), "vnm_spmm_info")
-        keys = ("nnz", "blocks", "valid_blocks", "slices", "slices_padded", "ksteps", "tiles", "a_bytes")
+        out = (ctypes.c_longlong * 13)()
+        _check(lib().vnm_spmm_info(self.h, out, 13), "vnm_spmm_info")
+        keys = ("nnz", "blocks", "valid_blocks", "slices", "slices_padded", "ksteps", "tiles", "a_bytes",
+                "residual_nnz", "residual_tasks", "tensor_tiles", "dense_min", "split_chunks")
         return dict(zip(keys, list(out)))
 
     def run(self, B, C=None):
@@ -489,3 +490,41 @@ def nm_learned(ctx, nrows, row, col, val, N, M, mode=LEARNED_MLP, net=None, obje
     res = {k: getattr(r, k) for k, _ in _LearnedResult._fields_ if k != "reserved"}
     dump = (dx[:r.ndump], dy[:r.ndump]) if dx is not None else None
     return res, newpos, dump
+
+
+# ---------------------------------------------------------------------------
+# Matrix Market files (host code of the library; no GPU needed)
+# ---------------------------------------------------------------------------
+def _io_lib():
+    L = lib()
+    if not hasattr(L, "_io_typed"):
+        L.vnm_mtx_read.argtypes = [ctypes.c_char_p, ctypes.c_int, _i32p, _i32p, _i32p, ctypes.POINTER(_i32p),
+                                   ctypes.POINTER(_i32p), ctypes.POINTER(_f32p)]
+        L.vnm_mtx_write.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p, _i32p, _f32p]
+        L.vnm_host_free.argtypes = [ctypes.c_void_p]
+        L._io_typed = True
+    return L
+
+
+def read_mtx(path, aligned=1):
+    """readMtx + the row padding of Mtx::init_from_file: (nrows, ncols, row,
+    col, val), sorted by (row, col), repeats removed, symmetric mirrored."""
+    L = _io_lib()
+    nr, nc, nz = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    r, c, v = _i32p(), _i32p(), _f32p()
+    _check(L.vnm_mtx_read(os.fsencode(path), int(aligned), nr, nc, nz, ctypes.byref(r), ctypes.byref(c),
+                          ctypes.byref(v)), "vnm_mtx_read")
+    n = nz.value
+    out = []
+    for p, t in ((r, np.int32), (c, np.int32), (v, np.float32)):
+        out.append(np.ctypeslib.as_array(p, shape=(n,)).astype(t, copy=True) if n else np.zeros(0, t))
+        L.vnm_host_free(ctypes.cast(p, ctypes.c_void_p))
+    return (nr.value, nc.value) + tuple(out)
+
+
+def write_mtx(path, nrows, ncols, row, col, val):
+    """Mtx::write_to_file: "real general" banner, "%d %d %.2f" lines, 1-based."""
+    L = _io_lib()
+    r, c, v = _host(row, np.int32), _host(col, np.int32), _host(val, np.float32)
+    _check(L.vnm_mtx_write(os.fsencode(path), int(nrows), int(ncols), len(r), r.ctypes.data_as(_i32p),
+                           c.ctypes.data_as(_i32p), v.ctypes.data_as(_f32p)), "vnm_mtx_write")
