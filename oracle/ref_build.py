@@ -11,6 +11,11 @@ mtx/Mtx.h:15-16 set to N and M -- the configuration step the reference's
 README prescribes -- followed by oracle/ref_harness.cu.  oracle/_ref/ is not
 committed; it is a build directory.
 
+The same step also writes oracle/_ref/ref_spmm_n<N>_m<M>.cu for the (N, M)
+pairs of the command's golden cases: main.cu itself (the `spmm` command of
+main.cu:339-352 with find_best_2toX and hybrid_reordering) with its quoted
+#includes inlined the same way.
+
 Step 2 (`compile`, run on a machine with nvcc; needs a GPU only to *run*):
 nvcc each flattened unit for sm_103a against cuSPARSE/cuBLAS, as the
 reference's Makefile does for sm_89, with -maxrregcount=64.  The register cap
@@ -21,8 +26,11 @@ it then exceeds the 65536 registers of an SM, the launch fails, nothing
 checks it, and every gain stays at the cudaMemset zero.  With the cap the
 kernel launches and computes what its source says, as on sm_89.
 
+The reference checkout is read from --ref, else from $VNM_REF_DIR, else
+from /root/reference.
+
 usage: python oracle/ref_build.py flatten [--ref DIR]
-       python oracle/ref_build.py compile
+       python oracle/ref_build.py compile [--only NAME]
 """
 import argparse
 import os
@@ -34,6 +42,8 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 CONFIGS = [(2, 8), (2, 4), (1, 4), (3, 8)]
+SPMM_CONFIGS = [(2, 8), (2, 4)]
+DEFAULT_REF = os.environ.get("VNM_REF_DIR", "/root/reference")
 INC_RE = re.compile(r'^\s*#\s*include\s+"([^"]+)"')
 
 
@@ -75,6 +85,13 @@ def flatten(ref):
         with open(p, "w") as f:
             f.writelines(lines)
         paths.append(p)
+    for N, M in SPMM_CONFIGS:
+        lines = ["// generated by oracle/ref_build.py from the reference checkout; not committed\n"]
+        _inline(os.path.join(ref, "main.cu"), set(), lines, (N, M))
+        p = os.path.join(OUT, "ref_spmm_n%d_m%d.cu" % (N, M))
+        with open(p, "w") as f:
+            f.writelines(lines)
+        paths.append(p)
     return paths
 
 
@@ -88,8 +105,22 @@ def _nvcc(src):
     return exe
 
 
-def compile_all():
+def ensure(name):
+    """Path of the compiled unit oracle/_ref/<name>, compiling it first when
+    its binary is missing or older than its flattened source."""
+    exe = os.path.join(OUT, name)
+    src = exe + ".cu"
+    if not os.path.exists(src):
+        raise FileNotFoundError("missing %s: run oracle/ref_build.py flatten where the reference checkout is" % src)
+    if not os.path.exists(exe) or os.path.getmtime(exe) < os.path.getmtime(src):
+        _nvcc(src)
+    return exe
+
+
+def compile_all(only=None):
     srcs = sorted(os.path.join(OUT, f) for f in os.listdir(OUT) if f.endswith(".cu")) if os.path.isdir(OUT) else []
+    if only:
+        srcs = [p for p in srcs if os.path.basename(p)[:-3] == only]
     if not srcs:
         return []
     with ThreadPoolExecutor(max_workers=len(srcs)) as ex:
@@ -99,7 +130,8 @@ def compile_all():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("step", choices=["flatten", "compile"])
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=DEFAULT_REF)
+    ap.add_argument("--only", default=None, help="compile one unit, e.g. ref_nm_n2_m4")
     a = ap.parse_args()
     if a.step == "flatten":
         if not os.path.isdir(a.ref):
@@ -107,7 +139,7 @@ def main():
         for p in flatten(a.ref):
             print(p)
     else:
-        for p in compile_all():
+        for p in compile_all(a.only):
             print(p)
 
 

@@ -4,8 +4,10 @@ The reference's NM path is CUDA, so its goldens are made on a GPU machine
 with the binaries that oracle/ref_build.py builds from the reference sources.
 
   prepare  (where the reference checkout is): write the synthetic inputs to
-           tests/golden/nm_inputs/ (committed) and copy the reference's
-           shipped matrices (mtxfile/*.mtx) to oracle/_ref/fixtures/.
+           tests/golden/nm_inputs/ and copy the reference's shipped matrices
+           (mtxfile/*.mtx) to oracle/_ref/fixtures/.  Neither folder is
+           committed: the npz below holds every input's COO as the
+           reference's reader returned it, which is what the tests use.
   run      (GPU machine, after `ref_build.py compile`): run every input x
            (N, M) x schedule through oracle/_ref/ref_nm_n<N>_m<M>; raw text
            results go to --out (default oracle/_ref/nm_raw; on a machine
@@ -162,7 +164,7 @@ def collect(src):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("step", choices=["prepare", "run", "collect"])
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("VNM_REF_DIR", "/root/reference"))
     ap.add_argument("--out", default=os.path.join(REPO, "oracle", "_ref", "nm_raw"))
     a = ap.parse_args()
     if a.step == "prepare":

@@ -70,7 +70,7 @@ def run_script(ref, tmp, args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("VNM_REF_DIR", "/root/reference"))
     a = ap.parse_args()
     from scipy.io import mmread, mmwrite
     from scipy.sparse import coo_matrix

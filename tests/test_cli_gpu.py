@@ -1,26 +1,37 @@
-"""The drop-in `spmm` command against the oracle's emulation of the
-reference command (find_best_2toX + hybrid_reordering with its file round
-trips): the 15 CSV fields other than the time, and the output .mtx text."""
+"""The drop-in `spmm` command against the reference's own command and the
+oracle's emulation of it.
+
+Reference: tests/golden/cli_ref_goldens.npz holds what the reference's
+`spmm` (main.cu built from its sources, its VNM stage the real
+reordering.py) printed and wrote on each case, with temp.mtx in its working
+directory a copy of the input (main.cu:207 evaluates whatever temp.mtx is
+there first).  The drop-in runs in a directory prepared the same way; its 15
+CSV fields other than the time and its output .mtx text must match.
+Oracle: orc_spmm_cli, which composes the oracle's pinned pieces with the
+file round trips, on the same cases plus --maxiter 0 (which the reference
+cannot run: it indexes an empty vector, main.cu:331)."""
 import os
+import shutil
 import subprocess
 
 import numpy as np
 import pytest
 
 import oracle
-from golden_cases import nm_input
+from golden_cases import CLI_CASES, cli_input
 
 pytestmark = pytest.mark.gpu
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SPMM = os.path.join(REPO, "vnm-graph-reordering_gb300", "spmm")
+REF = os.path.join(REPO, "tests", "golden", "cli_ref_goldens.npz")
 
 
-def _cli(tmp_path, mtx, N, M, V, maxiter):
-    out = str(tmp_path / "out.mtx")
+def _cli(wd, mtx, N, M, V, maxiter):
+    out = os.path.join(wd, "out.mtx")
     r = subprocess.run([SPMM, "--mtxfile", mtx, "--outmtxfile", out, "--maxiter", str(maxiter), "--n", "64",
                         "--sched", "0", "--v", str(V), "--N", str(N), "--M", str(M)],
-                       cwd=str(tmp_path), capture_output=True, text=True, timeout=600)
+                       cwd=wd, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
     fields = [float(x) for x in r.stdout.strip().split(",")]
     with open(out) as f:
@@ -28,43 +39,38 @@ def _cli(tmp_path, mtx, N, M, V, maxiter):
     return fields, text
 
 
-def _oracle(tmp_path, mtx, N, M, V, maxiter):
+def _write_input(wd, name, goldens, fname=None):
+    from vnm_gb300 import synth
+    p = os.path.join(wd, (fname or name) + ".mtx")
+    synth.write_mtx(p, *cli_input(name, goldens))
+    return p
+
+
+@pytest.mark.parametrize("case,name,N,M,V,maxiter", CLI_CASES)
+def test_cli_matches_oracle(tmp_path, goldens, case, name, N, M, V, maxiter):
+    mtx = _write_input(str(tmp_path), name, goldens)
+    fields, text = _cli(str(tmp_path), mtx, N, M, V, maxiter)
     csv, best, nr, r, c, v = oracle.spmm_cli(mtx, N, M, V, maxiter)
     p = str(tmp_path / "oracle_out.mtx")
     oracle.write_mtx(p, nr, nr, r, c, v)
     with open(p) as f:
-        return csv, f.read()
-
-
-def _write_input(tmp_path, name, nr, r, c, v):
-    from vnm_gb300 import synth
-    p = str(tmp_path / (name + ".mtx"))
-    synth.write_mtx(p, nr, r, c, v)
-    return p
-
-
-CASES = [("u256", 2, 8, 32, 2), ("u256", 2, 4, 64, 1), ("rmat1k", 2, 8, 32, 3), ("fixture_lund", 2, 8, 32, 2),
-         ("fixture_gd95", 2, 8, 4, 2), ("sym96", 2, 8, 8, 2), ("u256", 2, 8, 32, 0)]
-
-
-@pytest.mark.parametrize("name,N,M,V,maxiter", CASES)
-def test_cli_matches_oracle(tmp_path, goldens, name, N, M, V, maxiter):
-    from vnm_gb300 import synth
-    if name == "u256":
-        mtx = _write_input(tmp_path, name, *synth.uniform(256, 0.05, 3))
-    elif name == "rmat1k":
-        mtx = _write_input(tmp_path, name, *synth.rmat(10, 4096, 5, "uniform"))
-    elif name == "sym96":
-        n, r, c, v = synth.rmat(7, 300, 22, "uniform", R=96)
-        lo, hi = np.minimum(r, c), np.maximum(r, c)
-        v = np.round(np.sin(lo * 7.0 + hi * 3.0) * 0.9, 2).astype(np.float32)  # symmetric values
-        mtx = _write_input(tmp_path, name, n, r, c, v)
-    else:
-        key = {"fixture_lund": "lund_b__n2_m8", "fixture_gd95": "GD95_a__n2_m8"}[name]
-        nr, r, c, v = nm_input(goldens, key)
-        mtx = _write_input(tmp_path, name, nr, r, c, v)
-    fields, text = _cli(tmp_path, mtx, N, M, V, maxiter)
-    ocsv, otext = _oracle(tmp_path, mtx, N, M, V, maxiter)
+        otext = f.read()
     assert len(fields) == 16
-    np.testing.assert_allclose(fields[:15], ocsv[:15], rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(fields[:15], csv[:15], rtol=1e-5, atol=1e-6)
     assert text == otext
+
+
+@pytest.mark.parametrize("case", [c[0] for c in CLI_CASES if c[5] > 0])
+def test_cli_matches_reference_command(tmp_path, goldens, case):
+    if not os.path.exists(REF):
+        pytest.skip("the reference command's goldens are not collected yet (tests/golden/make_cli_goldens.py)")
+    g = np.load(REF)
+    _, name, N, M, V, maxiter = next(c for c in CLI_CASES if c[0] == case)
+    wd = str(tmp_path)
+    mtx = _write_input(wd, name, goldens, fname="input")
+    shutil.copyfile(mtx, os.path.join(wd, "temp.mtx"))  # the stale file the first evaluation reads
+    fields, text = _cli(wd, "input.mtx", N, M, V, maxiter)
+    want = [float(x) for x in str(g["csv__" + case]).split(",")]
+    assert len(fields) == len(want) == 16
+    np.testing.assert_allclose(fields[:15], want[:15], rtol=1e-5, atol=1e-6)
+    assert text.encode() == g["out__" + case].tobytes()

@@ -127,15 +127,40 @@ def test_status_strings_and_cpu_side_errors():
         vnm_gb300.swap_heap_order(np.zeros(300), np.zeros(300))
 
 
-def test_oracle_cli_composition_on_fixture():
+def test_oracle_cli_composition_on_fixture(tmp_path):
     """The whole spmm command on a small file: CSV fields are consistent."""
-    d = os.path.join(REPO, "tests", "golden", "nm_inputs")
-    if not os.path.isdir(d):
-        pytest.skip("golden inputs not generated")
-    path = os.path.join(d, "u256_d05.mtx")
+    from vnm_gb300 import synth
+    path = str(tmp_path / "u256_d05.mtx")
+    synth.write_mtx(path, *synth.uniform(256, 0.05, 3))
     csv, best, nr, r, c, v = oracle.spmm_cli(path, 2, 8, 32, 2)
     nr0, _, r0, c0, v0 = oracle.read_mtx(path, 8)
     res0, _, _, _ = oracle.nm_run(nr0, r0, c0, v0, 2, 8, best)
     assert csv[0] == nr0 and csv[1] == len(r0)
     assert csv[3] == res0[0] and csv[5] == res0[2]
     assert len(r) == len(r0) and nr == nr0
+
+
+def test_oracle_cli_matches_reference_command(tmp_path, goldens):
+    """orc_spmm_cli against the reference's own `spmm` command
+    (tests/golden/cli_ref_goldens.npz: main.cu built from its sources, its
+    VNM stage the real reordering.py; temp.mtx in its working directory a
+    copy of the input, so the stale first evaluation of main.cu:207 reads
+    the input): the 15 CSV fields other than the time and the output text."""
+    from golden_cases import CLI_CASES, cli_input
+    from vnm_gb300 import synth
+    p = os.path.join(REPO, "tests", "golden", "cli_ref_goldens.npz")
+    if not os.path.exists(p):
+        pytest.skip("the reference command's goldens are not collected yet (tests/golden/make_cli_goldens.py)")
+    g = np.load(p)
+    assert len(g["cases"]) == len([c for c in CLI_CASES if c[5] > 0])
+    for case, name, N, M, V, maxiter in CLI_CASES:
+        if maxiter == 0:
+            continue
+        p = str(tmp_path / (case + ".mtx"))
+        synth.write_mtx(p, *cli_input(name, goldens))
+        csv, best, nr, r, c, v = oracle.spmm_cli(p, N, M, V, maxiter, init_mb_path=p)
+        want = [float(x) for x in str(g["csv__" + case]).split(",")]
+        np.testing.assert_allclose(csv[:15], want[:15], rtol=1e-5, atol=1e-6, err_msg=case)
+        q = str(tmp_path / (case + "_out.mtx"))
+        oracle.write_mtx(q, nr, nr, r, c, v)
+        assert open(q, "rb").read() == g["out__" + case].tobytes(), case
