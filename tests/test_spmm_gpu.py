@@ -1,7 +1,10 @@
 """V:N:M SpMM on tcgen05 against the FP64 oracle (orc_spmm_f64).
 
-Error measure: max |C - C64| / max |C64| (normwise), tolerance 1e-2 as the
-north star states for BF16/FP16 operands with FP32 accumulation."""
+Error measure: the largest per-row relative error
+max_i ||C_i - C64_i||_inf / ||C64_i||_inf (oracle.rowwise_rel_err; a row whose
+reference is zero must come out zero), tolerance 1e-2 as the benchmark spec
+states for BF16/FP16 operands with FP32 accumulation.  Per row, so that a
+low-degree row cannot hide behind the hub rows of a power-law graph."""
 import numpy as np
 import pytest
 
@@ -9,6 +12,33 @@ import oracle
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-2
+
+
+class _dense_min:
+    """VNM_SPMM_DENSE_MIN for the operands compressed inside the block: 0
+    puts every V:N:M block on the tensor cores, a huge value every block on
+    the CUDA-core residual path."""
+
+    def __init__(self, value):
+        self.value = value
+
+    def __enter__(self):
+        import os
+        self.old = os.environ.get("VNM_SPMM_DENSE_MIN")
+        if self.value is None:
+            os.environ.pop("VNM_SPMM_DENSE_MIN", None)
+        else:
+            os.environ["VNM_SPMM_DENSE_MIN"] = str(self.value)
+
+    def __exit__(self, *a):
+        import os
+        if self.old is None:
+            os.environ.pop("VNM_SPMM_DENSE_MIN", None)
+        else:
+            os.environ["VNM_SPMM_DENSE_MIN"] = self.old
+
+
+TENSOR_ONLY, RESIDUAL_ONLY, DEFAULT = 0, 1 << 30, None
 
 
 def _run(ctx, nr, r, c, v, M, V, n, dtype, seed=0):
@@ -20,41 +50,70 @@ def _run(ctx, nr, r, c, v, M, V, n, dtype, seed=0):
     A = vnm_gb300.SpmmMatrix(ctx, nr, r, c, v, M, V, dtype)
     C = A.run(B.cuda()).cpu().numpy().astype(np.float64)
     ref = oracle.spmm_f64(nr, r, c, v.astype(np.float64), B.float().numpy().astype(np.float64))
-    err = np.abs(C - ref).max() / max(np.abs(ref).max(), 1e-30)
-    return err, A.info()
+    return oracle.rowwise_rel_err(C, ref), A.info()
 
 
-def test_spmm_identity_is_exact(ctx):
+@pytest.mark.parametrize("split", [TENSOR_ONLY, RESIDUAL_ONLY])
+def test_spmm_identity_is_exact(ctx, split):
     nr = 256
     idx = np.arange(nr, dtype=np.int32)
-    err, info = _run(ctx, nr, idx, idx, np.ones(nr, np.float32), 4, 64, 128, "bf16")
+    with _dense_min(split):
+        err, info = _run(ctx, nr, idx, idx, np.ones(nr, np.float32), 4, 64, 128, "bf16")
     assert err < 1e-6, err
-    assert info["slices"] == info["blocks"] == info["valid_blocks"]
+    if split == TENSOR_ONLY:
+        assert info["slices"] == info["blocks"] == info["valid_blocks"] and info["residual_nnz"] == 0
+    else:
+        assert info["residual_nnz"] == nr and info["ksteps"] == 0
 
 
+@pytest.mark.parametrize("split", [TENSOR_ONLY, RESIDUAL_ONLY, DEFAULT])
 @pytest.mark.parametrize("dtype", ["bf16", "fp16"])
-@pytest.mark.parametrize("n", [64, 128, 256])
-def test_spmm_random_matches_fp64(ctx, dtype, n):
+@pytest.mark.parametrize("n", [64, 128, 192, 256])
+def test_spmm_random_matches_fp64(ctx, dtype, n, split):
     from vnm_gb300 import synth
     nr, r, c, v = synth.uniform(384, 0.03, 5)
-    err, info = _run(ctx, nr, r, c, v, 8, 32, n, dtype)
+    with _dense_min(split):
+        err, info = _run(ctx, nr, r, c, v, 8, 32, n, dtype)
     assert err < TOL, (err, info)
 
 
 def test_spmm_rmat_blocks_that_violate_vnm(ctx):
     from vnm_gb300 import synth
     nr, r, c, v = synth.rmat(11, 12000, 9, "normal")   # dense hubs: many blocks need extra slices
-    err, info = _run(ctx, nr, r, c, v, 4, 64, 128, "bf16")
+    with _dense_min(TENSOR_ONLY):
+        err, info = _run(ctx, nr, r, c, v, 4, 64, 128, "bf16")
     assert info["slices"] > info["valid_blocks"]
     assert err < TOL, (err, info)
 
 
-def test_spmm_partial_last_tile_and_empty_tiles(ctx):
+@pytest.mark.parametrize("n", [64, 128, 256])
+def test_spmm_hybrid_split_and_hub_rows(ctx, n):
+    """Dense blocks on the tensor cores, sparse ones on the CUDA cores in one
+    product: R-MAT hubs plus three rows with 700-1900 nonzeros, which the
+    residual path cuts into chunks and adds back in chunk order."""
+    from vnm_gb300 import synth
+    nr, r, c, v = synth.rmat(11, 12000, 9, "normal")  # 2048 rows
+    rng = np.random.default_rng(2)
+    extra_r = np.concatenate([np.full(1900, 7), np.full(1500, 700), np.full(700, 1999)])
+    extra_c = np.concatenate([rng.choice(nr, 1900, replace=False), rng.choice(nr, 1500, replace=False),
+                              rng.choice(nr, 700, replace=False)])
+    key = np.unique(np.concatenate([r.astype(np.int64) * nr + c, extra_r.astype(np.int64) * nr + extra_c]))
+    r, c = (key // nr).astype(np.int32), (key % nr).astype(np.int32)
+    v = rng.standard_normal(len(r)).astype(np.float32)
+    with _dense_min(4):
+        err, info = _run(ctx, nr, r, c, v, 4, 64, n, "bf16")
+    assert info["residual_nnz"] > 0 and info["tensor_tiles"] > 0 and info["split_chunks"] > 0, info
+    assert err < TOL, (err, info)
+
+
+@pytest.mark.parametrize("split", [TENSOR_ONLY, RESIDUAL_ONLY, 4])
+def test_spmm_partial_last_tile_and_empty_tiles(ctx, split):
     nr = 328   # 3 tiles, the last one partly outside the matrix
     r = np.array([0, 5, 130, 300, 327], np.int32)
     c = np.array([3, 320, 9, 4, 327], np.int32)
     v = np.array([1.5, -2.0, 0.25, 3.0, -1.0], np.float32)
-    err, info = _run(ctx, nr, r, c, v, 8, 64, 64, "bf16")
+    with _dense_min(split):
+        err, info = _run(ctx, nr, r, c, v, 8, 64, 64, "bf16")
     assert err < TOL
 
 
@@ -68,8 +127,10 @@ def test_spmm_every_column_block_width(ctx, width):
     os.environ["VNM_SPMM_WIDTH"] = str(width)
     try:
         nr, r, c, v = synth.rmat(10, 1024 * 6, 9, "normal")
-        err, info = _run(ctx, nr, r, c, v, 8, 64, 256, "bf16")
-        assert err < TOL, (width, err)
+        for split in (TENSOR_ONLY, 4):
+            with _dense_min(split):
+                err, info = _run(ctx, nr, r, c, v, 8, 64, 256, "bf16")
+            assert err < TOL, (width, split, err)
     finally:
         if old is None:
             os.environ.pop("VNM_SPMM_WIDTH", None)
@@ -97,7 +158,7 @@ def test_storage_reuse_and_operand_outliving_its_context():
     C = A.run(B).cpu().numpy().astype(np.float64)
     c2.close()
     ref = oracle.spmm_f64(nr, r, c, v.astype(np.float64), B.float().cpu().numpy().astype(np.float64))
-    assert np.abs(C - ref).max() / max(np.abs(ref).max(), 1e-30) <= TOL
+    assert oracle.rowwise_rel_err(C, ref) <= TOL
     A.close()
 
 
@@ -122,3 +183,15 @@ def test_host_outputs_given_by_the_caller(ctx):
     C1 = A.run(B, C=hC)
     assert C1 is hC and np.array_equal(C0, C1)
     A.close()
+
+
+@pytest.mark.parametrize("V", [32, 64, 128])
+def test_full_vnm_blocks_go_to_the_tensor_cores(ctx, V):
+    """A matrix in full V:2:8 form (every block 2V nonzeros): by default
+    every block runs on the tensor cores, and the product matches FP64."""
+    from vnm_gb300 import synth
+    nr, r, c, v = synth.vnm_structured(512, 8, V, seed=V)
+    err, info = _run(ctx, nr, r, c, v, 8, V, 128, "bf16")
+    assert info["residual_nnz"] == 0 and info["valid_blocks"] == info["blocks"] == info["slices"], info
+    assert info["tensor_tiles"] == info["tiles"]
+    assert err < TOL, (err, info)

@@ -70,6 +70,14 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
 }
 
+// As cp_async16, reading only the first `src_bytes` (0 or 16) of `src` and
+// filling the rest of the 16 bytes with zeros: with 0 nothing is read, and
+// `src` must still be a valid address.
+__device__ __forceinline__ void cp_async16_zfill(void* dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(dst)), "l"(src), "r"(src_bytes)
+               : "memory");
+}
+
 // Arrive on `bar` once this thread's earlier cp.async copies have landed;
 // the arrival counts toward the barrier's expected count (.noinc).
 __device__ __forceinline__ void cp_async_mbar_arrive(uint64_t* bar) {

@@ -1,5 +1,7 @@
-// V:N:M SpMM on tcgen05 tensor cores: C = A * B with A sparse (the reordered
-// matrix) and B dense, BF16 or FP16 operands, FP32 accumulation.
+// V:N:M SpMM: C = A * B with A sparse (the reordered matrix) and B dense,
+// BF16 or FP16 operands, FP32 accumulation.  Dense V:N:M blocks run on the
+// tcgen05 tensor cores; the blocks too sparse to pay for a tensor-core tile
+// run on the CUDA cores.
 //
 // Replaces the reference's BSR WMMA kernel (kernel/spmm.cu:44-161), which
 // runs one warp per 16x16 output tile with wmma m16n16k16 over 16x16 BSR
@@ -9,25 +11,41 @@
 // Layout (the compressor below builds it on the device):
 //   - rows are cut into tiles of 128 (the MMA's M); V must divide 128, so a
 //     tile holds 128 / V block rows of V rows each.
-//   - every non-empty (block row, segment) block -- V rows x M columns -- is
-//     cut into slices: 4 of its columns, and per row at most 2 nonzeros
-//     among them (2:4 inside the slice).  A block that satisfies V:N:M (at
-//     most 4 nonzero columns, at most 2 nonzeros per row) is one slice;
-//     a block that does not spills into more slices, so no nonzero is
-//     dropped and the product is exact up to the operand rounding.
+//   - every non-empty (block row, segment) block -- V rows x M columns --
+//     with at least `dense_min` nonzeros is cut into slices: 4 of its
+//     columns, and per row at most 2 nonzeros among them (2:4 inside the
+//     slice).  A block that satisfies V:N:M (at most 4 nonzero columns, at
+//     most 2 nonzeros per row) is one slice; a block that does not spills
+//     into more slices, so no nonzero is dropped and the product is exact up
+//     to the operand rounding.
 //   - 4 slices make one K-step of 16: the A operand of a K-step (128 rows x
 //     16) is stored ready for the MMA (K-major, core matrices of 8 rows x 16
-//     bytes), and the 16 B rows it multiplies are listed by index.
+//     bytes), and the 16 B rows it multiplies are listed by index (-1 for a
+//     column that only pads a slice: its B row is zero-filled, not read).
 //   - values are stored divided by their block row's scale (max |a| of the
 //     V rows), and the epilogue multiplies each output row back by it.
-// Kernel: one CTA per (tile, column block of C).  A producer warp streams
-// each K-step's A tile (one bulk copy) and copies its 16 B rows with 16-byte
-// cp.async loads into the 128-byte swizzled layout (one warp instruction
-// per 512-byte row; the TMA's tile::gather4 issued too slowly here, one
-// K-step per ~2 us per CTA), with the row ids loaded eight K-steps ahead;
-// one thread issues the MMA per K-step; eight stages keep copies in flight
-// while the MMAs run.  Four warps then read the FP32
-// accumulator out of tensor memory, scale and store it.
+//   - the nonzeros of sparser blocks form the residual: a row-major CSR with
+//     FP32 values, cut into tasks of at most 256 nonzeros of one row (a row
+//     with more is split into up to 32 chunks whose partial rows are added
+//     in chunk order afterwards, so the sums do not depend on timing).
+// On graph sparsity most blocks hold one or two nonzeros; a 128 x 16
+// tensor-core tile for them would be >99 % padding, while a CUDA-core
+// gather reads one B row per nonzero.  `dense_min` (VNM_SPMM_DENSE_MIN in the
+// environment, else the default below) sets the split.
+//
+// Kernels of one product, in stream order:
+//   k_spmm_res  CUDA cores: every residual task (and every row of a tile with
+//               no tensor-core work) gathers its B rows with 16-byte loads and
+//               writes its C row (or a partial row);
+//   k_spmm_fin  adds the partial rows of the split rows, in chunk order;
+//   k_spmm_vnm  tensor cores, one CTA per (tile with K-steps, column block of
+//               C).  A producer warp streams each K-step's A tile (one bulk
+//               copy) and copies its 16 B rows with 16-byte cp.async loads
+//               into the 128-byte swizzled layout, with the row ids loaded
+//               eight K-steps ahead; one thread issues the MMA per K-step;
+//               eight stages keep copies in flight while the MMAs run.  Four
+//               warps then read the FP32 accumulator out of tensor memory,
+//               scale it and store it, or add it to what the residual wrote.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -44,13 +62,28 @@ struct vnm_spmm_matrix {
   int R = 0, M = 0, V = 0, dtype = 1;  // dtype: 1 bf16, 0 f16
   int ntiles = 0, nsteps = 0;
   long long nnz = 0, groups = 0, slices = 0, slices_padded = 0, valid_blocks = 0;
-  int* tile_step = nullptr;  // [ntiles + 1]
-  int* cols = nullptr;       // [nsteps * 16]
+  // tensor-core part
+  int ntt = 0;                 // tiles with at least one K-step
+  int* tile_step = nullptr;    // [ntiles + 1]
+  int2* tlist = nullptr;       // [ntt] {tile, 1 when the residual kernel wrote the tile's rows first}
+  int* cols = nullptr;         // [nsteps * 16], -1 = padding column
   unsigned char* a = nullptr;  // [nsteps * 4096]
-  float* rscale = nullptr;   // [ntiles * 128]
-  void* base = nullptr;      // one allocation for all of the above
-  size_t bytes = 0;          // its size
+  float* rscale = nullptr;     // [ntiles * 128]
+  // CUDA-core part
+  int dense_min = 0;           // blocks with fewer nonzeros went to the residual
+  long long nres = 0;          // residual nonzeros
+  int ntask = 0, nmulti = 0, nslots = 0;
+  int* rcol = nullptr;         // [nres], row-major
+  float* rval = nullptr;       // [nres]
+  int4* task = nullptr;        // [ntask] {row, begin, end, partial slot or -1}
+  int4* multi = nullptr;       // [nmulti] {row, first slot, chunks, 0}
+  void* base = nullptr;        // one allocation for all of the above
+  size_t bytes = 0;            // its size
   vnm_spmm_spare* spare = nullptr;  // the compressing context's spare storage
+  // state of the asynchronous entry point, allocated on its first call
+  float* part = nullptr;       // partial rows of split rows, for the largest n seen
+  size_t part_floats = 0;
+  int* err = nullptr;          // sticky failure flag of the tensor-core kernel
 };
 
 namespace vnm {
@@ -59,6 +92,18 @@ constexpr int SP_TM = 128;        // rows per tile (MMA M)
 constexpr int SP_KSTEP_BYTES = 4096;
 constexpr int SP_THREADS = 128;
 constexpr uint32_t SP_WAIT_LIMIT = 1u << 22;  // polls before a wait gives up
+constexpr int RES_CHUNK = 256;    // residual nonzeros per task, at most
+constexpr int RES_MAXCH = 32;     // chunks of one row, at most
+constexpr int RES_THREADS = 256;
+// A block runs on the tensor cores when it holds at least V nonzeros (one
+// a row on average), else on the CUDA cores.  Measured on GB300 with the
+// R-MAT 16384 (V=64, n=128) and Chung-Lu 262144 (V=128, n=256) operands,
+// thresholds 2..64 against all-residual: every tensor-core share was slower
+// (C2 0.037 ms all-residual vs 0.046-0.30 ms; C5 0.50 ms vs 0.67-4.9 ms):
+// at one or two nonzeros per block a tile is >99 % padding and its fixed
+// costs dominate.  A V:N:M operand whose blocks are full (2V nonzeros) goes
+// to the tensor cores.  VNM_SPMM_DENSE_MIN overrides the threshold (0 =
+// every block on the tensor cores).
 
 static inline int sp_grid(const vnm_ctx* ctx, long long n, int nt = 256) {
   long long g = (n + nt - 1) / nt, cap = (long long)ctx->num_sms * 16;
@@ -144,11 +189,16 @@ __device__ __forceinline__ unsigned low2(unsigned m) {  // the lowest two set bi
   return a | (rest & (0u - rest));
 }
 
-// Count slices per block and per tile.
-__global__ void k_cmp_count(const unsigned long long* skeys, const int* gstart, int ngroups, int nnz, int M, int V,
-                            int nseg, int* gsl, int* tile_raw, int* valid_blocks) {
+// Count slices per block and per tile.  A block with fewer than dense_min
+// nonzeros gets no slice: its entries are flagged for the residual (by
+// original position), counted per row and per tile.
+__global__ void k_cmp_count(const unsigned long long* skeys, const int* spos, const int* gstart, int ngroups, int nnz,
+                            int M, int V, int nseg, int dense_min, int* gsl, int* tile_raw, int* valid_blocks,
+                            int* resflag, int* rowlen, int* tile_res) {
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += gridDim.x * blockDim.x) {
     const int b0 = gstart[g], b1 = g + 1 < ngroups ? gstart[g + 1] : nnz;
+    const long long blk = (long long)(skeys[b0] / ((unsigned long long)V * M));
+    const int brow = (int)(blk / nseg);
     unsigned char mask[128];
     int nr = 0, lastr = -1;
     for (int i = b0; i < b1; ++i) {
@@ -167,20 +217,95 @@ __global__ void k_cmp_count(const unsigned long long* skeys, const int* gstart, 
       if (__popc(mask[r]) > 2) valid = 0;
     }
     if (__popc(orb) > 4) valid = 0;
+    if (valid) atomicAdd(valid_blocks, 1);
+    if (b1 - b0 < dense_min) {
+      for (int i = b0; i < b1; ++i) {
+        resflag[spos[i]] = 1;
+        atomicAdd(&rowlen[brow * V + (int)((skeys[i] / M) % V)], 1);
+      }
+      atomicAdd(&tile_res[(brow * V) / SP_TM], b1 - b0);
+      gsl[g] = 0;
+      continue;
+    }
     const int ns = block_slices(mask, nr, M, [&](const int*, int, unsigned chosen) {
       for (int r = 0; r < nr; ++r) mask[r] &= ~(unsigned char)low2(mask[r] & chosen);
     });
     gsl[g] = ns;
-    const long long blk = (long long)(skeys[b0] / ((unsigned long long)V * M));
-    const int brow = (int)(blk / nseg);
     atomicAdd(&tile_raw[(brow * V) / SP_TM], ns);
-    if (valid) atomicAdd(valid_blocks, 1);
   }
 }
 
-__global__ void k_cmp_pad(const int* tile_raw, int ntiles, int* tile_pad) {
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x)
+__global__ void k_cmp_pad(const int* tile_raw, int ntiles, int* tile_pad, int* tile_has) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x) {
     tile_pad[t] = (tile_raw[t] + 3) & ~3;
+    tile_has[t] = tile_raw[t] > 0 ? 1 : 0;
+  }
+}
+
+// The residual entries in their original order, keyed by row for the
+// stable sort that makes the CSR.
+__global__ void k_res_compact(const int* resflag, const int* rpos, const int* row, int nnz, unsigned long long* rkey,
+                              int* rsrc) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += gridDim.x * blockDim.x)
+    if (resflag[i]) {
+      rkey[rpos[i]] = (unsigned long long)(unsigned)row[i];
+      rsrc[rpos[i]] = i;
+    }
+}
+
+__global__ void k_res_gather(const int* src, const int* col, const float* val, int nres, int* rcol, float* rval) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nres; i += gridDim.x * blockDim.x) {
+    const int e = src[i];
+    rcol[i] = col[e];
+    rval[i] = val[e];
+  }
+}
+
+// Residual tasks of a row: none when its tile runs on the tensor cores and
+// holds no residual entry (the tensor kernel then writes the rows), else one
+// per chunk of at most RES_CHUNK entries (one task for an empty row, which
+// writes zeros), at most RES_MAXCH chunks.
+__device__ __forceinline__ int res_chunks(int len, bool needed) {
+  if (!needed) return 0;
+  if (len <= RES_CHUNK) return 1;
+  const int c = (len + RES_CHUNK - 1) / RES_CHUNK;
+  return c < RES_MAXCH ? c : RES_MAXCH;
+}
+
+__global__ void k_res_task_count(const int* rptr, int R, const int* tile_has, const int* tile_res, int* nmt, int* nst,
+                                 int* nmr) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < R; r += gridDim.x * blockDim.x) {
+    const int t = r / SP_TM;
+    const int nch = res_chunks(rptr[r + 1] - rptr[r], !(tile_has[t] && tile_res[t] == 0));
+    nmt[r] = nch > 1 ? nch : 0;
+    nst[r] = nch == 1 ? 1 : 0;
+    nmr[r] = nch > 1 ? 1 : 0;
+  }
+}
+
+// Split rows' chunks first (they are the longest tasks), then the others.
+__global__ void k_res_task_fill(const int* rptr, int R, const int* tile_has, const int* tile_res, const int* mt_off,
+                                const int* st_off, const int* mr_off, int nmt_total, int4* task, int4* multi) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < R; r += gridDim.x * blockDim.x) {
+    const int t = r / SP_TM;
+    const int b = rptr[r], e = rptr[r + 1];
+    const int nch = res_chunks(e - b, !(tile_has[t] && tile_res[t] == 0));
+    if (nch == 1) {
+      task[nmt_total + st_off[r]] = make_int4(r, b, e, -1);
+    } else if (nch > 1) {
+      const int base = mt_off[r], csz = (e - b + nch - 1) / nch;
+      for (int j = 0; j < nch; ++j) {
+        const int cb = min(b + j * csz, e), ce = min(cb + csz, e);
+        task[base + j] = make_int4(r, cb, ce, base + j);
+      }
+      multi[mr_off[r]] = make_int4(r, base, nch, 0);
+    }
+  }
+}
+
+__global__ void k_tile_list(const int* tile_has, const int* tile_res, int ntiles, const int* tl_off, int2* tlist) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x)
+    if (tile_has[t]) tlist[tl_off[t]] = make_int2(t, tile_res[t] > 0 ? 1 : 0);
 }
 
 template <class T>
@@ -197,10 +322,12 @@ __device__ __forceinline__ __half to_t<__half>(float x) {
 // Write every block's slices: B-row indices and A values in MMA layout.
 template <class T>
 __global__ void k_cmp_fill(const unsigned long long* skeys, const int* spos, const float* val, const int* gstart,
-                           int ngroups, int nnz, int M, int V, int nseg, const int* gofs, const int* tile_base,
-                           const int* tile_rawbase, const unsigned* bmax, int* cols, unsigned char* a) {
+                           int ngroups, int nnz, int M, int V, int nseg, int dense_min, const int* gofs,
+                           const int* tile_base, const int* tile_rawbase, const unsigned* bmax, int* cols,
+                           unsigned char* a) {
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += gridDim.x * blockDim.x) {
     const int b0 = gstart[g], b1 = g + 1 < ngroups ? gstart[g + 1] : nnz;
+    if (b1 - b0 < dense_min) continue;  // a residual block
     const long long blk = (long long)(skeys[b0] / ((unsigned long long)V * M));
     const int brow = (int)(blk / nseg), seg = (int)(blk % nseg);
     const int t = (brow * V) / SP_TM;
@@ -225,7 +352,7 @@ __global__ void k_cmp_fill(const unsigned long long* skeys, const int* spos, con
     int si = tile_base[t] + (gofs[g] - tile_rawbase[t]);  // this block's first slice
     block_slices(mask, nr, M, [&](const int* sel, int nsel, unsigned chosen) {
       const int ks = si >> 2, j = si & 3;
-      for (int q = 0; q < 4; ++q) cols[ks * 16 + 4 * j + q] = seg * M + sel[q < nsel ? q : 0];
+      for (int q = 0; q < 4; ++q) cols[ks * 16 + 4 * j + q] = q < nsel ? seg * M + sel[q] : -1;
       unsigned char* tile = a + (size_t)ks * SP_KSTEP_BYTES;
       for (int r = 0; r < nr; ++r) {
         const unsigned take = low2(mask[r] & chosen);
@@ -259,9 +386,99 @@ __global__ void k_cmp_rscale(const unsigned* bmax, int ntiles, int R, int V, flo
 }
 
 // ---------------------------------------------------------------------------
-// SpMM kernel
+// Residual kernels (CUDA cores)
+// ---------------------------------------------------------------------------
+// acc[0..7] += w * the 8 16-bit values in b (element 0 in the low half of b.x)
+template <bool BF16>
+__device__ __forceinline__ void fma8(float (&acc)[8], uint4 b, float w) {
+  const uint32_t q[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    float lo, hi;
+    if (BF16) {
+      lo = __uint_as_float(q[i] << 16);
+      hi = __uint_as_float(q[i] & 0xffff0000u);
+    } else {
+      const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&q[i]));
+      lo = f.x;
+      hi = f.y;
+    }
+    acc[2 * i] = fmaf(w, lo, acc[2 * i]);
+    acc[2 * i + 1] = fmaf(w, hi, acc[2 * i + 1]);
+  }
+}
+
+// One task per group of LW lanes (32 / LW tasks per warp); each lane owns 8
+// consecutive columns of the block's 8 * LW.  The group's lanes load LW
+// (column, value) pairs at a time and broadcast them by shuffle; every lane
+// then gathers its 16 bytes of each B row, four rows in flight.  Loop trip
+// counts are the warp's maximum, so every shuffle has the whole warp.
+template <int LW, bool BF16>
+__global__ void __launch_bounds__(RES_THREADS)
+    k_spmm_res(const int4* __restrict__ task, int ntask, const int* __restrict__ rcol, const float* __restrict__ rval,
+               const unsigned char* __restrict__ B, size_t ldb, float* __restrict__ C, int ldc,
+               float* __restrict__ P, int ldp) {
+  constexpr int G = 32 / LW;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, grp = lane / LW, lid = lane % LW;
+  const int t = (blockIdx.x * (RES_THREADS / 32) + warp) * G + grp;
+  const int cb = blockIdx.y * (8 * LW) + lid * 8;  // this lane's first column
+  const int4 tk = t < ntask ? task[t] : make_int4(0, 0, 0, -1);
+  const int len = tk.z - tk.y;
+  const int maxlen = __reduce_max_sync(0xffffffffu, len);
+  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  const unsigned char* bcol = B + (size_t)cb * 2;
+  for (int k0 = 0; k0 < maxlen; k0 += LW) {
+    const bool ok = k0 + lid < len;
+    const int mc = ok ? __ldg(rcol + tk.y + k0 + lid) : 0;
+    const float mv = ok ? __ldg(rval + tk.y + k0 + lid) : 0.f;
+    const int left = len - k0;  // this group's entries from k0 on (may be <= 0)
+    const int qmax = min(LW, maxlen - k0);
+    for (int q = 0; q < qmax; q += 4) {
+      int c[4];
+      float w[4];
+      uint4 b[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        c[u] = __shfl_sync(0xffffffffu, mc, q + u, LW);
+        w[u] = __shfl_sync(0xffffffffu, mv, q + u, LW);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        b[u] = q + u < left ? __ldg(reinterpret_cast<const uint4*>(bcol + (size_t)c[u] * ldb)) : make_uint4(0, 0, 0, 0);
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (q + u < left) fma8<BF16>(acc, b[u], w[u]);
+    }
+  }
+  if (t < ntask) {
+    float* dst = tk.w < 0 ? C + (size_t)tk.x * ldc + cb : P + (size_t)tk.w * ldp + cb;
+    reinterpret_cast<float4*>(dst)[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+    reinterpret_cast<float4*>(dst)[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
+  }
+}
+
+// C row of a split row = its partial rows added in chunk order.
+__global__ void k_spmm_fin(const int4* __restrict__ multi, const float* __restrict__ P, int ldp, float* C, int ldc,
+                           int n) {
+  const int4 m = multi[blockIdx.x];
+  for (int q = threadIdx.x; q < n / 4; q += blockDim.x) {
+    float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int j = 0; j < m.z; ++j) {
+      const float4 x = reinterpret_cast<const float4*>(P + (size_t)(m.y + j) * ldp)[q];
+      s.x += x.x;
+      s.y += x.y;
+      s.z += x.z;
+      s.w += x.w;
+    }
+    reinterpret_cast<float4*>(C + (size_t)m.x * ldc)[q] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Tensor-core kernel
 // ---------------------------------------------------------------------------
 struct SpmmArgs {
+  const int2* tlist;
   const int* tile_step;
   const int* cols;
   const unsigned char* a;
@@ -296,7 +513,9 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
   SpmmSmem<NT>& sm = *reinterpret_cast<SpmmSmem<NT>*>(
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(sp_raw) + 1023) & ~uintptr_t(1023)));
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int t = blockIdx.x;
+  const int2 tl = p.tlist[blockIdx.x];
+  const int t = tl.x;
+  const bool add = tl.y != 0;  // the residual kernel wrote these rows first
   const int n0 = blockIdx.y * NT;
   const int s0 = p.tile_step[t], nsteps = p.tile_step[t + 1] - s0;
 
@@ -371,9 +590,10 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             for (int kr0 = 0; kr0 < 16; kr0 += RPI) {
               const int kr = kr0 + sub;
               const int row = __shfl_sync(0xffffffffu, cur, d * 16 + kr);
-              const unsigned char* src = p.B + (size_t)row * p.ldb + (size_t)(n0 + 8 * c) * 2;
+              // a padding column (-1): its A column is zero; fill zeros, read nothing
+              const unsigned char* src = p.B + (size_t)(row < 0 ? 0 : row) * p.ldb + (size_t)(n0 + 8 * c) * 2;
               unsigned char* dst = bs + (c >> 3) * 2048 + (kr >> 3) * 1024 + (kr & 7) * 128 + (((c & 7) ^ (kr & 7)) << 4);
-              ptx::cp_async16(dst, src);
+              ptx::cp_async16_zfill(dst, src, row < 0 ? 0u : 16u);
             }
             ptx::cp_async_mbar_arrive(&sm.full[s]);
           }
@@ -423,18 +643,21 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
         if (row < p.R) {
           float4* dst = reinterpret_cast<float4*>(p.C + (size_t)row * p.ldc + n0 + c0);
 #pragma unroll
-          for (int q = 0; q < 8; ++q)
-            dst[q] = make_float4(__uint_as_float(v[4 * q]) * sc, __uint_as_float(v[4 * q + 1]) * sc,
-                                 __uint_as_float(v[4 * q + 2]) * sc, __uint_as_float(v[4 * q + 3]) * sc);
+          for (int q = 0; q < 8; ++q) {
+            float4 o = make_float4(__uint_as_float(v[4 * q]) * sc, __uint_as_float(v[4 * q + 1]) * sc,
+                                   __uint_as_float(v[4 * q + 2]) * sc, __uint_as_float(v[4 * q + 3]) * sc);
+            if (add) {
+              const float4 r = dst[q];
+              o.x += r.x;
+              o.y += r.y;
+              o.z += r.z;
+              o.w += r.w;
+            }
+            dst[q] = o;
+          }
         }
       }
     }
-  } else {
-    // an empty tile: C rows are zero
-    const int row = t * SP_TM + warp * 32 + lane;
-    if (row < p.R)
-      for (int c = 0; c < NT; c += 4)
-        *reinterpret_cast<float4*>(p.C + (size_t)row * p.ldc + n0 + c) = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   ptx::tc_fence_before();
   __syncthreads();
@@ -444,31 +667,75 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
 // ---------------------------------------------------------------------------
 // Host
 // ---------------------------------------------------------------------------
+static int spmm_dense_min(int V) {
+  if (const char* e = getenv("VNM_SPMM_DENSE_MIN")) {
+    const int v = atoi(e);
+    if (v >= 0) return v;
+  }
+  return V;
+}
+
+// Arena bytes compress_t takes for nnz entries and R rows.
+static size_t compress_scratch_bytes(int R, int nnz) {
+  const int ntiles = (R + SP_TM - 1) / SP_TM;
+  const size_t n = nnz > 0 ? (size_t)nnz : 1;
+  size_t b = arena_bytes(n, 8) + 6 * arena_bytes(n, 4);          // keys, flag, gstart, gsl, gofs, resflag, rpos
+  b += arena_bytes(n, 8) + arena_bytes(n, 4);                    // residual keys and sources
+  b += 2 * radix_sort_scratch_bytes(nnz);
+  b += 7 * arena_bytes(ntiles + 1, 4);                           // tile_raw/pad/has/base/rawbase/res, tl_off
+  b += 5 * arena_bytes((size_t)R + 1, 4);                        // rowlen, rptr, nmt, nst, nmr
+  b += 3 * arena_bytes((size_t)R + 1, 4);                        // their scans
+  b += arena_bytes((size_t)R + 2, 4);                            // bmax (R / V + 1 entries at most)
+  b += 8 * scan_scratch_bytes((nnz > R ? nnz : R) + 1) + 16384;
+  return b;
+}
+
 template <class T>
 static vnm_status compress_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, const int* d_col, const float* d_val,
                              int M, int V, vnm_spmm_matrix* out) {
   const int nseg = (R + M - 1) / M;
   const int nbrow = (R + V - 1) / V;
   const int ntiles = (R + SP_TM - 1) / SP_TM;
+  const int dense_min = spmm_dense_min(V);
   int* h = ctx->h_pinned;
-  unsigned long long* keys = arena_take<unsigned long long>(ctx, nnz > 0 ? nnz : 1);
-  int* flag = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
-  int* gstart = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
-  int* gsl = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
-  int* gofs = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
+  const size_t n1 = nnz > 0 ? (size_t)nnz : 1;
+  unsigned long long* keys = arena_take<unsigned long long>(ctx, n1);
+  int* flag = arena_take<int>(ctx, n1);
+  int* gstart = arena_take<int>(ctx, n1);
+  int* gsl = arena_take<int>(ctx, n1);
+  int* gofs = arena_take<int>(ctx, n1);
+  int* resflag = arena_take<int>(ctx, n1);
+  int* rpos = arena_take<int>(ctx, n1);
   int* tile_raw = arena_take<int>(ctx, ntiles + 1);
   int* tile_pad = arena_take<int>(ctx, ntiles + 1);
+  int* tile_has = arena_take<int>(ctx, ntiles + 1);
+  int* tile_res = arena_take<int>(ctx, ntiles + 1);
   int* tile_base = arena_take<int>(ctx, ntiles + 1);
   int* tile_rawbase = arena_take<int>(ctx, ntiles + 1);
+  int* tl_off = arena_take<int>(ctx, ntiles + 1);
+  int* rowlen = arena_take<int>(ctx, (size_t)R + 1);
+  int* rptr = arena_take<int>(ctx, (size_t)R + 1);
+  int* nmt = arena_take<int>(ctx, (size_t)R + 1);
+  int* nst = arena_take<int>(ctx, (size_t)R + 1);
+  int* nmr = arena_take<int>(ctx, (size_t)R + 1);
+  int* mt_off = arena_take<int>(ctx, (size_t)R + 1);
+  int* st_off = arena_take<int>(ctx, (size_t)R + 1);
+  int* mr_off = arena_take<int>(ctx, (size_t)R + 1);
   unsigned* bmax = arena_take<unsigned>(ctx, nbrow + 1);
-  int* counters = arena_take<int>(ctx, 4);
-  if (!keys || !flag || !gstart || !gsl || !gofs || !tile_raw || !tile_pad || !tile_base || !tile_rawbase ||
-      !bmax || !counters)
+  int* counters = arena_take<int>(ctx, 16);
+  if (!keys || !flag || !gstart || !gsl || !gofs || !resflag || !rpos || !tile_raw || !tile_pad || !tile_has ||
+      !tile_res || !tile_base || !tile_rawbase || !tl_off || !rowlen || !rptr || !nmt || !nst || !nmr || !mt_off ||
+      !st_off || !mr_off || !bmax || !counters)
     return VNM_ERR_NOMEM;
-  VNM_CUDA_TRY(cudaMemsetAsync(tile_raw, 0, sizeof(int) * (ntiles + 1), ctx->stream));
-  VNM_CUDA_TRY(cudaMemsetAsync(tile_pad, 0, sizeof(int) * (ntiles + 1), ctx->stream));
-  VNM_CUDA_TRY(cudaMemsetAsync(bmax, 0, sizeof(unsigned) * (nbrow + 1), ctx->stream));
-  VNM_CUDA_TRY(cudaMemsetAsync(counters, 0, sizeof(int) * 4, ctx->stream));
+  cudaStream_t st = ctx->stream;
+  VNM_CUDA_TRY(cudaMemsetAsync(tile_raw, 0, sizeof(int) * (ntiles + 1), st));
+  VNM_CUDA_TRY(cudaMemsetAsync(tile_pad, 0, sizeof(int) * (ntiles + 1), st));
+  VNM_CUDA_TRY(cudaMemsetAsync(tile_has, 0, sizeof(int) * (ntiles + 1), st));
+  VNM_CUDA_TRY(cudaMemsetAsync(tile_res, 0, sizeof(int) * (ntiles + 1), st));
+  VNM_CUDA_TRY(cudaMemsetAsync(rowlen, 0, sizeof(int) * ((size_t)R + 1), st));
+  VNM_CUDA_TRY(cudaMemsetAsync(resflag, 0, sizeof(int) * n1, st));
+  VNM_CUDA_TRY(cudaMemsetAsync(bmax, 0, sizeof(unsigned) * (nbrow + 1), st));
+  VNM_CUDA_TRY(cudaMemsetAsync(counters, 0, sizeof(int) * 16, st));
   int ngroups = 0;
   unsigned long long* skeys = keys;
   int* spos = nullptr;
@@ -480,33 +747,50 @@ static vnm_status compress_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, con
     VNM_TRY(exclusive_scan(ctx, flag, flag, nnz, counters));
     VNM_LAUNCH(ctx, k_cmp_group_start, sp_grid(ctx, nnz), 256, 0, flag, skeys, nnz, V * M, gstart);
     VNM_LAUNCH(ctx, k_cmp_scale, sp_grid(ctx, nnz), 256, 0, d_row, d_val, nnz, V, bmax);
-    VNM_CUDA_TRY(cudaMemcpyAsync(h, counters, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    VNM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    VNM_CUDA_TRY(cudaMemcpyAsync(h, counters, sizeof(int), cudaMemcpyDeviceToHost, st));
+    VNM_CUDA_TRY(cudaStreamSynchronize(st));
     ngroups = h[0];
   }
   if (ngroups > 0) {
-    VNM_LAUNCH(ctx, k_cmp_count, sp_grid(ctx, ngroups, 128), 128, 0, skeys, gstart, ngroups, nnz, M, V, nseg, gsl,
-               tile_raw, counters + 1);
+    VNM_LAUNCH(ctx, k_cmp_count, sp_grid(ctx, ngroups, 128), 128, 0, skeys, spos, gstart, ngroups, nnz, M, V, nseg,
+               dense_min, gsl, tile_raw, counters + 1, resflag, rowlen, tile_res);
     VNM_TRY(exclusive_scan(ctx, gsl, gofs, ngroups, counters + 2));
   }
-  VNM_LAUNCH(ctx, k_cmp_pad, sp_grid(ctx, ntiles), 256, 0, tile_raw, ntiles, tile_pad);
+  VNM_LAUNCH(ctx, k_cmp_pad, sp_grid(ctx, ntiles), 256, 0, tile_raw, ntiles, tile_pad, tile_has);
   VNM_TRY(exclusive_scan(ctx, tile_pad, tile_base, ntiles + 1, nullptr));
   VNM_TRY(exclusive_scan(ctx, tile_raw, tile_rawbase, ntiles + 1, nullptr));
-  VNM_CUDA_TRY(cudaMemcpyAsync(h, tile_base + ntiles, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  VNM_CUDA_TRY(cudaMemcpyAsync(h + 1, counters + 1, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  VNM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  VNM_TRY(exclusive_scan(ctx, tile_has, tl_off, ntiles, counters + 3));
+  VNM_TRY(exclusive_scan(ctx, resflag, rpos, nnz, counters + 4));
+  VNM_TRY(exclusive_scan(ctx, rowlen, rptr, R + 1, nullptr));
+  VNM_LAUNCH(ctx, k_res_task_count, sp_grid(ctx, R), 256, 0, rptr, R, tile_has, tile_res, nmt, nst, nmr);
+  VNM_TRY(exclusive_scan(ctx, nmt, mt_off, R, counters + 5));
+  VNM_TRY(exclusive_scan(ctx, nst, st_off, R, counters + 6));
+  VNM_TRY(exclusive_scan(ctx, nmr, mr_off, R, counters + 7));
+  VNM_CUDA_TRY(cudaMemcpyAsync(h, tile_base + ntiles, sizeof(int), cudaMemcpyDeviceToHost, st));
+  VNM_CUDA_TRY(cudaMemcpyAsync(h + 1, counters + 1, 7 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  VNM_CUDA_TRY(cudaStreamSynchronize(st));
   const int padded = h[0];
   out->valid_blocks = h[1];
   out->slices = ngroups > 0 ? h[2] : 0;
+  out->ntt = h[3];
+  out->nres = h[4];
+  const int nmt_total = h[5], nst_total = h[6];
+  out->nslots = nmt_total;
+  out->ntask = nmt_total + nst_total;
+  out->nmulti = h[7];
+  out->dense_min = dense_min;
   out->slices_padded = padded;
   out->groups = ngroups;
   out->nsteps = padded / 4;
   out->ntiles = ntiles;
   // the matrix's own storage (kept across calls)
-  const size_t b_step = arena_bytes(ntiles + 1, 4), b_cols = arena_bytes((size_t)out->nsteps * 16 + 1, 4),
+  const size_t b_step = arena_bytes(ntiles + 1, 4), b_tl = arena_bytes((size_t)out->ntt + 1, 8),
+               b_cols = arena_bytes((size_t)out->nsteps * 16 + 1, 4),
                b_a = arena_bytes((size_t)out->nsteps * SP_KSTEP_BYTES + 16, 1),
-               b_sc = arena_bytes((size_t)ntiles * SP_TM, 4);
-  const size_t need = b_step + b_cols + b_a + b_sc;
+               b_sc = arena_bytes((size_t)ntiles * SP_TM, 4), b_rc = arena_bytes((size_t)out->nres + 1, 4),
+               b_rv = arena_bytes((size_t)out->nres + 1, 4), b_tk = arena_bytes((size_t)out->ntask + 1, 16),
+               b_mu = arena_bytes((size_t)out->nmulti + 1, 16);
+  const size_t need = b_step + b_tl + b_cols + b_a + b_sc + b_rc + b_rv + b_tk + b_mu;
   void* base = nullptr;
   size_t have = 0;
   if (ctx->spare) {  // a freed operand's storage, when large enough
@@ -525,15 +809,47 @@ static vnm_status compress_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, con
   out->base = base;
   out->bytes = have;
   char* pb = static_cast<char*>(base);
-  out->tile_step = reinterpret_cast<int*>(pb);
-  out->cols = reinterpret_cast<int*>(pb + b_step);
-  out->a = reinterpret_cast<unsigned char*>(pb + b_step + b_cols);
-  out->rscale = reinterpret_cast<float*>(pb + b_step + b_cols + b_a);
-  VNM_CUDA_TRY(cudaMemsetAsync(out->cols, 0, b_cols, ctx->stream));
-  VNM_CUDA_TRY(cudaMemsetAsync(out->a, 0, b_a, ctx->stream));
-  if (ngroups > 0)
+  size_t o = 0;
+  out->tile_step = reinterpret_cast<int*>(pb + o);
+  o += b_step;
+  out->tlist = reinterpret_cast<int2*>(pb + o);
+  o += b_tl;
+  out->cols = reinterpret_cast<int*>(pb + o);
+  o += b_cols;
+  out->a = reinterpret_cast<unsigned char*>(pb + o);
+  o += b_a;
+  out->rscale = reinterpret_cast<float*>(pb + o);
+  o += b_sc;
+  out->rcol = reinterpret_cast<int*>(pb + o);
+  o += b_rc;
+  out->rval = reinterpret_cast<float*>(pb + o);
+  o += b_rv;
+  out->task = reinterpret_cast<int4*>(pb + o);
+  o += b_tk;
+  out->multi = reinterpret_cast<int4*>(pb + o);
+  // residual CSR: the residual entries in their original order, stably
+  // sorted by row
+  if (out->nres > 0) {
+    unsigned long long* rkey = arena_take<unsigned long long>(ctx, (size_t)out->nres);
+    int* rsrc = arena_take<int>(ctx, (size_t)out->nres);
+    if (!rkey || !rsrc) return VNM_ERR_NOMEM;
+    VNM_LAUNCH(ctx, k_res_compact, sp_grid(ctx, nnz), 256, 0, resflag, rpos, d_row, nnz, rkey, rsrc);
+    unsigned long long* sk = nullptr;
+    int* ss = nullptr;
+    VNM_TRY(radix_sort_u64(ctx, rkey, rsrc, (int)out->nres, sp_bits(R), &sk, &ss));
+    VNM_LAUNCH(ctx, k_res_gather, sp_grid(ctx, out->nres), 256, 0, ss, d_col, d_val, (int)out->nres, out->rcol,
+               out->rval);
+  }
+  if (out->ntask > 0)
+    VNM_LAUNCH(ctx, k_res_task_fill, sp_grid(ctx, R), 256, 0, rptr, R, tile_has, tile_res, mt_off, st_off, mr_off,
+               nmt_total, out->task, out->multi);
+  if (out->ntt > 0)
+    VNM_LAUNCH(ctx, k_tile_list, sp_grid(ctx, ntiles), 256, 0, tile_has, tile_res, ntiles, tl_off, out->tlist);
+  VNM_CUDA_TRY(cudaMemsetAsync(out->cols, 0xff, b_cols, st));  // -1: padding columns
+  VNM_CUDA_TRY(cudaMemsetAsync(out->a, 0, b_a, st));
+  if (ngroups > 0 && out->nsteps > 0)
     VNM_LAUNCH(ctx, k_cmp_fill<T>, sp_grid(ctx, ngroups, 128), 128, 0, skeys, spos, d_val, gstart, ngroups, nnz, M,
-               V, nseg, gofs, tile_base, tile_rawbase, bmax, out->cols, out->a);
+               V, nseg, dense_min, gofs, tile_base, tile_rawbase, bmax, out->cols, out->a);
   VNM_LAUNCH(ctx, k_cmp_rscale, sp_grid(ctx, (long long)ntiles * SP_TM), 256, 0, bmax, ntiles, R, V, out->rscale,
              tile_base, out->tile_step);
   return VNM_OK;
@@ -549,7 +865,7 @@ static vnm_status launch_spmm(vnm_ctx* ctx, const vnm_spmm_matrix* A, SpmmArgs& 
   if (smem < floor_bytes) smem = floor_bytes;
   VNM_CUDA_TRY(cudaFuncSetAttribute(k_spmm_vnm<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   p.idesc = ptx::idesc_f16(A->dtype == 1 ? 1u : 0u, 0u, 1u, SP_TM, NT);
-  dim3 grid(A->ntiles, p.n / NT);
+  dim3 grid(A->ntt, p.n / NT);
   VNM_LAUNCH(ctx, k_spmm_vnm<NT>, grid, SP_THREADS, smem, p);
   return VNM_OK;
 }
@@ -567,10 +883,7 @@ vnm_status vnm_spmm_compress(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
   if (mem != VNM_MEM_HOST && mem != VNM_MEM_DEVICE) return VNM_ERR_ARG;
   if (nnz > 0 && (!row || !col || !val)) return VNM_ERR_ARG;
   *out = nullptr;
-  const int ntiles = (nrows + SP_TM - 1) / SP_TM;
-  size_t need = 3 * arena_bytes(nnz, 4) + 8 * arena_bytes(nnz, 8) + 6 * arena_bytes(nnz, 4) +
-                4 * arena_bytes(ntiles + 1, 4) + arena_bytes(nrows / V + 2, 4) + radix_sort_scratch_bytes(nnz) +
-                4 * scan_scratch_bytes(nnz > ntiles ? nnz + 1 : ntiles + 1) + 8192;
+  const size_t need = 3 * arena_bytes(nnz, 4) + compress_scratch_bytes(nrows, nnz);
   VNM_TRY(arena_reserve(ctx, need));
   VNM_TRY(pinned_reserve(ctx, 64));
   VNM_TRY(begin_call(ctx));
@@ -605,15 +918,18 @@ vnm_status vnm_spmm_compress(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
 
 vnm_status vnm_spmm_info(const vnm_spmm_matrix* A, long long* info, int n) {
   if (!A || !info) return VNM_ERR_ARG;
-  const long long v[8] = {A->nnz, A->groups, A->valid_blocks, A->slices, A->slices_padded, A->nsteps, A->ntiles,
-                          (long long)A->nsteps * SP_KSTEP_BYTES};
-  for (int i = 0; i < n && i < 8; ++i) info[i] = v[i];
+  const long long v[13] = {A->nnz, A->groups, A->valid_blocks, A->slices, A->slices_padded, A->nsteps, A->ntiles,
+                           (long long)A->nsteps * SP_KSTEP_BYTES, A->nres, A->ntask, A->ntt, A->dense_min,
+                           A->nslots};
+  for (int i = 0; i < n && i < 13; ++i) info[i] = v[i];
   return VNM_OK;
 }
 
 vnm_status vnm_spmm_free(vnm_spmm_matrix* A) {
   if (!A) return VNM_ERR_ARG;
   cudaSetDevice(A->device);
+  if (A->part) cudaFree(A->part);
+  if (A->err) cudaFree(A->err);
   bool last = false;
   if (A->spare) {
     // keep the storage for the context's next compression (the larger of
@@ -633,29 +949,14 @@ vnm_status vnm_spmm_free(vnm_spmm_matrix* A) {
   return VNM_OK;
 }
 
-vnm_status vnm_spmm_run(vnm_ctx* ctx, const vnm_spmm_matrix* A, const void* B, int n, float* C, int mem) {
-  if (!ctx || !A || !B || !C || n <= 0 || (n % 64) != 0) return VNM_ERR_ARG;
-  if (mem != VNM_MEM_HOST && mem != VNM_MEM_DEVICE) return VNM_ERR_ARG;
-  if (A->device != ctx->device) return VNM_ERR_ARG;
-  const size_t bbytes = (size_t)A->R * n * 2, cbytes = (size_t)A->R * n * sizeof(float);
-  VNM_TRY(arena_reserve(ctx, (mem == VNM_MEM_HOST ? bbytes + cbytes : 0) + 4096));
-  VNM_TRY(pinned_reserve(ctx, 64));
-  VNM_TRY(begin_call(ctx));
-  const void* dB = B;
-  float* dC = C;
-  if (mem == VNM_MEM_HOST) {
-    void* tb = arena_take<unsigned char>(ctx, bbytes);
-    dC = arena_take<float>(ctx, (size_t)A->R * n);
-    if (!tb || !dC) return VNM_ERR_NOMEM;
-    VNM_CUDA_TRY(cudaMemcpyAsync(tb, B, bbytes, cudaMemcpyHostToDevice, ctx->stream));
-    dB = tb;
-  }
-  if ((reinterpret_cast<uintptr_t>(dB) & 15) != 0 || (reinterpret_cast<uintptr_t>(dC) & 15) != 0)
-    return VNM_ERR_ARG;
-  int* err = arena_take<int>(ctx, 1);
-  if (!err) return VNM_ERR_NOMEM;
-  VNM_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+// Enqueue one product on ctx->stream: the residual kernels, then the tensor
+// kernel at the column-block width the context measured fastest for this
+// operand shape and n (timed here, which synchronises the stream, on the
+// first call for a shape).  dB, dC, P and err are device memory.
+static vnm_status spmm_enqueue(vnm_ctx* ctx, const vnm_spmm_matrix* A, const void* dB, int n, float* dC, float* P,
+                               int* err, bool timed) {
   SpmmArgs p;
+  p.tlist = A->tlist;
   p.tile_step = A->tile_step;
   p.cols = A->cols;
   p.a = A->a;
@@ -667,9 +968,32 @@ vnm_status vnm_spmm_run(vnm_ctx* ctx, const vnm_spmm_matrix* A, const void* B, i
   p.n = n;
   p.ldc = n;
   p.err = err;
-  // column-block width: the one the context measured fastest for an
-  // operand of this shape and this n (all widths compute the same
-  // products; the first call for a shape times each width once)
+  // the CUDA-core part: lanes per task so that 8 columns a lane tile n
+  auto launch_res = [&]() -> vnm_status {
+    if (A->ntask > 0) {
+      const int lw = (n % 256) == 0 ? 32 : (n % 128) == 0 ? 16 : 8;
+      const int per_block = (RES_THREADS / 32) * (32 / lw);
+      dim3 grid((unsigned)((A->ntask + per_block - 1) / per_block), (unsigned)(n / (8 * lw)));
+#define VNM_RES(LWV, BFV)                                                                                   \
+  VNM_LAUNCH(ctx, (k_spmm_res<LWV, BFV>), grid, RES_THREADS, 0, A->task, A->ntask, A->rcol, A->rval, p.B, p.ldb, dC, \
+             n, P, n)
+      if (A->dtype == 1) {
+        if (lw == 32) VNM_RES(32, true);
+        else if (lw == 16) VNM_RES(16, true);
+        else VNM_RES(8, true);
+      } else {
+        if (lw == 32) VNM_RES(32, false);
+        else if (lw == 16) VNM_RES(16, false);
+        else VNM_RES(8, false);
+      }
+#undef VNM_RES
+    }
+    if (A->nmulti > 0) {
+      const int nt = n / 4 < 256 ? ((n / 4 + 31) / 32) * 32 : 256;
+      VNM_LAUNCH(ctx, k_spmm_fin, A->nmulti, nt, 0, A->multi, P, n, dC, n, n);
+    }
+    return VNM_OK;
+  };
   const long long key[3] = {A->R, A->nsteps, n};
   int nt = 0;
   if (const char* e = getenv("VNM_SPMM_WIDTH")) {  // a fixed width (64, 128 or 256) that divides n
@@ -681,11 +1005,16 @@ vnm_status vnm_spmm_run(vnm_ctx* ctx, const vnm_spmm_matrix* A, const void* B, i
         ctx->spmm_tune_key[q][2] == key[2])
       nt = ctx->spmm_tune_nt[q];
   auto launch_nt = [&](int w) -> vnm_status {
+    if (A->ntt == 0) return VNM_OK;
     if (w == 256) return launch_spmm<256>(ctx, A, p);
     if (w == 128) return launch_spmm<128>(ctx, A, p);
     return launch_spmm<64>(ctx, A, p);
   };
+  if (nt == 0 && A->ntt == 0) nt = 64;  // no tensor-core work: nothing to tune
   if (nt == 0) {
+    // the tensor kernel adds into rows the residual kernel wrote: time each
+    // width on that state (the final launches below write C afresh)
+    VNM_TRY(launch_res());
     const int cand[3] = {256, 128, 64};
     float best = 0.f;
     for (int w : cand) {
@@ -706,15 +1035,84 @@ vnm_status vnm_spmm_run(vnm_ctx* ctx, const vnm_spmm_matrix* A, const void* B, i
     for (int k = 0; k < 3; ++k) ctx->spmm_tune_key[slot][k] = key[k];
     ctx->spmm_tune_nt[slot] = nt;
   }
-  VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main0, ctx->stream));
+  if (timed) VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main0, ctx->stream));
+  VNM_TRY(launch_res());
   VNM_TRY(launch_nt(nt));
-  VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main1, ctx->stream));
+  if (timed) VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main1, ctx->stream));
+  return VNM_OK;
+}
+
+vnm_status vnm_spmm_run(vnm_ctx* ctx, const vnm_spmm_matrix* A, const void* B, int n, float* C, int mem) {
+  if (!ctx || !A || !B || !C || n <= 0 || (n % 64) != 0) return VNM_ERR_ARG;
+  if (mem != VNM_MEM_HOST && mem != VNM_MEM_DEVICE) return VNM_ERR_ARG;
+  if (A->device != ctx->device) return VNM_ERR_ARG;
+  const size_t bbytes = (size_t)A->R * n * 2, cbytes = (size_t)A->R * n * sizeof(float);
+  const size_t pbytes = arena_bytes((size_t)A->nslots * n + 1, sizeof(float));
+  VNM_TRY(arena_reserve(ctx, (mem == VNM_MEM_HOST ? bbytes + cbytes + 512 : 0) + pbytes + 4096));
+  VNM_TRY(pinned_reserve(ctx, 64));
+  VNM_TRY(begin_call(ctx));
+  const void* dB = B;
+  float* dC = C;
+  if (mem == VNM_MEM_HOST) {
+    void* tb = arena_take<unsigned char>(ctx, bbytes);
+    dC = arena_take<float>(ctx, (size_t)A->R * n);
+    if (!tb || !dC) return VNM_ERR_NOMEM;
+    VNM_CUDA_TRY(cudaMemcpyAsync(tb, B, bbytes, cudaMemcpyHostToDevice, ctx->stream));
+    dB = tb;
+  }
+  if ((reinterpret_cast<uintptr_t>(dB) & 15) != 0 || (reinterpret_cast<uintptr_t>(dC) & 15) != 0)
+    return VNM_ERR_ARG;
+  float* P = arena_take<float>(ctx, (size_t)A->nslots * n + 1);
+  int* err = arena_take<int>(ctx, 1);
+  if (!err || !P) return VNM_ERR_NOMEM;
+  VNM_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  VNM_TRY(spmm_enqueue(ctx, A, dB, n, dC, P, err, true));
   VNM_CUDA_TRY(cudaMemcpyAsync(ctx->h_pinned, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   if (mem == VNM_MEM_HOST)
     VNM_CUDA_TRY(cudaMemcpyAsync(C, dC, cbytes, cudaMemcpyDeviceToHost, ctx->stream));
   VNM_TRY(end_call(ctx));
   VNM_CUDA_TRY(cudaEventElapsedTime(&ctx->main_ms, ctx->ev_main0, ctx->ev_main1));
   if (ctx->h_pinned[0] != 0) return VNM_ERR_INTERNAL;
+  return VNM_OK;
+}
+
+vnm_status vnm_spmm_run_async(vnm_ctx* ctx, vnm_spmm_matrix* A, const void* B, int n, float* C, void* stream) {
+  if (!ctx || !A || !B || !C || n <= 0 || (n % 64) != 0) return VNM_ERR_ARG;
+  if (A->device != ctx->device) return VNM_ERR_ARG;
+  if ((reinterpret_cast<uintptr_t>(B) & 15) != 0 || (reinterpret_cast<uintptr_t>(C) & 15) != 0) return VNM_ERR_ARG;
+  VNM_CUDA_TRY(cudaSetDevice(ctx->device));
+  const size_t need = (size_t)A->nslots * n + 1;
+  if (!A->err) {
+    VNM_CUDA_TRY(cudaMalloc(&A->err, sizeof(int)));
+    VNM_CUDA_TRY(cudaMemset(A->err, 0, sizeof(int)));
+  }
+  if (need > A->part_floats) {  // the first call for a larger n: make room (this waits for the device)
+    if (A->part) VNM_CUDA_TRY(cudaFree(A->part));
+    A->part = nullptr;
+    A->part_floats = 0;
+    VNM_CUDA_TRY(cudaMalloc(&A->part, need * sizeof(float)));
+    A->part_floats = need;
+  }
+  ctx->launches = 0;
+  ctx->last_ms = ctx->main_ms = 0.f;
+  cudaStream_t own = ctx->stream;
+  ctx->stream = static_cast<cudaStream_t>(stream);
+  const vnm_status st = spmm_enqueue(ctx, A, B, n, C, A->part, A->err, false);
+  ctx->stream = own;
+  return st;
+}
+
+vnm_status vnm_spmm_check(vnm_spmm_matrix* A, void* stream, int* failed) {
+  if (!A || !failed) return VNM_ERR_ARG;
+  *failed = 0;
+  if (!A->err) return VNM_OK;
+  VNM_CUDA_TRY(cudaSetDevice(A->device));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int h = 0;
+  VNM_CUDA_TRY(cudaMemcpyAsync(&h, A->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  VNM_CUDA_TRY(cudaStreamSynchronize(s));
+  VNM_CUDA_TRY(cudaMemsetAsync(A->err, 0, sizeof(int), s));
+  *failed = h != 0;
   return VNM_OK;
 }
 

@@ -12,6 +12,8 @@ distributions of the five workloads:
   rmat_c4        R-MAT 65536, average degree 32
   chung_lu_c5    Chung-Lu power law (exponent 2.1, mean degree 20), 262144
                  nodes, symmetric-normalised weights D^-1/2 A D^-1/2
+  vnm_structured a matrix already in full V:2:M form (every V x M block
+                 keeps 4 columns, 2 nonzeros a row among them)
 
 All return (nrows, row, col, val) with (row, col) unique and sorted, which is
 the order the Matrix Market reader leaves a matrix in.
@@ -117,6 +119,29 @@ def chung_lu(n, exponent, mean_degree, seed):
 
 def chung_lu_c5(seed=0):
     return chung_lu(262144, 2.1, 20.0, seed)
+
+
+# the six ways to keep 2 of 4 columns
+_PAIRS_OF_4 = np.array([[0, 1], [0, 2], [0, 3], [1, 2], [1, 3], [2, 3]], np.int64)
+
+
+def vnm_structured(R, M=8, V=128, seed=0):
+    """A matrix already in full V:2:M form, the operand V:N:M sparsity is
+    made for (a pruned weight matrix): in every block of V rows x M columns
+    4 columns are kept and every row holds 2 nonzeros among them, so each
+    block has 2V nonzeros and the density is 2/M.  N(0, 1) values; (row,
+    col) sorted.  R must be a multiple of V and of M."""
+    assert R % V == 0 and R % M == 0 and M >= 4
+    rng = np.random.default_rng(seed)
+    nbr, nseg = R // V, R // M
+    keep = np.sort(np.argsort(rng.random((nbr, nseg, M)), axis=-1)[..., :4], axis=-1)  # [nbr][nseg][4]
+    combo = rng.integers(0, 6, (R, nseg), dtype=np.int8)
+    pick = _PAIRS_OF_4[combo]                                                            # [R][nseg][2]
+    k = keep[np.arange(R)[:, None] // V, np.arange(nseg)[None, :]]                       # [R][nseg][4]
+    sel = np.take_along_axis(k, pick, axis=-1)                                          # [R][nseg][2], ascending
+    col = (np.arange(nseg, dtype=np.int64)[None, :, None] * M + sel).reshape(-1).astype(np.int32)
+    row = np.repeat(np.arange(R, dtype=np.int32), nseg * 2)
+    return R, row, col, rng.standard_normal(len(row), dtype=np.float32)
 
 
 def write_mtx(path, nrows, row, col, val, field="real"):
