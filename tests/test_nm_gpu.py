@@ -125,26 +125,34 @@ def test_errors_are_reported(ctx):
     assert res.tolist() == [0, 0, 0, 0, 0] and newpos.tolist() == list(range(8))
 
 
+@pytest.mark.parametrize("table", ["1", "0"])
 @pytest.mark.parametrize("M", [4, 8])
-def test_cluster_sizes_agree(ctx, M):
+def test_cluster_sizes_agree(ctx, M, table):
     """Each job runs on a thread-block cluster whose size depends on the
-    matrix; every size gives the oracle's result bit for bit."""
+    matrix, with the round's row records in the blocks' shared-memory tables
+    (each row owned by one block, reached over DSMEM) or, with
+    VNM_NM_CLUSTER_TABLE=0, in global memory; every size and both places
+    give the oracle's result bit for bit."""
     import os
     from vnm_gb300 import synth
     n, r, c, v = synth.rmat(12, 4096 * 8, 17 + M, "normal")
     ores, _, _, opos = oracle.nm_run(n, r, c, v, 2, M, 1)
-    old = os.environ.get("VNM_NM_CLUSTER")
+    old = {k: os.environ.get(k) for k in ("VNM_NM_CLUSTER", "VNM_NM_CLUSTER_TABLE")}
     try:
+        os.environ["VNM_NM_CLUSTER_TABLE"] = table
         for cs in ("1", "2", "4", "8", "16"):
             os.environ["VNM_NM_CLUSTER"] = cs
             res, newpos = ctx.nm_reorder(n, r, c, v, 2, M, 1)
             assert np.array_equal(res, ores), cs
             assert np.array_equal(newpos, opos), cs
+            if cs != "1" and table == "1":
+                assert ctx.last_stats()["table_rounds"] > 0
     finally:
-        if old is None:
-            os.environ.pop("VNM_NM_CLUSTER", None)
-        else:
-            os.environ["VNM_NM_CLUSTER"] = old
+        for k, v0 in old.items():
+            if v0 is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v0
 
 
 def _large_gain_matrix():

@@ -1,0 +1,67 @@
+"""A bounded wait inside the round kernel that runs out fails the job with
+VNM_ERR_INTERNAL instead of hanging, and the context keeps working.
+
+The walk (one warp) waits for the swap heaps' pops with a poll limit.  The
+test hooks VNM_NM_TEST_HOLD_HEAPS=1 (the heaps publish nothing: a flag that
+nothing sets) and VNM_NM_TEST_WAIT_LIMIT (a small limit) make the wait run
+out on a matrix whose first round must wait: one invalid segment, so the
+walk pairs it with the emptiest segment and waits for that pair's first pop
+(reorder/reorder.h:1837-1860).  The round kernel has no bulk or
+asynchronous copies in flight while the walk waits."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from golden_cases import nm_input
+
+pytestmark = pytest.mark.gpu
+
+
+class _env:
+    def __init__(self, **kv):
+        self.kv = kv
+
+    def __enter__(self):
+        self.old = {k: os.environ.get(k) for k in self.kv}
+        os.environ.update({k: str(v) for k, v in self.kv.items()})
+
+    def __exit__(self, *a):
+        for k, v in self.old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
+def _one_invalid_segment():
+    nr = 64
+    r = np.array([5, 5, 5, 9], np.int32)   # row 5 holds three nodes of segment 0 at 2:4
+    c = np.array([0, 1, 2, 40], np.int32)
+    return nr, r, c, np.ones(4, np.float32)
+
+
+@pytest.mark.parametrize("cluster", ["1", "8"])
+def test_walk_wait_that_runs_out_fails_the_job(ctx, goldens, cluster):
+    import vnm_gb300
+    nr, r, c, v = _one_invalid_segment()
+    with _env(VNM_NM_CLUSTER=cluster):
+        ores, _, _, opos = oracle.nm_run(nr, r, c, v, 2, 4, 0)
+        res, pos = ctx.nm_reorder(nr, r, c, v, 2, 4, 0)   # without the hooks: the oracle's result
+        assert np.array_equal(res, ores) and np.array_equal(pos, opos)
+        with _env(VNM_NM_TEST_HOLD_HEAPS=1, VNM_NM_TEST_WAIT_LIMIT=4096):
+            with pytest.raises(vnm_gb300.VnmError) as e:
+                ctx.nm_reorder(nr, r, c, v, 2, 4, 0)
+            assert e.value.status == 6  # VNM_ERR_INTERNAL
+            with pytest.raises(vnm_gb300.VnmError) as e:
+                ctx.nm_search(nr, r, c, v, 2, 4)
+            assert e.value.status == 6
+        # the same context afterwards: results as before, and on a golden case
+        res, pos = ctx.nm_reorder(nr, r, c, v, 2, 4, 0)
+        assert np.array_equal(res, ores) and np.array_equal(pos, opos)
+        gnr, gr, gc, gv = nm_input(goldens, "rmat_1024__n2_m4")
+        for s in range(4):
+            ores, _, _, opos = oracle.nm_run(gnr, gr, gc, gv, 2, 4, s)
+            res, pos = ctx.nm_reorder(gnr, gr, gc, gv, 2, 4, s)
+            assert np.array_equal(res, ores) and np.array_equal(pos, opos), s

@@ -88,6 +88,8 @@ struct NMJob {
   int* trace_rounds;  // optional: pairs committed by the end of each round
   int trace_cap_pairs;
   int trace_cap_rounds;
+  int walk_wait_limit;  // polls before a wait of the walk gives up (WALK_WAIT_LIMIT)
+  int hold_heaps;       // test only: the swap heaps publish no pop, so a walk that waits runs out
 };
 
 // ---------------------------------------------------------------------------
@@ -218,7 +220,11 @@ struct RoundSmem {
   uint8_t ord[MM][HSTR];       // pop order: ord[k][a * K + b] is the k-th pop of ordered pair (a, b)
   int colstart[K * M];
   int colpre[K * M + 1];
-  uint8_t dest[K][M];          // bit moves of this round's swaps: (xi << 4) | k
+  static constexpr int DEST_W = (K * M + 3) / 4;  // dest in 32-bit words
+  union {
+    uint8_t dest[K][M];        // bit moves of this round's swaps: (xi << 4) | k
+    uint32_t dest_w[DEST_W];   // the same bytes as words, for copies to other blocks
+  };
   int newinv[K], newpres[K];
   int swaps[2 * K * M];        // committed swaps (positions)
   unsigned long long wtop[2][NW][K];
@@ -559,10 +565,16 @@ __device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J, Slice sl = Slice{
   __syncthreads();
   const int E = sm.E;
   if (sm.use_table) {
-    // open addressing, linear probing; a slot is claimed by CAS on its row key
-    unsigned* tw = reinterpret_cast<unsigned*>(sm.table);
+    // open addressing, linear probing; a slot is claimed by CAS on its row
+    // key.  In a cluster, row r's record lives in the table of block
+    // r % cs (reached over DSMEM), so each block later processes and clears
+    // the rows it owns from its own shared memory; the entries are dealt
+    // over every thread of the cluster.  The round uses the tables only
+    // when E <= 3/4 of a table, so a block's table holds every row of the
+    // round even if all of them are its own.
     const unsigned mask = (unsigned)sm.ts_max - 1u;
-    for (int e = tid; e < E; e += NM_THREADS) {
+    const int gthreads = sl.cs * NM_THREADS;
+    for (int e = sl.rank * NM_THREADS + tid; e < E; e += gthreads) {
       int lo = 0, hi = KM - 1;
       while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
@@ -570,13 +582,16 @@ __device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J, Slice sl = Slice{
         else hi = mid - 1;
       }
       const int q = lo, xi = q / M, k = q % M;
-      const unsigned key = (unsigned)J.crow[sm.colstart[q] + (e - sm.colpre[q])] + 1u;
+      const int row = J.crow[sm.colstart[q] + (e - sm.colpre[q])];
+      const unsigned key = (unsigned)row + 1u;
+      unsigned* tw = reinterpret_cast<unsigned*>(sm.table);
+      if (sl.cs > 1) tw = cg::this_cluster().map_shared_rank(tw, (unsigned)(row % sl.cs));
       unsigned h = (key * 2654435761u) >> sm.ts_shift;
       for (int probe = 0; probe <= (int)mask; ++probe) {
         const unsigned cur = atomicCAS(&tw[4 * h + 3], 0u, key);
         if (cur == 0u || cur == key) {
           atomicOr(&tw[4 * h + (xi >> 2)], (1u << k) << ((xi & 3) * 8));
-          if (cur == 0u) atomicAdd(&sm.ntouched, 1);
+          if (cur == 0u) atomicAdd(ntp, 1);
           break;
         }
         h = (h + 1u) & mask;
@@ -667,7 +682,7 @@ __device__ __forceinline__ void for_touched_warp(const RoundSmem<M>& sm, const N
 // touched rows (index = row).  Warp-uniform like for_touched_warp.
 template <int M, class F>
 __device__ __forceinline__ void for_rows_warp(const RoundSmem<M>& sm, const NMJob& J, Slice sl, F&& f) {
-  if (sm.use_table) {  // one block per job only
+  if (sm.use_table) {  // the rows this block's table holds
     constexpr int NW = NM_THREADS / 32;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int base = w * 32; base < sm.ts_max; base += NW * 32) {
@@ -999,7 +1014,7 @@ __device__ __forceinline__ unsigned order_key_lo(int s, bool rev) {  // segment:
 constexpr int WALK_WAIT_LIMIT = 1 << 20;
 
 template <int M>
-__device__ void walk_phase(RoundSmem<M>& sm, int sched) {
+__device__ void walk_phase(RoundSmem<M>& sm, int sched, int wait_limit) {
   constexpr int K = M + 1, MM = M * M;
   constexpr int HS = RoundSmem<M>::HSTR;
   constexpr unsigned FULLM = (1u << M) - 1u;
@@ -1013,7 +1028,7 @@ __device__ void walk_phase(RoundSmem<M>& sm, int sched) {
   auto wait_pops = [&](int col, int need) -> int {
     int avail = __shfl_sync(FULL, prog[col], 0);
     for (int spin = 0; avail < need; ++spin) {
-      if (spin >= WALK_WAIT_LIMIT) return -1;
+      if (spin >= wait_limit) return -1;
       avail = __shfl_sync(FULL, prog[col], 0);
     }
     __threadfence_block();
@@ -1283,6 +1298,7 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
   int round = 1;
   int committed = 0;
   unsigned long long sumE = 0, sumT = 0;
+  int table_rounds = 0;  // rounds whose row records were in shared-memory tables
   // cycles spent in each phase of a round, measured by thread 0 of the
   // leader at the barriers that end the phases: select, choose, gather,
   // process, heap, walk, apply
@@ -1311,14 +1327,16 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
         __syncthreads();
         VNM_PHASE(1);
       }
-      for (int r = 1; r < cs; ++r) {  // the round's segments to every block
-        RoundSmem<M>* rs = cl.map_shared_rank(&sm, r);
-        if (tid == 0) {
-          rs->go = sm.go;
-          rs->K_ = sm.K_;
-          rs->mode = sm.mode;
-        }
-        if (tid < K) rs->xseg[tid] = sm.xseg[tid];
+      // the round's segments to every block, one remote store a thread (a
+      // thread issuing them all in turn took ~4 K cycles a round)
+      constexpr int F = K + 3;
+      if (tid < (cs - 1) * F) {
+        const int f = tid % F;
+        RoundSmem<M>* rs = cl.map_shared_rank(&sm, 1 + tid / F);
+        if (f < K) rs->xseg[f] = sm.xseg[f];
+        else if (f == K) rs->go = sm.go;
+        else if (f == K + 1) rs->K_ = sm.K_;
+        else rs->mode = sm.mode;
       }
     }
     if (cs > 1) cl.sync();
@@ -1348,8 +1366,8 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     if (lead) {
       rank_phase<M>(sm);
       VNM_PHASE(4);
-      if (tid >= NM_THREADS - 32) walk_phase<M>(sm, J.sched);  // the last warp walks ...
-      else heap_sift<M>(sm);                                   // ... while the heaps pop
+      if (tid >= NM_THREADS - 32) walk_phase<M>(sm, J.sched, J.walk_wait_limit);  // the last warp walks ...
+      else if (!J.hold_heaps) heap_sift<M>(sm);                                   // ... while the heaps pop
       __syncthreads();
       VNM_PHASE(5);
       if (tid == 0 && J.trace_pairs) {
@@ -1364,9 +1382,13 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
       }
       sumE += (unsigned)sm.E;
       sumT += (unsigned)sm.ntouched;
-      for (int r = 1; r < cs; ++r) {  // where each bit of the round's segments goes
-        RoundSmem<M>* rs = cl.map_shared_rank(&sm, r);
-        if (tid < K * M) (&rs->dest[0][0])[tid] = (&sm.dest[0][0])[tid];
+      table_rounds += sm.use_table ? 1 : 0;
+      // where each bit of the round's segments goes, to every block (one
+      // remote word store a thread)
+      constexpr int DW = RoundSmem<M>::DEST_W;
+      if (tid < (cs - 1) * DW) {
+        RoundSmem<M>* rs = cl.map_shared_rank(&sm, 1 + tid / DW);
+        rs->dest_w[tid % DW] = sm.dest_w[tid % DW];
       }
     }
     if (cs > 1) cl.sync();
@@ -1401,6 +1423,7 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     J.res[8] = (int)(sumE >> 31);
     J.res[9] = (int)(sumT & 0x7fffffffull);
     J.res[10] = (int)(sumT >> 31);
+    J.res[11] = table_rounds;
     for (int q = 0; q < 7; ++q) J.res[16 + q] = (int)(tph[q] >> 10);  // kilocycles
   }
 }
@@ -1550,6 +1573,17 @@ static vnm_status make_job(vnm_ctx* ctx, const Pattern& P, int sched, int maxite
   J.trace_rounds = nullptr;
   J.trace_cap_pairs = 0;
   J.trace_cap_rounds = 0;
+  // Test hooks for the walk's bounded wait (a job whose wait runs out fails
+  // with VNM_ERR_INTERNAL instead of hanging): VNM_NM_TEST_WAIT_LIMIT
+  // lowers the poll limit, VNM_NM_TEST_HOLD_HEAPS=1 keeps the swap heaps
+  // from publishing, so the first wait runs out.  Unset, they change nothing.
+  J.walk_wait_limit = WALK_WAIT_LIMIT;
+  J.hold_heaps = 0;
+  if (const char* e = getenv("VNM_NM_TEST_WAIT_LIMIT")) {
+    const int v = atoi(e);
+    if (v > 0 && v < WALK_WAIT_LIMIT) J.walk_wait_limit = v;
+  }
+  if (const char* e = getenv("VNM_NM_TEST_HOLD_HEAPS")) J.hold_heaps = atoi(e) == 1 ? 1 : 0;
   if (!J.orig || !J.cnt || !J.zc || !J.rec || !J.touched || !J.res) return VNM_ERR_NOMEM;
   VNM_CUDA_TRY(cudaMemsetAsync(J.rec, 0, sizeof(uint4) * (P.R > 0 ? P.R : 1), ctx->stream));
   VNM_CUDA_TRY(cudaMemsetAsync(J.res, 0, sizeof(int) * 24, ctx->stream));
@@ -1581,7 +1615,13 @@ static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, 
   const size_t fixed = sizeof(RoundSmem<M>) + hbytes + (in_smem ? cbytes : 0);
   int ts = 8192;
   while (ts >= 1024 && fixed + (size_t)ts * sizeof(uint4) > NM_SMEM_BUDGET) ts >>= 1;
-  if (ts < 1024 || cs > 1) ts = 0;  // the shared-memory row table serves single-block jobs
+  if (ts < 1024) ts = 0;
+  // cluster jobs keep their round's row records in global memory unless
+  // VNM_NM_CLUSTER_TABLE=1 puts them in every block's shared memory table
+  if (cs > 1) {
+    const char* e = getenv("VNM_NM_CLUSTER_TABLE");
+    if (!(e && atoi(e) == 1)) ts = 0;
+  }
   const size_t dyn = hbytes + (size_t)ts * sizeof(uint4) + (in_smem ? cbytes : 0);
   // static + dynamic shared memory may pass the 48 KB a launch gets without
   // opting in (RoundSmem<8> alone is ~30 KB)
@@ -1760,6 +1800,7 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
     ctx->stats[1] += (long long)h[7] + ((long long)h[8] << 31);
     ctx->stats[2] += (long long)h[9] + ((long long)h[10] << 31);
     for (int q = 0; q < 7; ++q) ctx->stats[8 + q] += h[16 + q];
+    ctx->stats[7] += h[11];
   }
   if (trace) {
     const int committed = hres_copy[6];
@@ -1925,6 +1966,8 @@ static vnm_status run_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int6
     J.trace_rounds = nullptr;
     J.trace_cap_pairs = 0;
     J.trace_cap_rounds = 0;
+    J.walk_wait_limit = WALK_WAIT_LIMIT;
+    J.hold_heaps = 0;
     if (J.nseg > max_nseg) max_nseg = J.nseg;
   }
   VNM_CUDA_TRY(cudaMemcpyAsync(d_jobs, hj.data(), sizeof(NMJob) * nmat, cudaMemcpyHostToDevice, ctx->stream));
@@ -2034,6 +2077,19 @@ vnm_status vnm_permute_coo(vnm_ctx* ctx, int nrows, int nnz, int* row, int* col,
     VNM_CUDA_TRY(cudaMemcpyAsync(col, d_col, sizeof(int) * nnz, cudaMemcpyDeviceToHost, ctx->stream));
   }
   return end_call(ctx);
+}
+
+vnm_status vnm_permute_coo_async(vnm_ctx* ctx, int nrows, int nnz, int* row, int* col, const int* newpos,
+                                 void* stream) {
+  if (!ctx || nrows < 0 || nnz < 0 || !newpos || (nnz > 0 && (!row || !col))) return VNM_ERR_ARG;
+  VNM_CUDA_TRY(cudaSetDevice(ctx->device));
+  ctx->launches = 0;
+  ctx->last_ms = ctx->main_ms = 0.f;
+  if (nnz == 0) return VNM_OK;
+  const int grid = grid_for(ctx, nnz);
+  k_permute<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(row, col, nnz, newpos);
+  ctx->launches = 1;
+  return cudaGetLastError() == cudaSuccess ? VNM_OK : VNM_ERR_CUDA;
 }
 
 vnm_status vnm_nm_segment_counts(vnm_ctx* ctx, int nrows, int nnz, const int* row, const int* col,
