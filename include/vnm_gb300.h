@@ -19,7 +19,8 @@
  *     memory of the context's GPU; nothing is copied).
  *   - A context owns one CUDA stream and its scratch memory; use one context
  *     per host thread.  Calls are synchronous with respect to the host unless
- *     stated otherwise.
+ *     stated otherwise; the *_async calls enqueue on a stream the caller
+ *     passes and return without waiting.
  */
 #ifndef VNM_GB300_H
 #define VNM_GB300_H
@@ -73,7 +74,8 @@ float vnm_last_main_kernel_ms(const vnm_ctx* ctx);
  * out[0] rounds summed over jobs, out[1] column entries gathered,
  * out[2] row records touched, out[3] segments per job, out[4] jobs,
  * out[5] nonzero-valued entries of the pattern, out[6] thread blocks per
- * job (the cluster size the launch used), out[8..14] kilocycles
+ * job (the cluster size the launch used), out[7] rounds whose row records
+ * were in shared-memory tables (summed over jobs), out[8..14] kilocycles
  * spent per round phase (select, choose, gather, process, heap entries,
  * swap heaps and walk overlapped, apply) summed over jobs.  n <= 16
  * values. */
@@ -163,6 +165,11 @@ vnm_status vnm_nm_reorder_noalloc(int nrows, int nnz, const int* row, const int*
  * col = newpos[col] -- the Reorder kernel of reorder/reorder.h:23-35 with all
  * rounds composed.  The order of the entries does not change. */
 vnm_status vnm_permute_coo(vnm_ctx* ctx, int nrows, int nnz, int* row, int* col, int mem, const int* newpos);
+
+/* vnm_permute_coo for device arrays, enqueued on the caller's `stream` (a
+ * cudaStream_t, NULL = the default stream) without waiting. */
+vnm_status vnm_permute_coo_async(vnm_ctx* ctx, int nrows, int nnz, int* row, int* col, const int* newpos,
+                                 void* stream);
 
 /* Per-segment counts of the current matrix: invalid[s] = rows whose M-group
  * in segment s has more than N nonzeros (LocateinvalidSegment,
@@ -283,29 +290,53 @@ vnm_status vnm_vnm_reorder(vnm_ctx* ctx, int m, int n, int nnz, int* row, int* c
 typedef struct vnm_spmm_matrix vnm_spmm_matrix;
 
 /* Compress a (reordered) sparse matrix into the V:N:M layout the SpMM
- * kernel reads: 128-row tiles; every non-empty V x M block is cut into
- * slices of 4 columns with at most 2 nonzeros per row (one slice when the
- * block satisfies V:N:M, more when it does not, so nothing is dropped);
- * values are divided by their V-block row's largest magnitude and stored
- * as `dtype` (1 = BF16, 0 = FP16).  Requires 128 % V == 0, 2 <= M <= 8.
+ * kernels read: 128-row tiles; every V x M block with at least V nonzeros
+ * (VNM_SPMM_DENSE_MIN in the environment sets another threshold, 0 = every
+ * block) is cut into slices of 4 columns with at most 2 nonzeros per row
+ * (one slice when the block satisfies V:N:M, more when it does not, so
+ * nothing is dropped) for the tensor cores; their values are divided by
+ * their V-block row's largest magnitude and stored as `dtype` (1 = BF16,
+ * 0 = FP16).  The nonzeros of sparser blocks form a row-major residual
+ * (FP32 values) that a CUDA-core kernel multiplies.  Requires 128 % V == 0,
+ * 2 <= M <= 8.
  * COO in any order.  The result lives in device memory of the context's
  * GPU until vnm_spmm_free; its storage is taken from the last operand this
  * context's operands freed when that is large enough, else allocated. */
 vnm_status vnm_spmm_compress(vnm_ctx* ctx, int nrows, int nnz, const int* row, const int* col, const float* val,
                              int mem, int M, int V, int dtype, vnm_spmm_matrix** out);
 
-/* info[0..7] = {nnz, non-empty blocks, blocks that satisfy V:N:M, slices,
- * slices after padding tiles to K-steps of 4, K-steps, tiles, bytes of A}. */
+/* info[0..12] = {nnz, non-empty blocks, blocks that satisfy V:N:M, slices,
+ * slices after padding tiles to K-steps of 4, K-steps, tiles, bytes of A
+ * tiles, residual nonzeros, residual tasks, tiles with tensor-core work,
+ * the block threshold used, partial rows of split residual rows}. */
 vnm_status vnm_spmm_info(const vnm_spmm_matrix* A, long long* info, int n);
 
 /* C (nrows x n, FP32, row-major) = A * B with B (nrows x n, row-major, the
  * compressed dtype).  n must be a multiple of 64.  mem = where B and C are
- * (device: 16-byte aligned).  The kernel works on column blocks of 256, 128
- * or 64; the first call of a context for an operand shape (rows, K-steps)
+ * (device: 16-byte aligned).  The tensor-core kernel works on column blocks
+ * of 256, 128 or 64; the first call of a context for an operand shape (rows, K-steps)
  * and n times each width that divides n once and keeps the fastest for
  * later calls (up to 8 shapes per context).  VNM_SPMM_WIDTH=64|128|256 in
  * the environment fixes the width where it divides n. */
 vnm_status vnm_spmm_run(vnm_ctx* ctx, const vnm_spmm_matrix* A, const void* B, int n, float* C, int mem);
+
+/* vnm_spmm_run on the caller's stream, for device buffers, without
+ * waiting: the kernels are enqueued on `stream` (a cudaStream_t, NULL = the
+ * default stream) after the work the caller enqueued there, and the call
+ * returns at once.  B (nrows x n, the operand's 16-bit type) and C (nrows x
+ * n, FP32) are device memory, 16-byte aligned, valid until the stream
+ * reaches the product.  Exceptions to "without waiting": the first call for
+ * an operand shape and n times the tensor-core column-block widths
+ * (synchronising `stream` once), and the first call with a larger n than
+ * before allocates the operand's scratch (cudaMalloc).  Calls on one operand
+ * share that scratch, so they must run in order (one stream, or streams the
+ * caller orders).  A bounded wait that ran out inside the tensor-core kernel
+ * sets a flag on the operand; vnm_spmm_check reads it. */
+vnm_status vnm_spmm_run_async(vnm_ctx* ctx, vnm_spmm_matrix* A, const void* B, int n, float* C, void* stream);
+
+/* Waits for `stream`; *failed = 1 when a vnm_spmm_run_async of A failed
+ * inside a kernel since the last check (the flag is cleared), else 0. */
+vnm_status vnm_spmm_check(vnm_spmm_matrix* A, void* stream, int* failed);
 
 /* Release an operand.  While its context lives, the context keeps the
  * largest freed operand's device storage for its next vnm_spmm_compress

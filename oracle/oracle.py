@@ -254,3 +254,17 @@ def spmm_f64(nrows, row, col, val, B):
     lib().orc_spmm_f64(nrows, len(row), _p(row, _i32p), _p(col, _i32p), _p(val, _f64p), _p(B, _f64p), n,
                        _p(C, _f64p))
     return C
+
+
+def rowwise_rel_err(C, ref):
+    """Largest per-row relative error max_i ||C_i - ref_i||_inf / ||ref_i||_inf.
+
+    Rows whose reference is exactly zero (no nonzero in the row) count with
+    a denominator of 1e-30, so any nonzero output there fails the bound.
+    Unlike max |C - ref| / max |ref| over the whole matrix, a low-degree row
+    cannot hide behind the hub rows that set the global maximum."""
+    C = np.asarray(C, np.float64)
+    ref = np.asarray(ref, np.float64)
+    num = np.abs(C - ref).max(axis=1) if C.size else np.zeros(len(C))
+    den = np.maximum(np.abs(ref).max(axis=1) if ref.size else np.zeros(len(ref)), 1e-30)
+    return float((num / den).max()) if len(num) else 0.0

@@ -153,8 +153,8 @@ class Context:
     def last_stats(self):
         out = (ctypes.c_longlong * 16)()
         _check(lib().vnm_last_stats(self.h, out, 16), "vnm_last_stats")
-        keys = ("rounds", "gathered", "touched", "nseg", "jobs", "pattern_nnz", "blocks_per_job")
-        d = dict(zip(keys, list(out)[:7]))
+        keys = ("rounds", "gathered", "touched", "nseg", "jobs", "pattern_nnz", "blocks_per_job", "table_rounds")
+        d = dict(zip(keys, list(out)[:8]))
         d["phase_kcycles"] = dict(zip(("select", "choose", "gather", "process", "heap_entries", "heaps_and_walk", "apply"),
                                       list(out)[8:15]))
         return d
@@ -310,6 +310,8 @@ class SpmmMatrix:
             L.vnm_spmm_info.argtypes = [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]
             L.vnm_spmm_run.argtypes = [_vp, _vp, _vp, ctypes.c_int, _vp, ctypes.c_int]
             L.vnm_spmm_free.argtypes = [_vp]
+            L.vnm_spmm_run_async.argtypes = [_vp, _vp, _vp, ctypes.c_int, _vp, _vp]
+            L.vnm_spmm_check.argtypes = [_vp, _vp, _i32p]
             L._spmm_typed = True
         self.ctx = ctx
         self.nrows = nrows
@@ -349,6 +351,32 @@ class SpmmMatrix:
         _check(lib().vnm_spmm_run(self.ctx.h, self.h, ctypes.c_void_p(B.ctypes.data), n,
                                   ctypes.c_void_p(C.ctypes.data), MEM_HOST), "vnm_spmm_run")
         return C
+
+    def run_async(self, B, C=None, stream=None):
+        """C = A B enqueued on a CUDA stream (torch's current stream of B's
+        device by default) without waiting; B and C are CUDA tensors.  The
+        first call for an operand shape and n times the kernel widths once."""
+        import torch
+        n = B.shape[1]
+        if C is None:
+            C = torch.empty((self.nrows, n), dtype=torch.float32, device=B.device)
+        if stream is None:
+            stream = torch.cuda.current_stream(B.device)
+        _check(lib().vnm_spmm_run_async(self.ctx.h, self.h, ctypes.c_void_p(B.data_ptr()), n,
+                                        ctypes.c_void_p(C.data_ptr()), ctypes.c_void_p(stream.cuda_stream)),
+               "vnm_spmm_run_async")
+        return C
+
+    def check(self, stream=None):
+        """Wait for the stream; raise if an asynchronous product failed in a kernel."""
+        import torch
+        if stream is None:
+            stream = torch.cuda.current_stream()
+        failed = ctypes.c_int()
+        _check(lib().vnm_spmm_check(self.h, ctypes.c_void_p(stream.cuda_stream), ctypes.byref(failed)),
+               "vnm_spmm_check")
+        if failed.value:
+            raise VnmError(6, "vnm_spmm_run_async")
 
     def close(self):
         if self.h:

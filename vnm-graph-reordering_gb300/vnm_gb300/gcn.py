@@ -15,9 +15,11 @@ second operand built from the transposed pattern, or through the same
 operand when the adjacency is symmetric (the normalised adjacency
 D^-1/2 A D^-1/2 of an undirected graph is).
 
-The library call runs on the context's own stream and returns when it is
-done; the op waits for the producer of X on the current PyTorch stream
-before it starts.
+Every aggregation is enqueued on PyTorch's current stream of X's device
+(vnm_spmm_run_async) after the work that produced X, and the op returns
+without waiting for it, so a training loop does not stall the host at each
+layer.  The first aggregation of an operand shape and feature width times
+the kernel's widths once (a one-time wait).
 """
 import numpy as np
 
@@ -70,8 +72,7 @@ class VnmAdjacency:
         import torch
         assert X.is_cuda and X.dim() == 2 and X.shape[0] == self.n
         Xp, F = _pad_cols(X.detach().to(self.torch_dtype))
-        torch.cuda.current_stream(X.device).synchronize()  # X is complete before the library's stream reads it
-        Y = (self.bwd if transpose else self.fwd).run(Xp)
+        Y = (self.bwd if transpose else self.fwd).run_async(Xp, stream=torch.cuda.current_stream(X.device))
         return Y[:, :F] if Y.shape[1] != F else Y
 
     def close(self):
