@@ -23,6 +23,8 @@ configurations are measured and reported in the same JSON line:
               65536: wall time to the plain reorder's retained-nnz
   c5_gcn      Chung-Lu 262144 graph: learned reorder, compression and 100
               SpMMs with a 262144x256 BF16 / FP16 operand, error vs FP64
+  s1_structured_spmm  a matrix in full V:2:8 form (the operand V:N:M is
+              made for) through the tensor-core SpMM, beside cuBLAS/cuSPARSE
 (--no-extended skips them.)
 
 --impl reference runs the CPU port of the reference algorithm (the
@@ -54,7 +56,13 @@ N_NM, M_NM, V, N_B = 2, 4, 64, 128
 TARGETS = 4
 WORKLOAD = ("C2: R-MAT 16384x16384 (a=.57,b=.19,c=.19), 131072 edges symmetrised, N(0,1), 2:4, V=64; "
             "find_best_2toX + V:N:M SpMM with B 16384x128 bf16")
-METRIC = "reorder wall-time (find_best_2toX, R-MAT 16384, 2:4) + V:N:M SpMM, as hot-path steps per second"
+# the headline metric of the workload table; `value` is its plain-reorder +
+# SpMM step on the R-MAT 16384 workload, the learned-vs-plain half is under
+# c4_learned and the SpMM TFLOP/s under spmm / c5_gcn
+METRIC = "reorder wall-time to equal retained-nnz (learned vs plain); V:N:M SpMM TFLOP/s"
+VALUE_IS = ("hot-path steps/s of the R-MAT 16384 2:4 step (find_best_2toX + relabel + V:N:M compress + SpMM); "
+            "learned vs plain in c4_learned, SpMM TFLOP/s in spmm and c5_gcn")
+GOLD = os.path.join(REPO, "tests", "golden")
 
 
 def parse():
@@ -68,6 +76,9 @@ def parse():
     ap.add_argument("--c5-spmm-only", action="store_true",
                     help="only the GCN workload's BF16 SpMM, --steps runs, with the reorder's state released first "
                          "(a few GB on the device: the command profiles of that kernel use)")
+    ap.add_argument("--s1-spmm-only", action="store_true",
+                    help="only the structured V:2:8 SpMM workload on the tensor cores, --steps runs (the command "
+                         "profiles of the tensor-core kernel use)")
     return ap.parse_args()
 
 
@@ -140,12 +151,17 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def load_tensor_peak():
+def load_tensor_peak(sustained=False):
+    """The measured bf16 tensor peak: the burst figure for a kernel timed
+    alone, the sustained one for a kernel timed inside a long loop."""
     p = os.path.join(REPO, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         with open(p) as f:
-            return float(json.load(f)["bf16_tflops"]), "measured (burst)"
-    return 1900.0, "fallback"
+            d = json.load(f)
+        if sustained and "bf16_tflops_sustained" in d:
+            return float(d["bf16_tflops_sustained"]), "measured (sustained)"
+        return float(d["bf16_tflops"]), "measured (burst)"
+    return (1700.0, "fallback (sustained)") if sustained else (1900.0, "fallback")
 
 
 def whole_job_rate(elapsed_s, steps, world, device=None):
@@ -168,12 +184,34 @@ def workload(rank):
 
 
 def cpu_port_find_best(nr, r, c, v, threads):
+    """The oracle's find_best_2toX on `threads` host threads: (seconds, the
+    schedule it picks, the four result vectors)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle
     oracle.set_threads(threads)
     t0 = time.perf_counter()
-    best, _ = oracle.find_best(nr, r, c, v, N_NM, M_NM)
-    return time.perf_counter() - t0, best
+    best, out = oracle.find_best(nr, r, c, v, N_NM, M_NM)
+    dt = time.perf_counter() - t0
+    # find_best's rows: nrows, nnz, density, init_size, final_size, init_cnt,
+    # final_cnt, improve, rounds, ... (main.cu:59-69)
+    res4 = np.rint(out[:, [3, 4, 5, 6, 8]]).astype(np.int32)
+    return dt, best, res4
+
+
+def cpu_port_one_schedule(nr, r, c, v, sched, threads):
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    oracle.set_threads(threads)
+    t0 = time.perf_counter()
+    oracle.nm_run(nr, r, c, v, N_NM, M_NM, sched)
+    return time.perf_counter() - t0
+
+
+def oracle_nm_run(nr, r, c, v, sched, N=N_NM, M=M_NM):
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    oracle.set_threads(host_threads())
+    return oracle.nm_run(nr, r, c, v, N, M, sched)
 
 
 def host_threads():
@@ -197,8 +235,155 @@ def cpu_port_step(nr, r, c, v, B64, threads):
     return time.perf_counter() - t0, best
 
 
+def scale_golden(name):
+    """The oracle's committed results at a benchmarked size (made by
+    tests/golden/make_scale_goldens.py), or None when absent."""
+    p = os.path.join(GOLD, "scale_oracle_goldens.npz")
+    if not os.path.exists(p):
+        return None
+    g = np.load(p)
+    if name + "__res5x4" not in g:
+        return None
+    return {"res5x4": g[name + "__res5x4"], "newpos4": g[name + "__newpos4"], "best": int(g[name + "__best"]),
+            "sha256": str(g[name + "__sha256"])}
+
+
+def coo_digest(nrows, row, col, val):
+    import hashlib
+    h = hashlib.sha256()
+    h.update(np.int64(nrows).tobytes())
+    for a, t in ((row, np.int32), (col, np.int32), (val, np.float32)):
+        h.update(np.ascontiguousarray(a, t).tobytes())
+    return h.hexdigest()
+
+
+def nonzero_groups(nrows, row, col, val, M):
+    """Nonzero (row, M-column segment) groups of the pattern (val != 0)."""
+    m = val != 0
+    return int(len(np.unique(row[m].astype(np.int64) * (nrows // M) + col[m] // M)))
+
+
+def spmm_hbm_bytes(nrows, nnz, n, elem=2):
+    """Algorithmic bytes of C = A B: A as CSR (a 16-bit value and a 32-bit
+    column per nonzero, 32-bit row pointers), B read once, C (FP32) written
+    once."""
+    return nnz * (elem + 4) + 4 * (nrows + 1) + nrows * n * elem + nrows * n * 4
+
+
+def time_cuda(fn, reps, stream=None):
+    """Median milliseconds of fn() over reps runs, CUDA events on the
+    current stream, one warm-up run."""
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return float(np.median(ms))
+
+
+def library_spmm_baselines(nr, r, c, v, n, dtype, dense=True, reps=10):
+    """Context baselines for the V:N:M SpMM (not the product): cuSPARSE CSR
+    SpMM through torch.sparse (FP32, and the 16-bit type where the build
+    supports it) and, where the densified matrix fits, a cuBLAS GEMM of the
+    densified matrix (16-bit operands, FP32 accumulation)."""
+    import torch
+    dev = torch.device("cuda", torch.cuda.current_device())
+    out = {}
+    g = torch.Generator().manual_seed(99)
+    Bf = torch.randn((nr, n), generator=g).to(dev)
+    idx = torch.from_numpy(np.stack([r, c]).astype(np.int64)).to(dev)
+    A32 = torch.sparse_coo_tensor(idx, torch.from_numpy(v).to(dev), (nr, nr)).coalesce().to_sparse_csr()
+    flops = 2.0 * len(r) * n
+    try:
+        ms = time_cuda(lambda: torch.sparse.mm(A32, Bf), reps)
+        out["cusparse_csr_fp32"] = {"ms": ms, "useful_tflops": flops / ms / 1e9}
+    except Exception as e:  # report, keep the rest
+        out["cusparse_csr_fp32"] = {"error": "%s: %s" % (type(e).__name__, e)}
+    try:
+        A16 = A32.to(dtype)
+        B16 = Bf.to(dtype)
+        ms = time_cuda(lambda: torch.sparse.mm(A16, B16), reps)
+        out["cusparse_csr_16bit"] = {"ms": ms, "useful_tflops": flops / ms / 1e9, "dtype": str(dtype)}
+    except Exception as e:
+        out["cusparse_csr_16bit"] = {"error": "%s: %s" % (type(e).__name__, e)}
+    if dense and nr * nr * 2 <= (2 << 30):
+        Ad = A32.to_dense().to(dtype)
+        B16 = Bf.to(dtype)
+        ms = time_cuda(lambda: torch.matmul(Ad, B16), reps)
+        out["cublas_dense_16bit"] = {"ms": ms, "dense_tflops": 2.0 * nr * nr * n / ms / 1e9,
+                                     "useful_tflops": flops / ms / 1e9, "dtype": str(dtype),
+                                     "note": "the densified matrix times B; output in the 16-bit type"}
+        del Ad
+    del A32, Bf
+    torch.cuda.empty_cache()
+    return out
+
+
+def reference_gpu_c2(nr, r, c, v, timeout=300.0):
+    """The reference's own GPU reorder (reorder/reorder.h built from its
+    sources with N=2, M=4 into oracle/_ref/ref_nm_n2_m4 by
+    oracle/ref_build.py) on the same matrix, schedule by schedule, as
+    find_best_2toX (main.cu:72-114) runs them: wall seconds per schedule
+    and the result integers."""
+    import tempfile
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import ref_build
+    from vnm_gb300 import synth
+    try:
+        exe = ref_build.ensure("ref_nm_n2_m4")
+    except Exception as e:
+        return {"unavailable": "%s: %s" % (type(e).__name__, e)}
+    out = {"what": "the reference's own GPU find_best_2toX schedules (reorder/reorder.h, main.cu:72-114), built "
+                   "from its sources for sm_103a; includes each run's file read and CUDA set-up, as the "
+                   "reference's command does", "seconds": {}, "res5": {}}
+    with tempfile.TemporaryDirectory() as td:
+        mtx = os.path.join(td, "c2.mtx")
+        synth.write_mtx(mtx, nr, r, c, v)
+        for sch in range(4):
+            o = os.path.join(td, "res%d.txt" % sch)
+            t0 = time.perf_counter()
+            try:
+                p = subprocess.run([exe, mtx, str(sch), o], capture_output=True, text=True, timeout=timeout)
+                out["seconds"][sch] = time.perf_counter() - t0
+                if p.returncode == 0:
+                    with open(o) as f:
+                        out["res5"][sch] = [int(x) for x in f.readline().split()[2:7]]
+                else:
+                    out["res5"][sch] = "rc %d" % p.returncode
+            except subprocess.TimeoutExpired:
+                out["seconds"][sch] = None
+                out["res5"][sch] = "timeout after %.0f s" % timeout
+    secs = [x for x in out["seconds"].values() if x is not None]
+    out["total_seconds"] = sum(secs) if len(secs) == 4 else None
+    return out
+
+
+def vnm_stage_port(nr, r, c, v):
+    """The CPU port of reordering.py (the oracle's restatement) on the same
+    matrix at M=8, V=64, one thread: seconds per VNM round.  (At the step's
+    2:4 a segment has 4 columns, so no V-block can be invalid and the stage
+    does no round.)"""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    oracle.set_threads(1)
+    t0 = time.perf_counter()
+    out5, _, _, _ = oracle.vnm_run(nr, nr, r, c, 8, V, 10)
+    dt = time.perf_counter() - t0
+    return {"seconds": dt, "rounds": int(out5[4]), "seconds_per_round": dt / max(1, int(out5[4])),
+            "out5": out5.tolist(), "cores": 1, "kind": "port",
+            "what": "C++ restatement of reordering.py (M=8, V=64) on the R-MAT 16384 matrix"}
+
+
 def run_reference(args, rank, world):
-    """CPU port of the reference path, on the host cores, rank 0 only."""
+    """CPU port of the reference path, on the host cores, rank 0 only.  The
+    line also carries the reference's own GPU reorder on the same matrix
+    (reference_gpu), the port on one thread, and the VNM-stage port."""
     if rank != 0:
         return
     nr, r, c, v = workload(0)
@@ -213,8 +398,8 @@ def run_reference(args, rank, world):
     tot = sum(times)
     value = args.steps / tot
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": "hot-path steps/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot / args.steps,
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "hot-path steps/s", "value_is": VALUE_IS,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32 (reorder), fp64 (SpMM)",
         "data": "synthetic (seeded R-MAT)",
         "config": {"workload": WORKLOAD, "nrows": nr, "nnz": int(len(r)), "N": N_NM, "M": M_NM, "V": V,
@@ -224,6 +409,12 @@ def run_reference(args, rank, world):
                                    "restatement of reorder/reorder.h + main.cu, OpenMP) + FP64 SpMM"},
         "e2e": {"value": value, "unit": "hot-path steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if not args.no_extended:
+        line["cpu_baseline"]["one_thread"] = {
+            "seconds_one_schedule": cpu_port_one_schedule(nr, r, c, v, int(best), 1), "cores": 1,
+            "sample": "schedule %d of find_best_2toX on one thread" % int(best)}
+        line["vnm_stage_port"] = vnm_stage_port(nr, r, c, v)
+        line["reference_gpu"] = reference_gpu_c2(nr, r, c, v)
     print(json.dumps(line), flush=True)
 
 
@@ -280,6 +471,8 @@ def run_ours(args, rank, world, local):
         t["launches"] += ctx.last_launch_count
         t["info"] = A.info()
         t["best"] = best
+        t["res4"] = res
+        t["newpos"] = newpos
         A.close()
         return t
 
@@ -339,29 +532,51 @@ def run_ours(args, rank, world, local):
     nnz = len(r)
     h2d = 12 * nnz + 8 * nnz + 4 * nr + 12 * nnz + 2 * nr * N_B
     d2h = 4 * 20 + 4 + 4 * nr + 8 * nnz + 4 * nr * N_B
+    newpos = t["newpos"]
     # SpMM accuracy against the FP64 oracle (outside the timed region)
-    spmm_err = None
+    spmm_err = spmm_err_norm = None
     if rank == 0:
         sys.path.insert(0, os.path.join(REPO, "oracle"))
         import oracle
-        _, rr, cc, nv = oracle.nm_run(nr, r, c, v, N_NM, M_NM, best)
+        rr, cc = newpos[r], newpos[c]
         ref = oracle.spmm_f64(nr, rr, cc, v.astype(np.float64), Bh.float().numpy().astype(np.float64))
-        spmm_err = float(np.abs(C.astype(np.float64) - ref).max() / np.abs(ref).max())
-    # roofline of the persistent reorder kernel: the bytes its algorithm must
-    # move per step = per round the segment-count scan (4 B x nseg) + per
-    # gathered column entry 4 B (row id) + 16 B record update, + per touched
-    # row the 16 B record read and clear
+        spmm_err = oracle.rowwise_rel_err(C, ref)
+        spmm_err_norm = float(np.abs(C.astype(np.float64) - ref).max() / np.abs(ref).max())
+        del ref
+    # roofline of the persistent reorder kernel.  Algorithmic bytes per round
+    # of the scorer (the byte model of the workload table): the CSR pattern
+    # read once, 4 (R + 1) + 4 nnz, plus the (row, segment) group bitmap
+    # written and read, 2 B per nonzero group; the scored-pair term (8 M^2 B
+    # per pair) is left out, so this is a lower bound on the bytes.  The
+    # kernel's own work counters (entries gathered, rows touched) give the
+    # second, incremental figure.
     stt = stats_sum
-    alg_bytes = 4.0 * stt["rounds"] * stt["nseg"] + 20.0 * stt["gathered"] + 32.0 * stt["touched"]
+    groups = nonzero_groups(nr, r, c, v, M_NM)
+    bytes_per_round = 4.0 * (nr + 1) + 4.0 * stt["pattern_nnz"] / max(1, args.steps) + 2.0 * groups
+    alg_bytes = stt["rounds"] * bytes_per_round
+    inc_bytes = (4.0 * stt["rounds"] * stt["nseg"] / max(1, args.steps) + 20.0 * stt["gathered"] +
+                 32.0 * stt["touched"])
     peak, peak_kind = load_peaks()
-    achieved = alg_bytes / (tot["rounds_kernel_ms"] / 1000.0) / 1e9 if tot["rounds_kernel_ms"] > 0 else 0.0
+    kt = tot["rounds_kernel_ms"] / 1000.0
+    achieved = alg_bytes / kt / 1e9 if kt > 0 else 0.0
     tflops_peak, tkind = load_tensor_peak()
     issued = 2.0 * 128 * 16 * N_B * info["ksteps"]
     useful = 2.0 * nnz * N_B
     sk = tot["spmm_kernel_ms"] / args.steps / 1000.0
+    spmm_bytes = spmm_hbm_bytes(nr, nnz, N_B)
+    # parity at this size: the GPU search against the oracle's committed
+    # results (all four schedules' result integers, the winner and its
+    # permutation), the input checked by its SHA-256 first
+    parity = {}
+    gold = scale_golden("c2")
+    if gold is not None and rank == 0:
+        same_input = coo_digest(nr, r, c, v) == gold["sha256"]
+        parity["c2_vs_oracle_goldens"] = bool(same_input and np.array_equal(t["res4"], gold["res5x4"]) and
+                                              best == gold["best"] and
+                                              np.array_equal(newpos, gold["newpos4"][gold["best"]]))
     out = {
-        "metric": METRIC, "value": value, "unit": "hot-path steps/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+        "metric": METRIC, "value": value, "unit": "hot-path steps/s", "value_is": VALUE_IS, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32 (reorder), bf16 x bf16 -> fp32 (SpMM)",
         "data": "synthetic (seeded R-MAT, seed = rank; B ~ N(0,1))",
         "config": {"workload": WORKLOAD, "nrows": nr, "nnz": nnz, "N": N_NM, "M": M_NM, "V": V, "n_B": N_B,
@@ -376,11 +591,19 @@ def run_ours(args, rank, world, local):
                 "ms_per_step": 1000.0 * e2e_t / args.steps},
         "roofline": {"kernel": "k_nm_rounds<4>", "bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "bytes_model": "per round 4(R+1) + 4 nnz (CSR pattern) + 2 B per nonzero (row, segment) "
+                                    "group; %d groups" % groups,
                      # dram__bytes_read.sum + dram__bytes_write.sum of one launch, from the ncu
                      # capture summarised in profiles/k_nm_rounds_c2_rmat16384_m4.md
                      "traffic": 2.04e6, "traffic_unit": "bytes per launch",
+                     "traffic_source": "profiles/k_nm_rounds_c2_rmat16384_m4.md",
                      "alg_bytes_per_launch": alg_bytes / args.steps,
                      "kernel_ms_per_launch": tot["rounds_kernel_ms"] / args.steps,
+                     # the launch's time over the mean rounds of its (concurrent) jobs
+                     "us_per_round": 1000.0 * tot["rounds_kernel_ms"] / max(1.0, stt["rounds"] / max(1, stt["jobs"])) /
+                     max(1, args.steps),
+                     "incremental_bytes_per_launch": inc_bytes / args.steps,
+                     "incremental_frac": inc_bytes / kt / 1e9 / peak if kt > 0 else 0.0,
                      "note": "latency-bound sequential greedy (4 jobs x cluster of %d blocks); see profiles/"
                              % int(t["stats"]["blocks_per_job"]),
                      "round_phase_share": {k: round(vv / max(1, sum(phase_sum.values())), 4)
@@ -389,23 +612,49 @@ def run_ours(args, rank, world, local):
                  "useful_tflops": useful / sk / 1e12,
                  "issued_tflops": issued / sk / 1e12, "bound": "tensor", "peak_tflops": tflops_peak,
                  "peak_kind": tkind, "issued_frac": issued / sk / 1e12 / tflops_peak,
-                 "max_rel_err_vs_fp64": spmm_err, "slices": info["slices"], "ksteps": info["ksteps"],
+                 "hbm": {"alg_bytes": spmm_bytes, "achieved_gbs": spmm_bytes / sk / 1e9, "peak": peak,
+                         "frac": spmm_bytes / sk / 1e9 / peak, "peak_kind": peak_kind,
+                         "bytes_model": "A as CSR (2 B value + 4 B column per nonzero, row pointers), B read "
+                                        "once, C (fp32) written once"},
+                 "max_rel_err_vs_fp64_per_row": spmm_err, "max_rel_err_vs_fp64_normwise": spmm_err_norm,
+                 "slices": info["slices"], "ksteps": info["ksteps"],
                  "blocks": info["blocks"], "valid_blocks": info["valid_blocks"]},
+        "parity": parity,
         "gpu_launches": launches,
         "clocks": clk,
         "wall_ms_per_step": 1000.0 * wall / args.steps,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = host_threads()
-        dt, cbest = cpu_port_find_best(nr, r, c, v, threads)
+        dt, cbest, ores = cpu_port_find_best(nr, r, c, v, threads)
         out["cpu_baseline"] = {"value": 1.0 / dt, "unit": "hot-path steps/s", "cores": threads, "kind": "port",
                                "sample": "one full find_best_2toX of the same matrix (C++ restatement of the "
                                          "reference NM path, OpenMP); the SpMM part is not included",
                                "best_sched": int(cbest)}
-        out["cpu_baseline_agrees"] = bool(cbest == best)
+        # the same port on one thread, on a bounded sample: the winning
+        # schedule alone (a quarter of find_best_2toX)
+        dt1 = cpu_port_one_schedule(nr, r, c, v, int(cbest), 1)
+        out["cpu_baseline"]["one_thread"] = {"seconds_one_schedule": dt1, "cores": 1,
+                                             "sample": "schedule %d of find_best_2toX on one thread" % int(cbest)}
+        # live parity against the oracle run here: all four schedules' result
+        # integers, the winner, and the winner's permutation
+        _, _, _, opos = oracle_nm_run(nr, r, c, v, int(cbest))
+        parity["c2_vs_oracle_live"] = bool(cbest == best and np.array_equal(ores, t["res4"]) and
+                                           np.array_equal(opos, newpos))
+        out["cpu_baseline_agrees"] = parity["c2_vs_oracle_live"]
+    if rank == 0 and world == 1 and not args.no_extended:
+        try:
+            out["baselines_c2_spmm"] = library_spmm_baselines(nr, newpos[r], newpos[c], v, N_B, torch.bfloat16)
+            ours = tot["spmm_kernel_ms"] / args.steps
+            for k, d in out["baselines_c2_spmm"].items():
+                if "ms" in d:
+                    d["vnm_kernel_speedup"] = d["ms"] / ours
+        except Exception as e:
+            out["baselines_c2_spmm"] = {"error": "%s: %s" % (type(e).__name__, e)}
     if rank == 0 and world == 1 and not args.no_extended:
         # the other configurations, untimed by the headline (one GPU, after it)
-        for key, fn in (("c3_batch", bench_batch_c3), ("c4_learned", bench_learned_c4), ("c5_gcn", bench_gcn_c5)):
+        for key, fn in (("c3_batch", bench_batch_c3), ("c4_learned", bench_learned_c4), ("c5_gcn", bench_gcn_c5),
+                        ("s1_structured_spmm", bench_structured_spmm)):
             try:
                 out[key] = fn(ctx)
             except Exception as e:  # report, keep the headline line
@@ -445,8 +694,20 @@ def bench_batch_c3(ctx, reps=3):
         loop_wall += 1000.0 * (time.perf_counter() - t0)
         loop_ms += ctx.last_kernel_ms
         same = same and np.array_equal(res, res_b[b]) and np.array_equal(pos, pos_b[b])
+    # three members (the smallest, a middle one, the largest) against the
+    # oracle run here, outside the timed runs
+    sizes = np.array([m[0] for m in mats])
+    order = np.argsort(sizes, kind="stable")
+    checked = {}
+    for b in (int(order[0]), int(order[len(order) // 2]), int(order[-1])):
+        n, r, c, v = mats[b]
+        ores, _, _, opos = oracle_nm_run(n, r, c, v, 0, N=2, M=M)
+        checked[str(b)] = {"nrows": int(n), "same_as_oracle": bool(np.array_equal(res_b[b], ores) and
+                                                                   np.array_equal(pos_b[b], opos))}
     return {"workload": "C3: 256 R-MAT matrices, rows log-uniform [256, 8192], degree U[4,32], U[-1,1], 2:8, "
                         "schedule 0, nm_maxiter 10",
+            "members_vs_oracle": checked,
+            "parity_members_vs_oracle": all(x["same_as_oracle"] for x in checked.values()),
             "matrices": len(mats), "nnz_total": int(nnz), "rows_total": int(sum(m[0] for m in mats)),
             "batched_device_ms": _median(bt), "batched_wall_ms": _median(bw),
             "per_matrix_device_ms_sum": loop_ms, "per_matrix_wall_ms_sum": loop_wall,
@@ -474,10 +735,16 @@ def bench_learned_c4(ctx, reps=3):
     o = np.lexsort((pc, pr))
     pl, _, _ = vnm_gb300.nm_learned(ctx, n, pr[o], pc[o], v[o], N, M, mode=vnm_gb300.LEARNED_RANDOM, max_rounds=0)
     target = pl["init_retained"] - ret0
+    gold = scale_golden("c4")
+    parity = None
+    if gold is not None:
+        parity = bool(coo_digest(n, r, c, v) == gold["sha256"] and np.array_equal(res4, gold["res5x4"]) and
+                      best == gold["best"] and np.array_equal(newpos, gold["newpos4"][gold["best"]]))
     out = {"workload": "C4: R-MAT 65536x65536, 1048576 edges symmetrised (%d entries), N(0,1), 2:8" % len(r),
            "plain": {"what": "find_best_2toX, 4 schedules, bit-exact with the reference", "wall_ms": plain_wall,
                      "device_ms": plain_dev, "best_sched": int(best), "retained": int(pl["init_retained"]),
                      "invalid_groups": int(pl["init_invalid"]), "retained_gain": int(target)},
+           "parity_plain_vs_oracle_goldens": parity,
            "init_retained": int(ret0)}
     modes = (("network_top8", vnm_gb300.LEARNED_MLP, 8), ("network_top1", vnm_gb300.LEARNED_MLP, 1),
              ("random_top8", vnm_gb300.LEARNED_RANDOM, 8), ("exhaustive", vnm_gb300.LEARNED_EXHAUSTIVE, 8))
@@ -513,6 +780,19 @@ def bench_learned_c4(ctx, reps=3):
     out["inputs_in_hbm"] = {"plain_device_ms": _median(dev_plain), "network_top8_to_plain_device_ms": _median(dev_net),
                             "speedup": _median(dev_plain) / _median(dev_net)}
     out["retained_converged_vs_plain"] = out["network_top8"]["converged"]["retained"] / max(1, pl["init_retained"])
+    # the V:N:M retained-nnz at V=128 (per V-block and segment the 4 columns
+    # with the most nonzeros kept, then per row at most N of them), counted
+    # by the oracle on the input, the plain result and the learned result
+    res, pos, _ = vnm_gb300.nm_learned(ctx, n, r, c, v, N, M, mode=vnm_gb300.LEARNED_MLP, net=net, topk=8,
+                                       targets=TARGETS, max_rounds=64, patience=3, seed=1)
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    Vc = 128
+    out["vnm_retained_v128"] = {"input": int(oracle.retained_vnm(n, r, c, v, N, M, Vc)),
+                                "plain": int(oracle.retained_vnm(n, newpos[r], newpos[c], v, N, M, Vc)),
+                                "network_top8_converged": int(oracle.retained_vnm(n, pos[r], pos[c], v, N, M, Vc)),
+                                "nnz": int(len(r))}
+    out["hybrid_maxiter30"] = hybrid_cli(n, r, c, v, N, M, Vc, 30)
     X = np.random.default_rng(0).normal(0, 1, (1 << 20, 32)).astype(np.float32)
     ms = []
     for _ in range(4):
@@ -525,6 +805,31 @@ def bench_learned_c4(ctx, reps=3):
                             "frac_of_bf16_peak": fl / _median(ms[1:]) / 1e9 / tpk, "peak_kind": tkind}
     net.close()
     return out
+
+
+def hybrid_cli(n, r, c, v, N, M, Vc, maxiter):
+    """The drop-in `spmm` command (find_best_2toX, then maxiter rounds of the
+    VNM stage and the NM reorder, main.cu:195-337) on a matrix written as a
+    Matrix Market file: its own CSV line (field 16 is the hybrid loop's
+    milliseconds, timed as the reference times it) and the process's wall
+    time including the file read and write."""
+    import tempfile
+    from vnm_gb300 import synth
+    exe = os.path.join(PKG, "spmm")
+    with tempfile.TemporaryDirectory() as td:
+        mtx = os.path.join(td, "in.mtx")
+        synth.write_mtx(mtx, n, r, c, v)
+        t0 = time.perf_counter()
+        p = subprocess.run([exe, "--mtxfile", mtx, "--outmtxfile", os.path.join(td, "out.mtx"), "--maxiter",
+                            str(maxiter), "--n", "64", "--sched", "0", "--v", str(Vc), "--N", str(N), "--M", str(M)],
+                           cwd=td, capture_output=True, text=True, timeout=1200)
+        wall = time.perf_counter() - t0
+    if p.returncode != 0:
+        return {"error": p.stderr[-500:]}
+    f = [float(x) for x in p.stdout.strip().split(",")]
+    return {"what": "spmm command, --maxiter %d --v %d, %d:%d" % (maxiter, Vc, N, M), "hybrid_ms": f[15],
+            "process_wall_s": wall, "init_cnt": f[5], "final_cnt": f[6], "init_vblocks": f[8], "final_vblocks": f[9],
+            "nm_rounds": f[12], "vnm_rounds": f[13]}
 
 
 def bench_gcn_c5(ctx, reps=100):
@@ -544,6 +849,19 @@ def bench_gcn_c5(ctx, reps=100):
                                           targets=TARGETS, max_rounds=64, patience=3, seed=1)
     reorder_wall = 1000.0 * (time.perf_counter() - t0)
     reorder_dev = ctx.last_kernel_ms
+    # the same search with random proposals and with every candidate scored
+    # exactly, to convergence: what the network buys on this graph
+    modes = {"network_top8": {"wall_ms": reorder_wall, "device_ms": reorder_dev, "rounds": res["rounds"],
+                              "final_invalid": int(res["final_invalid"]),
+                              "final_retained": int(res["final_retained"]),
+                              "exact_scored": int(res["exact_scored"])}}
+    for name, mode in (("random_top8", vnm_gb300.LEARNED_RANDOM), ("exhaustive", vnm_gb300.LEARNED_EXHAUSTIVE)):
+        t1 = time.perf_counter()
+        rm, _, _ = vnm_gb300.nm_learned(ctx, n, r, c, v, N, M, mode=mode, topk=8, targets=TARGETS, max_rounds=64,
+                                        patience=3, seed=1, want_newpos=False)
+        modes[name] = {"wall_ms": 1000.0 * (time.perf_counter() - t1), "device_ms": ctx.last_kernel_ms,
+                       "rounds": rm["rounds"], "final_invalid": int(rm["final_invalid"]),
+                       "final_retained": int(rm["final_retained"]), "exact_scored": int(rm["exact_scored"])}
     net.close()
     pr, pc = ctx.permute_coo(n, r, c, newpos)
     dev = torch.device("cuda", torch.cuda.current_device())
@@ -555,7 +873,8 @@ def bench_gcn_c5(ctx, reps=100):
            "reorder": {"mode": "network top8", "wall_ms": reorder_wall, "device_ms": reorder_dev,
                        "rounds": res["rounds"], "init_retained": int(res["init_retained"]),
                        "final_retained": int(res["final_retained"]), "init_invalid": int(res["init_invalid"]),
-                       "final_invalid": int(res["final_invalid"])}}
+                       "final_invalid": int(res["final_invalid"])},
+           "reorder_modes_converged": modes}
     for dt, tdt in (("bf16", torch.bfloat16), ("fp16", torch.float16)):
         A = vnm_gb300.SpmmMatrix(ctx, n, tr, tc, tv, M, Vc, dt)
         comp_ms = ctx.last_kernel_ms
@@ -576,19 +895,132 @@ def bench_gcn_c5(ctx, reps=100):
         # error against the FP64 oracle on the same (rounded) X
         ref = oracle.spmm_f64(n, pr, pc, v.astype(np.float64), X32.to(tdt).float().numpy().astype(np.float64))
         Ch = C.cpu().numpy().astype(np.float64)
-        err = float(np.abs(Ch - ref).max() / np.abs(ref).max())
+        err = oracle.rowwise_rel_err(Ch, ref)
+        err_norm = float(np.abs(Ch - ref).max() / np.abs(ref).max())
         del ref
         useful = 2.0 * len(r) * nB
         issued = 2.0 * 128 * 16 * nB * info["ksteps"]
         sk = kms / reps / 1000.0
-        tpk, tkind = load_tensor_peak()
+        tpk, tkind = load_tensor_peak(sustained=True)  # 100 calls back to back: about half a second
+        hpk, hkind = load_peaks()
+        hb = spmm_hbm_bytes(n, len(r), nB)
         out["spmm_" + dt] = {"runs": reps, "total_ms": total_ms, "kernel_ms_per_run": kms / reps,
                              "compress_ms": comp_ms, "useful_tflops": useful / sk / 1e12,
                              "issued_tflops": issued / sk / 1e12, "issued_frac": issued / sk / 1e12 / tpk,
-                             "peak_kind": tkind, "max_rel_err_vs_fp64": err, "ksteps": info["ksteps"],
+                             "peak_kind": tkind,
+                             "hbm": {"alg_bytes": hb, "achieved_gbs": hb / sk / 1e9, "frac": hb / sk / 1e9 / hpk,
+                                     "peak": hpk, "peak_kind": hkind},
+                             "max_rel_err_vs_fp64_per_row": err,
+                             "max_rel_err_vs_fp64_normwise": err_norm, "ksteps": info["ksteps"],
                              "slices": info["slices"], "valid_blocks": info["valid_blocks"]}
         A.close()
+    try:
+        out["baselines_spmm"] = library_spmm_baselines(n, pr, pc, v, nB, torch.bfloat16, dense=False)
+        ours = out["spmm_bf16"]["kernel_ms_per_run"]
+        for k, d in out["baselines_spmm"].items():
+            if "ms" in d:
+                d["vnm_kernel_speedup"] = d["ms"] / ours
+    except Exception as e:
+        out["baselines_spmm"] = {"error": "%s: %s" % (type(e).__name__, e)}
     return out
+
+
+def bench_structured_spmm(ctx, reps=20):
+    """The operand V:N:M is made for: a 19456 x 19456 matrix (152 row tiles
+    of 128, one per SM) already in full V:2:8 form with V=128 (density 1/4,
+    94.6 M nonzeros), times B 19456 x 256 BF16 -- all on the tensor cores.
+    Beside it: the same product on the CUDA-core residual path, cuSPARSE CSR
+    and a dense cuBLAS GEMM of the densified matrix.  Error per row against
+    float64 on 1024 sampled rows."""
+    import torch
+    import vnm_gb300
+    from vnm_gb300 import synth
+    R, M, Vs, nB = 19456, 8, 128, 256
+    n, r, c, v = synth.vnm_structured(R, M, Vs, seed=3)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    tr, tc, tv = (torch.from_numpy(x).to(dev) for x in (r, c, v))
+    g = torch.Generator().manual_seed(11)
+    X = torch.randn((n, nB), generator=g).to(torch.bfloat16)
+    Xd = X.to(dev)
+    C = torch.empty((n, nB), dtype=torch.float32, device=dev)
+    tpk, tkind = load_tensor_peak()
+    hpk, hkind = load_peaks()
+    out = {"workload": "S1: 19456x19456 in full V:2:8 form (V=128, every block 4 columns x 2 nonzeros a row; "
+                       "%d nonzeros), B 19456x256 bf16 N(0,1)" % len(r)}
+    rows = np.sort(np.random.default_rng(5).choice(n, 1024, replace=False))
+    ptr = np.searchsorted(r, np.arange(n + 1))
+    Xf = X.float().numpy().astype(np.float64)
+    ref = np.stack([(v[ptr[i]:ptr[i + 1]].astype(np.float64)[:, None] * Xf[c[ptr[i]:ptr[i + 1]]]).sum(0) for i in rows])
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    for label, dm in (("tensor_cores", None), ("cuda_core_residual", 1 << 30)):
+        old = os.environ.get("VNM_SPMM_DENSE_MIN")
+        if dm is None:
+            os.environ.pop("VNM_SPMM_DENSE_MIN", None)
+        else:
+            os.environ["VNM_SPMM_DENSE_MIN"] = str(dm)
+        try:
+            A = vnm_gb300.SpmmMatrix(ctx, n, tr, tc, tv, M, Vs, "bf16")
+        finally:
+            if old is None:
+                os.environ.pop("VNM_SPMM_DENSE_MIN", None)
+            else:
+                os.environ["VNM_SPMM_DENSE_MIN"] = old
+        info = A.info()
+        A.run(Xd, C)
+        A.run(Xd, C)
+        ms = []
+        for _ in range(reps):
+            A.run(Xd, C)
+            ms.append(ctx.last_main_kernel_ms)
+        k = _median(ms)
+        useful = 2.0 * len(r) * nB
+        issued = 2.0 * 128 * 16 * nB * info["ksteps"]
+        hb = info["a_bytes"] + info["residual_nnz"] * 8 + n * nB * 2 + n * nB * 4
+        err = oracle.rowwise_rel_err(C[torch.from_numpy(rows).to(dev)].cpu().numpy(), ref)
+        out[label] = {"kernel_ms": k, "useful_tflops": useful / k / 1e9, "issued_tflops": issued / k / 1e9,
+                      "issued_frac": issued / k / 1e9 / tpk, "peak_kind": tkind,
+                      "hbm": {"bytes": hb, "achieved_gbs": hb / k / 1e6, "frac": hb / k / 1e6 / hpk,
+                              "what": "A as stored (tiles, or 8 B per residual nonzero) + B + C once"},
+                      "max_rel_err_vs_fp64_per_row_sampled": err, "ksteps": info["ksteps"],
+                      "residual_nnz": info["residual_nnz"], "tensor_tiles": info["tensor_tiles"]}
+        A.close()
+    try:
+        out["baselines"] = library_spmm_baselines(n, r, c, v, nB, torch.bfloat16, dense=True, reps=10)
+        for kk, d in out["baselines"].items():
+            if "ms" in d:
+                d["vnm_tensor_speedup"] = d["ms"] / out["tensor_cores"]["kernel_ms"]
+    except Exception as e:
+        out["baselines"] = {"error": "%s: %s" % (type(e).__name__, e)}
+    del tr, tc, tv, Xd, C
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_s1_spmm_only(steps):
+    """The structured V:2:8 operand of bench_structured_spmm through the
+    tensor-core SpMM alone, `steps` calls."""
+    import torch
+    import vnm_gb300
+    from vnm_gb300 import synth
+    R, M, Vs, nB = 19456, 8, 128, 256
+    n, r, c, v = synth.vnm_structured(R, M, Vs, seed=3)
+    dev = torch.device("cuda", 0)
+    with vnm_gb300.Context(0) as ctx:
+        tr, tc, tv = (torch.from_numpy(x).to(dev) for x in (r, c, v))
+        A = vnm_gb300.SpmmMatrix(ctx, n, tr, tc, tv, M, Vs, "bf16")
+        X = torch.randn((n, nB), generator=torch.Generator().manual_seed(11)).to(torch.bfloat16).to(dev)
+        C = torch.empty((n, nB), dtype=torch.float32, device=dev)
+        ms = []
+        for _ in range(max(steps, 1)):
+            A.run(X, C)
+            ms.append(ctx.last_main_kernel_ms)
+        info = A.info()
+        A.close()
+    best = min(ms)
+    return {"workload": "S1 SpMM only: 19456x19456 full V:2:8 (V=128), B 19456x256 bf16", "runs": len(ms),
+            "kernel_ms_min": best, "issued_tflops": 2.0 * 128 * 16 * nB * info["ksteps"] / (best * 1e-3) / 1e12,
+            "useful_tflops": 2.0 * len(r) * nB / (best * 1e-3) / 1e12, "info": info}
 
 
 def run_c5_spmm_only(steps):
@@ -623,7 +1055,7 @@ def run_c5_spmm_only(steps):
     best = min(ms)
     return {"workload": "C5 SpMM only: Chung-Lu 262144, learned reorder 2:8, V=128, X 262144x256 bf16",
             "runs": len(ms), "kernel_ms_min": best, "kernel_ms_median": sorted(ms)[len(ms) // 2],
-            "issued_tflops": 2.0 * 128 * 16 * nB * info["ksteps"] / (best * 1e-3) / 1e12, "ksteps": info["ksteps"]}
+            "issued_tflops": 2.0 * 128 * 16 * nB * info["ksteps"] / (best * 1e-3) / 1e12, "info": info}
 
 
 def main():
@@ -631,6 +1063,9 @@ def main():
     rank, world, local = dist_env()
     if args.c5_spmm_only:
         print(json.dumps(run_c5_spmm_only(args.steps)))
+        return
+    if args.s1_spmm_only:
+        print(json.dumps(run_s1_spmm_only(args.steps)))
         return
     if args.impl == "reference":
         run_reference(args, rank, world)
