@@ -77,8 +77,9 @@ float vnm_last_main_kernel_ms(const vnm_ctx* ctx);
  * job (the cluster size the launch used), out[7] rounds whose row records
  * were in shared-memory tables (summed over jobs), out[8..14] kilocycles
  * spent per round phase (select, choose, gather, process, heap entries,
- * swap heaps and walk overlapped, apply) summed over jobs.  n <= 16
- * values. */
+ * swap heaps and walk overlapped, apply) summed over jobs, out[15] rounds
+ * whose tables ran out of slots and gathered into global memory instead.
+ * n <= 16 values. */
 vnm_status vnm_last_stats(const vnm_ctx* ctx, long long* out, int n);
 
 /* ---------------------------------------------------------------------------

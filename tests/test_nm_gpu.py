@@ -205,3 +205,35 @@ def test_other_group_sizes_match_oracle(ctx, M):
             os.environ.pop("VNM_NM_CLUSTER", None)
         else:
             os.environ["VNM_NM_CLUSTER"] = old
+
+
+def test_table_overflow_falls_back_to_global_records(ctx):
+    """With VNM_NM_CLUSTER_TABLE=1 cluster jobs keep a round's row records in
+    the blocks' shared-memory tables, row r in block r % 16.  Here the only invalid segment touches
+    4608 rows that are all multiples of 16, more than block 0's 4096 slots:
+    that block's table overflows, the round gathers into global memory
+    instead, and the result is still the oracle's."""
+    import os
+    R = 81920
+    rows = np.arange(4608, dtype=np.int64) * 16
+    r = np.concatenate([np.repeat(rows, 3), rows])
+    c = np.concatenate([np.tile([0, 1, 2], len(rows)), np.full(len(rows), 5)])  # three nodes of segment 0, one of 1
+    key = np.unique(r * R + c)
+    r, c = (key // R).astype(np.int32), (key % R).astype(np.int32)
+    v = np.ones(len(r), np.float32)
+    ores, _, _, opos = oracle.nm_run(R, r, c, v, 2, 4, 0)
+    old = {k: os.environ.get(k) for k in ("VNM_NM_CLUSTER", "VNM_NM_CLUSTER_TABLE")}
+    try:
+        os.environ["VNM_NM_CLUSTER"] = "16"
+        os.environ["VNM_NM_CLUSTER_TABLE"] = "1"
+        res, newpos = ctx.nm_reorder(R, r, c, v, 2, 4, 0)
+        st = ctx.last_stats()
+        assert st["blocks_per_job"] == 16
+        assert st["table_fallback_rounds"] > 0, st
+        assert np.array_equal(res, ores) and np.array_equal(newpos, opos)
+    finally:
+        for k, v0 in old.items():
+            if v0 is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v0

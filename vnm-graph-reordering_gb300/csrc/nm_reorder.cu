@@ -200,6 +200,10 @@ struct RoundSmem {
   int ts_max;       // slots of `table` (a power of two) or 0
   int ts_shift;     // 32 - log2(ts_max)
   int use_table;    // this round's records are in `table` (else in J.rec)
+  int* tlist;       // the slots of `table` claimed this round, densely (ts_max entries)
+  int tcount;       // how many
+  int tover;        // a block's table ran out of slots this round (the leader's copy is read)
+  int tfall;        // ... so this round gathers into global memory after all
   int status;
   int nswaps;
   int hprog[K * K];  // pops of each ordered pair's heap written to ord so far
@@ -518,12 +522,14 @@ __device__ void clear_round_smem(RoundSmem<M>& sm) {
   if (threadIdx.x == 0) {
     sm.ntouched = 0;
     sm.nswaps = 0;
+    sm.tover = 0;
   }
 }
 
 // OR the bitmaps of the round's segments into per-row records.
 template <int M>
-__device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J, Slice sl = Slice{0, 1}, int* ntp = nullptr) {
+__device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J, Slice sl = Slice{0, 1}, int* ntp = nullptr,
+                             bool force_global = false) {
   constexpr int K = M + 1;
   const int tid = threadIdx.x;
   if (!ntp) ntp = &sm.ntouched;
@@ -559,20 +565,28 @@ __device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J, Slice sl = Slice{
     if (tid == 31) {
       sm.colpre[KM] = incl;
       sm.E = incl;
-      sm.use_table = sm.ts_max > 0 && incl <= (sm.ts_max >> 2) * 3;
+      // a single block's table takes the round when it can hold every row
+      // (E <= 3/4 of it); a cluster's tables when the expected load of
+      // each is at most half (rows are dealt by row % cs), with the
+      // overflow fallback of the round loop behind it
+      sm.use_table = !force_global && sm.ts_max > 0 &&
+                     (sl.cs == 1 ? incl <= (sm.ts_max >> 2) * 3 : incl <= (sm.ts_max >> 1) * sl.cs);
     }
   }
   __syncthreads();
   const int E = sm.E;
   if (sm.use_table) {
     // open addressing, linear probing; a slot is claimed by CAS on its row
-    // key.  In a cluster, row r's record lives in the table of block
-    // r % cs (reached over DSMEM), so each block later processes and clears
-    // the rows it owns from its own shared memory; the entries are dealt
-    // over every thread of the cluster.  The round uses the tables only
-    // when E <= 3/4 of a table, so a block's table holds every row of the
-    // round even if all of them are its own.
+    // key and appended to its table's list of claimed slots, which the
+    // process and apply phases walk in full 32-row chunks.  In a cluster,
+    // row r's record lives in the table of block r % cs (reached over
+    // DSMEM), so each block later processes and clears the rows it owns
+    // from its own shared memory; the entries are dealt over every thread
+    // of the cluster.  A cluster entry that finds no free slot within 64
+    // probes raises the leader's overflow flag instead (the round loop then
+    // redoes the gather into global memory).
     const unsigned mask = (unsigned)sm.ts_max - 1u;
+    const int plim = sl.cs > 1 ? 64 : (int)mask + 1;
     const int gthreads = sl.cs * NM_THREADS;
     for (int e = sl.rank * NM_THREADS + tid; e < E; e += gthreads) {
       int lo = 0, hi = KM - 1;
@@ -585,17 +599,31 @@ __device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J, Slice sl = Slice{
       const int row = J.crow[sm.colstart[q] + (e - sm.colpre[q])];
       const unsigned key = (unsigned)row + 1u;
       unsigned* tw = reinterpret_cast<unsigned*>(sm.table);
-      if (sl.cs > 1) tw = cg::this_cluster().map_shared_rank(tw, (unsigned)(row % sl.cs));
+      int* tl = sm.tlist;
+      int* tc = &sm.tcount;
+      if (sl.cs > 1) {
+        cg::cluster_group cl = cg::this_cluster();
+        const unsigned owner = (unsigned)(row % sl.cs);
+        tw = cl.map_shared_rank(tw, owner);
+        tl = cl.map_shared_rank(tl, owner);
+        tc = cl.map_shared_rank(tc, owner);
+      }
       unsigned h = (key * 2654435761u) >> sm.ts_shift;
-      for (int probe = 0; probe <= (int)mask; ++probe) {
+      bool placed = false;
+      for (int probe = 0; probe < plim; ++probe) {
         const unsigned cur = atomicCAS(&tw[4 * h + 3], 0u, key);
         if (cur == 0u || cur == key) {
           atomicOr(&tw[4 * h + (xi >> 2)], (1u << k) << ((xi & 3) * 8));
-          if (cur == 0u) atomicAdd(ntp, 1);
+          if (cur == 0u) {
+            tl[atomicAdd(tc, 1)] = (int)h;
+            atomicAdd(ntp, 1);
+          }
+          placed = true;
           break;
         }
         h = (h + 1u) & mask;
       }
+      if (!placed) atomicOr(cg::this_cluster().map_shared_rank(&sm.tover, 0), 1);
     }
     __syncthreads();
     return;
@@ -682,13 +710,15 @@ __device__ __forceinline__ void for_touched_warp(const RoundSmem<M>& sm, const N
 // touched rows (index = row).  Warp-uniform like for_touched_warp.
 template <int M, class F>
 __device__ __forceinline__ void for_rows_warp(const RoundSmem<M>& sm, const NMJob& J, Slice sl, F&& f) {
-  if (sm.use_table) {  // the rows this block's table holds
+  if (sm.use_table) {  // the rows this block's table holds, from its list of claimed slots
     constexpr int NW = NM_THREADS / 32;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int base = w * 32; base < sm.ts_max; base += NW * 32) {
-      const int slot = base + lane;
-      const uint4 v = sm.table[slot];
-      if (__ballot_sync(FULL, v.w != 0u) != 0u) f(slot, v, v.w != 0u);  // f is a no-op on empty slots
+    const int n = sm.tcount;
+    for (int base = w * 32; base < n; base += NW * 32) {
+      const int i = base + lane;
+      const int slot = i < n ? sm.tlist[i] : 0;
+      const uint4 v = i < n ? sm.table[slot] : make_uint4(0u, 0u, 0u, 0u);
+      f(slot, v, i < n);
     }
   } else {
     for_touched_warp<M>(sm, J, sl, f);
@@ -1227,6 +1257,7 @@ __device__ void apply_recount(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl)
     }
   });
   __syncthreads();
+  if (threadIdx.x == 0) sm.tcount = 0;  // the table is empty again (before the next round's inserts)
 }
 
 // The new counts of the round's segments (leader block).
@@ -1268,10 +1299,12 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
   static_assert(offsetof(RoundSmem<M>, newpres) == offsetof(RoundSmem<M>, newinv) + sizeof(int) * K,
                 "newinv, newpres adjacent");
   constexpr int NSUM = K * M + 2 * RoundSmem<M>::NPAIR * RoundSmem<M>::MM;
-  // dynamic shared memory: [heap scratch][row-record table: ts_max x 16 B][segment counts]
+  // dynamic shared memory: [heap scratch][row-record table: ts_max x 16 B]
+  // [claimed-slot list: ts_max x 4 B][segment counts]
   extern __shared__ uint4 smem_heap[];
   uint4* smem_dyn = smem_heap + RoundSmem<M>::SCR_U4;
-  int* smem_cnt = reinterpret_cast<int*>(smem_dyn + ts_max);
+  int* smem_list = reinterpret_cast<int*>(smem_dyn + ts_max);
+  int* smem_cnt = smem_list + ts_max;
   cg::cluster_group cl = cg::this_cluster();
   const int rank = cs > 1 ? (int)cl.block_rank() : 0;
   const bool lead = rank == 0;
@@ -1285,6 +1318,9 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
   if (tid == 0) {
     sm.status = JOB_OK;
     sm.table = ts_max > 0 ? smem_dyn : nullptr;
+    sm.tlist = ts_max > 0 ? smem_list : nullptr;
+    sm.tcount = 0;
+    sm.tfall = 0;
     sm.ts_max = ts_max;
     sm.ts_shift = 32 - (31 - __clz(ts_max > 0 ? ts_max : 1));
     sm.use_table = 0;
@@ -1299,6 +1335,7 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
   int committed = 0;
   unsigned long long sumE = 0, sumT = 0;
   int table_rounds = 0;  // rounds whose row records were in shared-memory tables
+  int fallback_rounds = 0;  // rounds whose tables overflowed and gathered into global memory
   // cycles spent in each phase of a round, measured by thread 0 of the
   // leader at the barriers that end the phases: select, choose, gather,
   // process, heap, walk, apply
@@ -1345,11 +1382,30 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
       clear_round_smem<M>(sm);
       __syncthreads();
     }
-    gather_phase<M>(sm, J, sl, lead ? &sm.ntouched : cl.map_shared_rank(&sm.ntouched, 0));
+    int* ntp = lead ? &sm.ntouched : cl.map_shared_rank(&sm.ntouched, 0);
+    gather_phase<M>(sm, J, sl, ntp);
     if (cs > 1) {
       cl.sync();
-      if (!lead && tid == 0) sm.ntouched = *cl.map_shared_rank(&sm.ntouched, 0);
+      if (tid == 0) {
+        if (!lead) sm.ntouched = *cl.map_shared_rank(&sm.ntouched, 0);
+        sm.tfall = sm.use_table && *cl.map_shared_rank(&sm.tover, 0) != 0;
+      }
       __syncthreads();
+      if (sm.tfall) {
+        // a block's table ran out of slots: empty every table and gather
+        // this round's records into global memory instead
+        for (int i = tid; i < sm.ts_max; i += NM_THREADS) sm.table[i] = make_uint4(0u, 0u, 0u, 0u);
+        if (tid == 0) {
+          sm.tcount = 0;
+          if (lead) sm.ntouched = 0;
+        }
+        __syncthreads();
+        cl.sync();
+        gather_phase<M>(sm, J, sl, ntp, true);
+        cl.sync();
+        if (!lead && tid == 0) sm.ntouched = *cl.map_shared_rank(&sm.ntouched, 0);
+        __syncthreads();
+      }
     }
     VNM_PHASE(2);
     process_phase<M>(sm, J, N, sl);
@@ -1383,6 +1439,7 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
       sumE += (unsigned)sm.E;
       sumT += (unsigned)sm.ntouched;
       table_rounds += sm.use_table ? 1 : 0;
+      fallback_rounds += sm.tfall ? 1 : 0;
       // where each bit of the round's segments goes, to every block (one
       // remote word store a thread)
       constexpr int DW = RoundSmem<M>::DEST_W;
@@ -1424,6 +1481,7 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     J.res[9] = (int)(sumT & 0x7fffffffull);
     J.res[10] = (int)(sumT >> 31);
     J.res[11] = table_rounds;
+    J.res[12] = fallback_rounds;
     for (int q = 0; q < 7; ++q) J.res[16 + q] = (int)(tph[q] >> 10);  // kilocycles
   }
 }
@@ -1613,16 +1671,21 @@ static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, 
   const int in_smem = cbytes <= (64u << 10) ? 1 : 0;
   const size_t hbytes = (size_t)RoundSmem<M>::SCR_U4 * sizeof(uint4);
   const size_t fixed = sizeof(RoundSmem<M>) + hbytes + (in_smem ? cbytes : 0);
+  constexpr size_t SLOT = sizeof(uint4) + sizeof(int);  // a table slot and its list entry
   int ts = 8192;
-  while (ts >= 1024 && fixed + (size_t)ts * sizeof(uint4) > NM_SMEM_BUDGET) ts >>= 1;
+  while (ts >= 1024 && fixed + (size_t)ts * SLOT > NM_SMEM_BUDGET) ts >>= 1;
   if (ts < 1024) ts = 0;
-  // cluster jobs keep their round's row records in global memory unless
-  // VNM_NM_CLUSTER_TABLE=1 puts them in every block's shared memory table
+  // Cluster jobs keep the round's row records in global memory (L2) unless
+  // VNM_NM_CLUSTER_TABLE=1 puts them in the blocks' shared-memory tables.
+  // Measured on GB300, R-MAT 16384 2:4 find_best: global 10.59 ms; tables
+  // for rounds of at most 3/4 of a table's slots 10.68, at most 1/8 of the
+  // cluster's slots 10.70, at most 1/2 12.51 -- the DSMEM atomics of the
+  // inserts cost what the process and apply phases gain.
   if (cs > 1) {
     const char* e = getenv("VNM_NM_CLUSTER_TABLE");
     if (!(e && atoi(e) == 1)) ts = 0;
   }
-  const size_t dyn = hbytes + (size_t)ts * sizeof(uint4) + (in_smem ? cbytes : 0);
+  const size_t dyn = hbytes + (size_t)ts * SLOT + (in_smem ? cbytes : 0);
   // static + dynamic shared memory may pass the 48 KB a launch gets without
   // opting in (RoundSmem<8> alone is ~30 KB)
   VNM_CUDA_TRY(cudaFuncSetAttribute(k_nm_rounds<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
@@ -1669,9 +1732,9 @@ static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, 
     }
     // no cluster fits: one block per job, with the shared-memory row table
     ts = 8192;
-    while (ts >= 1024 && fixed + (size_t)ts * sizeof(uint4) > NM_SMEM_BUDGET) ts >>= 1;
+    while (ts >= 1024 && fixed + (size_t)ts * SLOT > NM_SMEM_BUDGET) ts >>= 1;
     if (ts < 1024) ts = 0;
-    const size_t dyn1 = hbytes + (size_t)ts * sizeof(uint4) + (in_smem ? cbytes : 0);
+    const size_t dyn1 = hbytes + (size_t)ts * SLOT + (in_smem ? cbytes : 0);
     VNM_CUDA_TRY(cudaFuncSetAttribute(k_nm_rounds<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn1));
     VNM_LAUNCH(ctx, k_nm_rounds<M>, njobs, NM_THREADS, dyn1, d_jobs, N, in_smem, ts, 1);
     ctx->last_cluster = 1;
@@ -1801,6 +1864,7 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
     ctx->stats[2] += (long long)h[9] + ((long long)h[10] << 31);
     for (int q = 0; q < 7; ++q) ctx->stats[8 + q] += h[16 + q];
     ctx->stats[7] += h[11];
+    ctx->stats[15] += h[12];
   }
   if (trace) {
     const int committed = hres_copy[6];

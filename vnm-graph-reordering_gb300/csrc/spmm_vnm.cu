@@ -73,8 +73,7 @@ struct vnm_spmm_matrix {
   int dense_min = 0;           // blocks with fewer nonzeros went to the residual
   long long nres = 0;          // residual nonzeros
   int ntask = 0, nmulti = 0, nslots = 0;
-  int* rcol = nullptr;         // [nres], row-major
-  float* rval = nullptr;       // [nres]
+  int2* rcv = nullptr;         // [nres], row-major: {column, value bits}
   int4* task = nullptr;        // [ntask] {row, begin, end, partial slot or -1}
   int4* multi = nullptr;       // [nmulti] {row, first slot, chunks, 0}
   void* base = nullptr;        // one allocation for all of the above
@@ -95,6 +94,7 @@ constexpr uint32_t SP_WAIT_LIMIT = 1u << 22;  // polls before a wait gives up
 constexpr int RES_CHUNK = 256;    // residual nonzeros per task, at most
 constexpr int RES_MAXCH = 32;     // chunks of one row, at most
 constexpr int RES_THREADS = 256;
+constexpr int RES_U = 8;          // entries in flight per lane group (8 measured ahead of 4)
 // A block runs on the tensor cores when it holds at least V nonzeros (one
 // a row on average), else on the CUDA cores.  Measured on GB300 with the
 // R-MAT 16384 (V=64, n=128) and Chung-Lu 262144 (V=128, n=256) operands,
@@ -253,11 +253,10 @@ __global__ void k_res_compact(const int* resflag, const int* rpos, const int* ro
     }
 }
 
-__global__ void k_res_gather(const int* src, const int* col, const float* val, int nres, int* rcol, float* rval) {
+__global__ void k_res_gather(const int* src, const int* col, const float* val, int nres, int2* rcv) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nres; i += gridDim.x * blockDim.x) {
     const int e = src[i];
-    rcol[i] = col[e];
-    rval[i] = val[e];
+    rcv[i] = make_int2(col[e], __float_as_int(val[e]));
   }
 }
 
@@ -388,7 +387,18 @@ __global__ void k_cmp_rscale(const unsigned* bmax, int ntiles, int R, int V, flo
 // ---------------------------------------------------------------------------
 // Residual kernels (CUDA cores)
 // ---------------------------------------------------------------------------
-// acc[0..7] += w * the 8 16-bit values in b (element 0 in the low half of b.x)
+// acc[0..7] += w * the 8 16-bit values in b (element 0 in the low half of
+// b.x), as four packed FP32 FMAs (fma.rn.f32x2: two round-to-nearest FP32
+// FMAs, the same results as eight scalar ones in half the instructions).
+__device__ __forceinline__ void fma2(float& a0, float& a1, float w, float x0, float x1) {
+  unsigned long long acc = ((unsigned long long)__float_as_uint(a1) << 32) | __float_as_uint(a0);
+  const unsigned long long ww = ((unsigned long long)__float_as_uint(w) << 32) | __float_as_uint(w);
+  const unsigned long long xx = ((unsigned long long)__float_as_uint(x1) << 32) | __float_as_uint(x0);
+  asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(acc) : "l"(ww), "l"(xx));
+  a0 = __uint_as_float((unsigned)acc);
+  a1 = __uint_as_float((unsigned)(acc >> 32));
+}
+
 template <bool BF16>
 __device__ __forceinline__ void fma8(float (&acc)[8], uint4 b, float w) {
   const uint32_t q[4] = {b.x, b.y, b.z, b.w};
@@ -403,19 +413,19 @@ __device__ __forceinline__ void fma8(float (&acc)[8], uint4 b, float w) {
       lo = f.x;
       hi = f.y;
     }
-    acc[2 * i] = fmaf(w, lo, acc[2 * i]);
-    acc[2 * i + 1] = fmaf(w, hi, acc[2 * i + 1]);
+    fma2(acc[2 * i], acc[2 * i + 1], w, lo, hi);
   }
 }
 
 // One task per group of LW lanes (32 / LW tasks per warp); each lane owns 8
-// consecutive columns of the block's 8 * LW.  The group's lanes load LW
-// (column, value) pairs at a time and broadcast them by shuffle; every lane
-// then gathers its 16 bytes of each B row, four rows in flight.  Loop trip
-// counts are the warp's maximum, so every shuffle has the whole warp.
+// consecutive columns of the block's 8 * LW.  Every lane of a group reads
+// the same (column, value) record (one 8-byte load served once for the
+// group) and gathers its 16 bytes of that B row, RES_U entries in flight.
+// Loop trip counts are the warp's maximum; a group past its end reads a
+// zero weight and a zero row, so the arithmetic needs no predicate.
 template <int LW, bool BF16>
 __global__ void __launch_bounds__(RES_THREADS)
-    k_spmm_res(const int4* __restrict__ task, int ntask, const int* __restrict__ rcol, const float* __restrict__ rval,
+    k_spmm_res(const int4* __restrict__ task, int ntask, const int2* __restrict__ rcv,
                const unsigned char* __restrict__ B, size_t ldb, float* __restrict__ C, int ldc,
                float* __restrict__ P, int ldp) {
   constexpr int G = 32 / LW;
@@ -424,31 +434,27 @@ __global__ void __launch_bounds__(RES_THREADS)
   const int cb = blockIdx.y * (8 * LW) + lid * 8;  // this lane's first column
   const int4 tk = t < ntask ? task[t] : make_int4(0, 0, 0, -1);
   const int len = tk.z - tk.y;
-  const int maxlen = __reduce_max_sync(0xffffffffu, len);
+  const int maxlen = G == 1 ? len : __reduce_max_sync(0xffffffffu, len);
   float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   const unsigned char* bcol = B + (size_t)cb * 2;
-  for (int k0 = 0; k0 < maxlen; k0 += LW) {
-    const bool ok = k0 + lid < len;
-    const int mc = ok ? __ldg(rcol + tk.y + k0 + lid) : 0;
-    const float mv = ok ? __ldg(rval + tk.y + k0 + lid) : 0.f;
-    const int left = len - k0;  // this group's entries from k0 on (may be <= 0)
-    const int qmax = min(LW, maxlen - k0);
-    for (int q = 0; q < qmax; q += 4) {
-      int c[4];
-      float w[4];
-      uint4 b[4];
+  const int2* ent = rcv + tk.y;
+  // the records of the next RES_U entries are loaded one iteration ahead,
+  // so an iteration waits on one global load (the B rows), not two
+  int2 e[RES_U];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        c[u] = __shfl_sync(0xffffffffu, mc, q + u, LW);
-        w[u] = __shfl_sync(0xffffffffu, mv, q + u, LW);
-      }
+  for (int u = 0; u < RES_U; ++u) e[u] = u < len ? __ldg(ent + u) : make_int2(0, 0);
+  for (int k = 0; k < maxlen; k += RES_U) {
+    uint4 b[RES_U];
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
-        b[u] = q + u < left ? __ldg(reinterpret_cast<const uint4*>(bcol + (size_t)c[u] * ldb)) : make_uint4(0, 0, 0, 0);
+    for (int u = 0; u < RES_U; ++u)
+      b[u] = k + u < len ? __ldg(reinterpret_cast<const uint4*>(bcol + (size_t)e[u].x * ldb)) : make_uint4(0, 0, 0, 0);
+    int2 en[RES_U];
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
-        if (q + u < left) fma8<BF16>(acc, b[u], w[u]);
-    }
+    for (int u = 0; u < RES_U; ++u) en[u] = k + RES_U + u < len ? __ldg(ent + k + RES_U + u) : make_int2(0, 0);
+#pragma unroll
+    for (int u = 0; u < RES_U; ++u) fma8<BF16>(acc, b[u], __int_as_float(e[u].y));
+#pragma unroll
+    for (int u = 0; u < RES_U; ++u) e[u] = en[u];
   }
   if (t < ntask) {
     float* dst = tk.w < 0 ? C + (size_t)tk.x * ldc + cb : P + (size_t)tk.w * ldp + cb;
@@ -491,8 +497,11 @@ struct SpmmArgs {
   int* err;
 };
 
-constexpr int SP_STAGES = 8;  // K-steps in flight per CTA
-constexpr int SP_PF = 4;      // pairs of K-steps whose column ids are loaded ahead
+// K-steps in flight per CTA.  16 stages were measured slower on a full
+// V:2:8 operand (19456 rows, n=256: 0.29 vs 0.25 ms): their shared memory
+// leaves one CTA per SM at every column-block width.
+constexpr int SP_STAGES = 8;
+constexpr int SP_PF = 8;      // pairs of K-steps whose column ids are loaded ahead (the ids come from DRAM)
 
 template <int NT>
 struct SpmmSmem {
@@ -544,6 +553,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
       // i + 2q + (l >> 4) for the SP_PF pairs q ahead (coalesced 128-byte
       // loads issued 2*SP_PF steps before use); lane 0 issues the A tile by
       // bulk copy, and every lane copies its 16-byte pieces of the 16 B rows.
+      const uint64_t pol_a = ptx::policy_evict_first(), pol_b = ptx::policy_evict_last();
       int pf[SP_PF];
 #pragma unroll
       for (int q = 0; q < SP_PF; ++q) {
@@ -574,8 +584,11 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             break;
           }
           if (lane == 0) {
+            // A tiles are read once: evict-first, so that they do not push
+            // the B rows (read by every tile) out of L2
             ptx::mbar_arrive_expect_tx(&sm.full[s], SP_KSTEP_BYTES);
-            ptx::bulk_g2s(sm.a[s], p.a + (size_t)(s0 + ii) * SP_KSTEP_BYTES, SP_KSTEP_BYTES, &sm.full[s]);
+            ptx::bulk_g2s_hint(sm.a[s], p.a + (size_t)(s0 + ii) * SP_KSTEP_BYTES, SP_KSTEP_BYTES, &sm.full[s],
+                               pol_a);
           }
           // the 16 B rows: each lane copies 16-byte chunks into the
           // 128-byte-swizzled layout of the MMA's B operand (atoms of 8 k-rows
@@ -593,7 +606,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
               // a padding column (-1): its A column is zero; fill zeros, read nothing
               const unsigned char* src = p.B + (size_t)(row < 0 ? 0 : row) * p.ldb + (size_t)(n0 + 8 * c) * 2;
               unsigned char* dst = bs + (c >> 3) * 2048 + (kr >> 3) * 1024 + (kr & 7) * 128 + (((c & 7) ^ (kr & 7)) << 4);
-              ptx::cp_async16_zfill(dst, src, row < 0 ? 0u : 16u);
+              ptx::cp_async16_zfill_hint(dst, src, row < 0 ? 0u : 16u, pol_b);
             }
             ptx::cp_async_mbar_arrive(&sm.full[s]);
           }
@@ -787,10 +800,10 @@ static vnm_status compress_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, con
   const size_t b_step = arena_bytes(ntiles + 1, 4), b_tl = arena_bytes((size_t)out->ntt + 1, 8),
                b_cols = arena_bytes((size_t)out->nsteps * 16 + 1, 4),
                b_a = arena_bytes((size_t)out->nsteps * SP_KSTEP_BYTES + 16, 1),
-               b_sc = arena_bytes((size_t)ntiles * SP_TM, 4), b_rc = arena_bytes((size_t)out->nres + 1, 4),
-               b_rv = arena_bytes((size_t)out->nres + 1, 4), b_tk = arena_bytes((size_t)out->ntask + 1, 16),
+               b_sc = arena_bytes((size_t)ntiles * SP_TM, 4), b_rc = arena_bytes((size_t)out->nres + 1, 8),
+               b_tk = arena_bytes((size_t)out->ntask + 1, 16),
                b_mu = arena_bytes((size_t)out->nmulti + 1, 16);
-  const size_t need = b_step + b_tl + b_cols + b_a + b_sc + b_rc + b_rv + b_tk + b_mu;
+  const size_t need = b_step + b_tl + b_cols + b_a + b_sc + b_rc + b_tk + b_mu;
   void* base = nullptr;
   size_t have = 0;
   if (ctx->spare) {  // a freed operand's storage, when large enough
@@ -820,10 +833,8 @@ static vnm_status compress_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, con
   o += b_a;
   out->rscale = reinterpret_cast<float*>(pb + o);
   o += b_sc;
-  out->rcol = reinterpret_cast<int*>(pb + o);
+  out->rcv = reinterpret_cast<int2*>(pb + o);
   o += b_rc;
-  out->rval = reinterpret_cast<float*>(pb + o);
-  o += b_rv;
   out->task = reinterpret_cast<int4*>(pb + o);
   o += b_tk;
   out->multi = reinterpret_cast<int4*>(pb + o);
@@ -837,8 +848,7 @@ static vnm_status compress_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, con
     unsigned long long* sk = nullptr;
     int* ss = nullptr;
     VNM_TRY(radix_sort_u64(ctx, rkey, rsrc, (int)out->nres, sp_bits(R), &sk, &ss));
-    VNM_LAUNCH(ctx, k_res_gather, sp_grid(ctx, out->nres), 256, 0, ss, d_col, d_val, (int)out->nres, out->rcol,
-               out->rval);
+    VNM_LAUNCH(ctx, k_res_gather, sp_grid(ctx, out->nres), 256, 0, ss, d_col, d_val, (int)out->nres, out->rcv);
   }
   if (out->ntask > 0)
     VNM_LAUNCH(ctx, k_res_task_fill, sp_grid(ctx, R), 256, 0, rptr, R, tile_has, tile_res, mt_off, st_off, mr_off,
@@ -975,7 +985,7 @@ static vnm_status spmm_enqueue(vnm_ctx* ctx, const vnm_spmm_matrix* A, const voi
       const int per_block = (RES_THREADS / 32) * (32 / lw);
       dim3 grid((unsigned)((A->ntask + per_block - 1) / per_block), (unsigned)(n / (8 * lw)));
 #define VNM_RES(LWV, BFV)                                                                                   \
-  VNM_LAUNCH(ctx, (k_spmm_res<LWV, BFV>), grid, RES_THREADS, 0, A->task, A->ntask, A->rcol, A->rval, p.B, p.ldb, dC, \
+  VNM_LAUNCH(ctx, (k_spmm_res<LWV, BFV>), grid, RES_THREADS, 0, A->task, A->ntask, A->rcv, p.B, p.ldb, dC, \
              n, P, n)
       if (A->dtype == 1) {
         if (lw == 32) VNM_RES(32, true);

@@ -157,6 +157,7 @@ class Context:
         d = dict(zip(keys, list(out)[:8]))
         d["phase_kcycles"] = dict(zip(("select", "choose", "gather", "process", "heap_entries", "heaps_and_walk", "apply"),
                                       list(out)[8:15]))
+        d["table_fallback_rounds"] = out[15]
         return d
 
     # ---- array plumbing: numpy arrays (host) or torch CUDA tensors (device)
