@@ -653,7 +653,8 @@ def run_ours(args, rank, world, local):
             out["baselines_c2_spmm"] = {"error": "%s: %s" % (type(e).__name__, e)}
     if rank == 0 and world == 1 and not args.no_extended:
         # the other configurations, untimed by the headline (one GPU, after it)
-        for key, fn in (("c3_batch", bench_batch_c3), ("c4_learned", bench_learned_c4), ("c5_gcn", bench_gcn_c5),
+        for key, fn in (("vnm_stage_c2", bench_vnm_stage), ("c3_batch", bench_batch_c3),
+                        ("c4_learned", bench_learned_c4), ("c5_gcn", bench_gcn_c5),
                         ("s1_structured_spmm", bench_structured_spmm)):
             try:
                 out[key] = fn(ctx)
@@ -804,6 +805,36 @@ def bench_learned_c4(ctx, reps=3):
                             "ms": _median(ms[1:]), "tflops": fl / _median(ms[1:]) / 1e9,
                             "frac_of_bf16_peak": fl / _median(ms[1:]) / 1e9 / tpk, "peak_kind": tkind}
     net.close()
+    return out
+
+
+def bench_vnm_stage(ctx, reps=5):
+    """The VNM stage (reordering.py --m 8 --v 64) on the R-MAT 16384 matrix
+    on the GPU, against the reference script's own run of it (a committed
+    fixture made where the script runs: its result and its seconds on that
+    machine's one core) and the oracle's port on one host core."""
+    from vnm_gb300 import synth
+    nr, r, c, v = synth.rmat_c2(0)
+    ms, out5 = [], None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        out5, _, _, _ = ctx.vnm_reorder(nr, nr, r, c, 8, 64, maxiter=10)
+        ms.append(1000.0 * (time.perf_counter() - t0))
+    out = {"workload": "R-MAT 16384 (C2 matrix), VNM stage at M=8, V=64, maxiter 10", "wall_ms": _median(ms),
+           "device_ms": ctx.last_kernel_ms, "out5": out5.tolist()}
+    p = os.path.join(GOLD, "scale_vnm_c2.npz")
+    if os.path.exists(p):
+        g = np.load(p)
+        out["same_as_reordering_py"] = out5.tolist() == g["out5"].tolist()
+        out["reordering_py_seconds_1core"] = float(g["seconds"])
+        out["reordering_py_note"] = "measured where the reference checkout is (x86 host), not on this machine"
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    oracle.set_threads(1)
+    t0 = time.perf_counter()
+    o5, _, _, _ = oracle.vnm_run(nr, nr, r, c, 8, 64, 10)
+    out["port_1core_ms"] = 1000.0 * (time.perf_counter() - t0)
+    out["same_as_port"] = o5.tolist() == out5.tolist()
     return out
 
 

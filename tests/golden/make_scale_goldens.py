@@ -23,9 +23,16 @@ oracle/ref_build.py makes): `ref-run` on a GPU machine writes its raw output,
 `ref-collect` turns it into scale_ref_c2.npz (result integers, final
 position of every node that carries an entry, seconds per schedule).
 
+The reference's VNM stage, `python3 reordering.py --m 8 --v 64`, is run on
+the c2 matrix as well (`vnm-ref`, where the reference checkout is, about 5
+minutes on one core): scale_vnm_c2.npz holds the five integers it writes to
+output.txt, the (row, col) of the matrix it writes back in entry order,
+and its wall seconds (this machine's, for the record).
+
 usage: python tests/golden/make_scale_goldens.py oracle [--only c2|c4] [--threads T]
        python tests/golden/make_scale_goldens.py ref-run [--out DIR]
        python tests/golden/make_scale_goldens.py ref-collect [--src DIR]
+       python tests/golden/make_scale_goldens.py vnm-ref [--ref DIR]
 """
 import argparse
 import hashlib
@@ -43,6 +50,8 @@ sys.path.insert(0, os.path.join(REPO, "oracle"))
 
 OUT_NPZ = os.path.join(HERE, "scale_oracle_goldens.npz")
 REF_NPZ = os.path.join(HERE, "scale_ref_c2.npz")
+VNM_NPZ = os.path.join(HERE, "scale_vnm_c2.npz")
+DEFAULT_REF = os.environ.get("VNM_REF_DIR", "/root/reference")
 WORKLOADS = {"c2": ("rmat_c2", 2, 4), "c4": ("rmat_c4", 2, 8)}
 
 
@@ -139,9 +148,36 @@ def ref_collect(src):
     print("wrote", REF_NPZ, res4)
 
 
+def vnm_ref(ref):
+    """reordering.py (M=8, V=64, maxiter 10) on the c2 matrix, in a scratch
+    working directory as main.cu runs it (temp.mtx in, temp.mtx and
+    output.txt out)."""
+    import subprocess
+    import tempfile
+    from scipy.io import mmread
+    from vnm_gb300 import synth
+    nr, r, c, v, N, M = load("c2")
+    with tempfile.TemporaryDirectory() as td:
+        synth.write_mtx(os.path.join(td, "temp.mtx"), nr, r, c, v)
+        t0 = time.perf_counter()
+        p = subprocess.run([sys.executable, os.path.join(ref, "reordering.py"), "--m", "8", "--v", "64", "--maxiter",
+                            "10"], cwd=td, capture_output=True, text=True)
+        dt = time.perf_counter() - t0
+        if p.returncode != 0:
+            raise SystemExit(p.stderr[-2000:])
+        with open(os.path.join(td, "output.txt")) as f:
+            out5 = [int(x) for x in f.read().strip().split(",")]
+        mm = mmread(os.path.join(td, "temp.mtx"))
+    np.savez_compressed(VNM_NPZ, out5=np.array(out5, np.int32), row=np.asarray(mm.row, np.int32),
+                        col=np.asarray(mm.col, np.int32), seconds=np.float64(dt),
+                        sha256=np.array(coo_digest(nr, r, c, v)))
+    print("wrote", VNM_NPZ, out5, "%.1f s" % dt)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("step", choices=["oracle", "ref-run", "ref-collect"])
+    ap.add_argument("step", choices=["oracle", "ref-run", "ref-collect", "vnm-ref"])
+    ap.add_argument("--ref", default=DEFAULT_REF)
     ap.add_argument("--only", choices=sorted(WORKLOADS), default=None)
     ap.add_argument("--threads", type=int, default=max(1, (os.cpu_count() or 4) // 4))
     ap.add_argument("--out", default=os.path.join(REPO, "gpurun_out", "ref_c2"))
@@ -151,6 +187,8 @@ def main():
         return ref_run(a.out)
     if a.step == "ref-collect":
         return ref_collect(a.src)
+    if a.step == "vnm-ref":
+        return vnm_ref(a.ref)
     names = [a.only] if a.only else sorted(WORKLOADS)
     old = dict(np.load(OUT_NPZ)) if os.path.exists(OUT_NPZ) else {}
     out = {k: v for k, v in old.items() if k.split("__")[0] not in names}

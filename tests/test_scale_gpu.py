@@ -85,3 +85,20 @@ def test_c3_batch_members_match_oracle(ctx):
         ores, _, _, opos = oracle.nm_run(nr, r, c, v, 2, M, 0)
         assert np.array_equal(res[b], ores), (b, nr)
         assert np.array_equal(pos[b], opos), (b, nr)
+
+
+def test_c2_vnm_stage_matches_reordering_py(ctx):
+    """The VNM stage (reordering.py:200-265) at M=8, V=64 on the R-MAT 16384
+    matrix: the five integers of output.txt and the matrix written back,
+    against the reference script's own run (scale_vnm_c2.npz), and every
+    array against the oracle's port."""
+    g = np.load(os.path.join(GOLD, "scale_vnm_c2.npz"))
+    msg = _scale()
+    nr, r, c, v, N, M = msg.load("c2")
+    assert msg.coo_digest(nr, r, c, v) == str(g["sha256"])
+    out5, r2, c2, pos = ctx.vnm_reorder(nr, nr, r, c, 8, 64, maxiter=10)
+    assert out5.tolist() == g["out5"].tolist()
+    assert set(zip(r2.tolist(), c2.tolist())) == set(zip(g["row"].tolist(), g["col"].tolist()))
+    o5, or2, oc2, opos = oracle.vnm_run(nr, nr, r, c, 8, 64, 10)
+    assert out5.tolist() == o5.tolist()
+    assert np.array_equal(r2, or2) and np.array_equal(c2, oc2) and np.array_equal(pos, opos)
