@@ -204,6 +204,8 @@ struct RoundSmem {
   int tcount;       // how many
   int tover;        // a block's table ran out of slots this round (the leader's copy is read)
   int tfall;        // ... so this round gathers into global memory after all
+  uint4* rcache;    // the process phase's first pass of touched rows, kept for the apply phase
+  int* rcrow;       //   (NM_THREADS x 4 records and their rows), or null
   int status;
   int nswaps;
   int hprog[K * K];  // pops of each ordered pair's heap written to ord so far
@@ -680,9 +682,13 @@ __device__ __forceinline__ unsigned rec_byte(const uint4& w, int xi) {
 // end get valid = false and a zero record) so f may use warp votes.  Each
 // lane first loads the records of TOUCH_U rows so their L2 round trips
 // overlap.
-template <int M, class F>
+// CM = 1: keep the records of the first pass in shared memory (process
+// phase); CM = 2: take them from there (apply phase), saving two dependent
+// L2 loads.  Both phases deal the rows to threads the same way, and the
+// touched rows and their records do not change in between.
+constexpr int TOUCH_U = 4;
+template <int M, int CM, class F>
 __device__ __forceinline__ void for_touched_warp(const RoundSmem<M>& sm, const NMJob& J, Slice sl, F&& f) {
-  constexpr int TOUCH_U = 4;
   constexpr int NW = NM_THREADS / 32;
   const int nt = sm.ntouched;
   // 32-row chunks dealt round-robin over the job's blocks first, then over
@@ -690,16 +696,33 @@ __device__ __forceinline__ void for_touched_warp(const RoundSmem<M>& sm, const N
   // SM of the cluster (the phases are issue-bound per SM)
   const int NWt = sl.cs * NW;
   const int lane = threadIdx.x & 31, w = (threadIdx.x >> 5) * sl.cs + sl.rank;
+  bool first = true;
   for (int c0 = w; c0 * 32 < nt; c0 += NWt * TOUCH_U) {
     int rv[TOUCH_U];
     uint4 wv[TOUCH_U];
+    if (CM == 2 && first && sm.rcache) {
 #pragma unroll
-    for (int u = 0; u < TOUCH_U; ++u) {
-      const int t = (c0 + u * NWt) * 32 + lane;
-      rv[u] = t < nt ? J.touched[t] : -1;
+      for (int u = 0; u < TOUCH_U; ++u) {
+        rv[u] = sm.rcrow[u * NM_THREADS + threadIdx.x];
+        wv[u] = sm.rcache[u * NM_THREADS + threadIdx.x];
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < TOUCH_U; ++u) {
+        const int t = (c0 + u * NWt) * 32 + lane;
+        rv[u] = t < nt ? J.touched[t] : -1;
+      }
+#pragma unroll
+      for (int u = 0; u < TOUCH_U; ++u) wv[u] = rv[u] >= 0 ? J.rec[rv[u]] : make_uint4(0u, 0u, 0u, 0u);
+      if (CM == 1 && first && sm.rcache) {
+#pragma unroll
+        for (int u = 0; u < TOUCH_U; ++u) {
+          sm.rcrow[u * NM_THREADS + threadIdx.x] = rv[u];
+          sm.rcache[u * NM_THREADS + threadIdx.x] = wv[u];
+        }
+      }
     }
-#pragma unroll
-    for (int u = 0; u < TOUCH_U; ++u) wv[u] = rv[u] >= 0 ? J.rec[rv[u]] : make_uint4(0u, 0u, 0u, 0u);
+    first = false;
 #pragma unroll 1
     for (int u = 0; u < TOUCH_U && (c0 + u * NWt) * 32 < nt; ++u) f(rv[u], wv[u], rv[u] >= 0);
   }
@@ -708,7 +731,7 @@ __device__ __forceinline__ void for_touched_warp(const RoundSmem<M>& sm, const N
 // Run f(index, record, valid) over this round's row records: the table
 // slots (index = slot) when the records are in shared memory, else the
 // touched rows (index = row).  Warp-uniform like for_touched_warp.
-template <int M, class F>
+template <int M, int CM, class F>
 __device__ __forceinline__ void for_rows_warp(const RoundSmem<M>& sm, const NMJob& J, Slice sl, F&& f) {
   if (sm.use_table) {  // the rows this block's table holds, from its list of claimed slots
     constexpr int NW = NM_THREADS / 32;
@@ -721,7 +744,7 @@ __device__ __forceinline__ void for_rows_warp(const RoundSmem<M>& sm, const NMJo
       f(slot, v, i < n);
     }
   } else {
-    for_touched_warp<M>(sm, J, sl, f);
+    for_touched_warp<M, CM>(sm, J, sl, f);
   }
 }
 
@@ -743,7 +766,7 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
   // this warp's row masks: VL[x][k] at vw[2x * M + k], VE[x][k] at vw[(2x + 1) * M + k]
   extern __shared__ uint4 smem_heap[];
   unsigned* vw = reinterpret_cast<unsigned*>(smem_heap) + (threadIdx.x >> 5) * (2 * K * M);
-  for_rows_warp<M>(sm, J, sl, [&](int r, const uint4& w, bool valid) {
+  for_rows_warp<M, 1>(sm, J, sl, [&](int r, const uint4& w, bool valid) {
     (void)r;
     unsigned b[K];
     int p[K];
@@ -1225,7 +1248,7 @@ __device__ void apply_recount(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl)
     bitmove[xi][h][v] = make_uint4(o[0], o[1], o[2], 0u);
   }
   __syncthreads();
-  for_rows_warp<M>(sm, J, sl, [&](int r, const uint4& w, bool valid) {
+  for_rows_warp<M, 2>(sm, J, sl, [&](int r, const uint4& w, bool valid) {
     // the row's groups after the swaps, packed like the record
     unsigned n0 = 0, n1 = 0, n2 = 0;
 #pragma unroll 1
@@ -1290,7 +1313,7 @@ __device__ void cluster_push(cg::cluster_group& cl, int* mine, int n) {
 // to run a round is copied to every block before the barrier that opens it.
 template <int M>
 __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __restrict__ jobs, int N,
-                                                              int cnt_in_smem, int ts_max, int cs) {
+                                                              int cnt_in_smem, int ts_max, int cs, int rcache_on) {
   constexpr int K = M + 1;
   __shared__ RoundSmem<M> sm;
   static_assert(offsetof(RoundSmem<M>, CL) == offsetof(RoundSmem<M>, S) + sizeof(int) * K * M, "S, CL adjacent");
@@ -1300,11 +1323,14 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
                 "newinv, newpres adjacent");
   constexpr int NSUM = K * M + 2 * RoundSmem<M>::NPAIR * RoundSmem<M>::MM;
   // dynamic shared memory: [heap scratch][row-record table: ts_max x 16 B]
-  // [claimed-slot list: ts_max x 4 B][segment counts]
+  // [claimed-slot list: ts_max x 4 B][record cache: NM_THREADS x TOUCH_U x
+  // (16 + 4) B, when on][segment counts]
   extern __shared__ uint4 smem_heap[];
   uint4* smem_dyn = smem_heap + RoundSmem<M>::SCR_U4;
   int* smem_list = reinterpret_cast<int*>(smem_dyn + ts_max);
-  int* smem_cnt = smem_list + ts_max;
+  uint4* smem_rcache = reinterpret_cast<uint4*>(smem_list + ts_max);
+  int* smem_rcrow = reinterpret_cast<int*>(smem_rcache + (rcache_on ? NM_THREADS * TOUCH_U : 0));
+  int* smem_cnt = smem_rcrow + (rcache_on ? NM_THREADS * TOUCH_U : 0);
   cg::cluster_group cl = cg::this_cluster();
   const int rank = cs > 1 ? (int)cl.block_rank() : 0;
   const bool lead = rank == 0;
@@ -1319,6 +1345,8 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     sm.status = JOB_OK;
     sm.table = ts_max > 0 ? smem_dyn : nullptr;
     sm.tlist = ts_max > 0 ? smem_list : nullptr;
+    sm.rcache = rcache_on ? smem_rcache : nullptr;
+    sm.rcrow = rcache_on ? smem_rcrow : nullptr;
     sm.tcount = 0;
     sm.tfall = 0;
     sm.ts_max = ts_max;
@@ -1496,6 +1524,8 @@ __global__ void __launch_bounds__(NM_THREADS) k_pair_score(NMJob J, int N, int s
     sm.table = nullptr;
     sm.ts_max = 0;
     sm.use_table = 0;
+    sm.rcache = nullptr;
+    sm.rcrow = nullptr;
     sm.xseg[0] = s1;
     sm.xcnt[0] = 0;
     if (s1 == s2) {
@@ -1685,7 +1715,10 @@ static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, 
     const char* e = getenv("VNM_NM_CLUSTER_TABLE");
     if (!(e && atoi(e) == 1)) ts = 0;
   }
-  const size_t dyn = hbytes + (size_t)ts * SLOT + (in_smem ? cbytes : 0);
+  // the record cache of the apply phase, when the budget allows it
+  constexpr size_t RCACHE = (size_t)NM_THREADS * TOUCH_U * (sizeof(uint4) + sizeof(int));
+  int rc = fixed + (size_t)ts * SLOT + RCACHE <= NM_SMEM_BUDGET ? 1 : 0;
+  const size_t dyn = hbytes + (size_t)ts * SLOT + (rc ? RCACHE : 0) + (in_smem ? cbytes : 0);
   // static + dynamic shared memory may pass the 48 KB a launch gets without
   // opting in (RoundSmem<8> alone is ~30 KB)
   VNM_CUDA_TRY(cudaFuncSetAttribute(k_nm_rounds<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
@@ -1725,7 +1758,7 @@ static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, 
     if (pick > 1) {
       attr[0].val.clusterDim.x = (unsigned)pick;
       cfg.gridDim = dim3((unsigned)(njobs * pick));
-      VNM_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_nm_rounds<M>, d_jobs, N, in_smem, ts, pick));
+      VNM_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_nm_rounds<M>, d_jobs, N, in_smem, ts, pick, rc));
       ctx->launches++;
       ctx->last_cluster = pick;
       return VNM_OK;
@@ -1734,13 +1767,14 @@ static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, 
     ts = 8192;
     while (ts >= 1024 && fixed + (size_t)ts * SLOT > NM_SMEM_BUDGET) ts >>= 1;
     if (ts < 1024) ts = 0;
-    const size_t dyn1 = hbytes + (size_t)ts * SLOT + (in_smem ? cbytes : 0);
+    rc = fixed + (size_t)ts * SLOT + RCACHE <= NM_SMEM_BUDGET ? 1 : 0;
+    const size_t dyn1 = hbytes + (size_t)ts * SLOT + (rc ? RCACHE : 0) + (in_smem ? cbytes : 0);
     VNM_CUDA_TRY(cudaFuncSetAttribute(k_nm_rounds<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn1));
-    VNM_LAUNCH(ctx, k_nm_rounds<M>, njobs, NM_THREADS, dyn1, d_jobs, N, in_smem, ts, 1);
+    VNM_LAUNCH(ctx, k_nm_rounds<M>, njobs, NM_THREADS, dyn1, d_jobs, N, in_smem, ts, 1, rc);
     ctx->last_cluster = 1;
     return VNM_OK;
   }
-  VNM_LAUNCH(ctx, k_nm_rounds<M>, njobs, NM_THREADS, dyn, d_jobs, N, in_smem, ts, 1);
+  VNM_LAUNCH(ctx, k_nm_rounds<M>, njobs, NM_THREADS, dyn, d_jobs, N, in_smem, ts, 1, rc);
   ctx->last_cluster = 1;
   return VNM_OK;
 }
