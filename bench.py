@@ -325,9 +325,9 @@ def library_spmm_baselines(nr, r, c, v, n, dtype, dense=True, reps=10):
     return out
 
 
-def reference_gpu_c2(nr, r, c, v, timeout=300.0):
+def reference_gpu(nr, r, c, v, N=N_NM, M=M_NM, timeout=300.0):
     """The reference's own GPU reorder (reorder/reorder.h built from its
-    sources with N=2, M=4 into oracle/_ref/ref_nm_n2_m4 by
+    sources with N and M fixed into oracle/_ref/ref_nm_n<N>_m<M> by
     oracle/ref_build.py) on the same matrix, schedule by schedule, as
     find_best_2toX (main.cu:72-114) runs them: wall seconds per schedule
     and the result integers."""
@@ -336,14 +336,14 @@ def reference_gpu_c2(nr, r, c, v, timeout=300.0):
     import ref_build
     from vnm_gb300 import synth
     try:
-        exe = ref_build.ensure("ref_nm_n2_m4")
+        exe = ref_build.ensure("ref_nm_n%d_m%d" % (N, M))
     except Exception as e:
         return {"unavailable": "%s: %s" % (type(e).__name__, e)}
     out = {"what": "the reference's own GPU find_best_2toX schedules (reorder/reorder.h, main.cu:72-114), built "
                    "from its sources for sm_103a; includes each run's file read and CUDA set-up, as the "
                    "reference's command does", "seconds": {}, "res5": {}}
     with tempfile.TemporaryDirectory() as td:
-        mtx = os.path.join(td, "c2.mtx")
+        mtx = os.path.join(td, "in.mtx")
         synth.write_mtx(mtx, nr, r, c, v)
         for sch in range(4):
             o = os.path.join(td, "res%d.txt" % sch)
@@ -414,7 +414,10 @@ def run_reference(args, rank, world):
             "seconds_one_schedule": cpu_port_one_schedule(nr, r, c, v, int(best), 1), "cores": 1,
             "sample": "schedule %d of find_best_2toX on one thread" % int(best)}
         line["vnm_stage_port"] = vnm_stage_port(nr, r, c, v)
-        line["reference_gpu"] = reference_gpu_c2(nr, r, c, v)
+        line["reference_gpu"] = reference_gpu(nr, r, c, v)
+        from vnm_gb300 import synth
+        n1, r1, c1, v1 = synth.uniform_c1(0)
+        line["reference_gpu_c1"] = dict(reference_gpu(n1, r1, c1, v1, 2, 8), workload=C1_WORKLOAD)
     print(json.dumps(line), flush=True)
 
 
@@ -606,11 +609,22 @@ def run_ours(args, rank, world, local):
                      "incremental_frac": inc_bytes / kt / 1e9 / peak if kt > 0 else 0.0,
                      "note": "latency-bound sequential greedy (4 jobs x cluster of %d blocks); see profiles/"
                              % int(t["stats"]["blocks_per_job"]),
-                     "round_phase_share": {k: round(vv / max(1, sum(phase_sum.values())), 4)
-                                           for k, vv in phase_sum.items()}},
-        "spmm": {"kernel": "k_spmm_vnm<64|128|256> (column-block width picked by timing on the first call)",
+                     # shares of the leaders' cycles from the kernel's start to its end
+                     "round_phase_share": dict({k: round(vv / max(1, stt.get("kernel_kcycles", 0),
+                                                                  sum(phase_sum.values())), 4)
+                                                for k, vv in phase_sum.items()},
+                                               outside_rounds=round(max(0, stt.get("kernel_kcycles", 0) -
+                                                                        sum(phase_sum.values())) /
+                                                                    max(1, stt.get("kernel_kcycles", 0)), 4))},
+        "spmm": {"kernel": ("k_spmm_vnm<64|128|256> (column-block width picked by timing on the first call) + "
+                            "k_spmm_res" if info["tensor_tiles"] > 0 else "k_spmm_res + k_spmm_fin (CUDA cores)"),
+                 "routing": "%d tensor-core tiles; %d residual nonzeros on the CUDA cores (V-blocks with fewer "
+                            "than dense_min = %d nonzeros)" % (info["tensor_tiles"], info["residual_nnz"],
+                                                               info["dense_min"]),
                  "useful_tflops": useful / sk / 1e12,
-                 "issued_tflops": issued / sk / 1e12, "bound": "tensor", "peak_tflops": tflops_peak,
+                 "issued_tflops": issued / sk / 1e12,
+                 "bound": "tensor" if info["tensor_tiles"] > 0 else "hbm (gathered B rows)",
+                 "peak_tflops": tflops_peak,
                  "peak_kind": tkind, "issued_frac": issued / sk / 1e12 / tflops_peak,
                  "hbm": {"alg_bytes": spmm_bytes, "achieved_gbs": spmm_bytes / sk / 1e9, "peak": peak,
                          "frac": spmm_bytes / sk / 1e9 / peak, "peak_kind": peak_kind,
@@ -653,7 +667,7 @@ def run_ours(args, rank, world, local):
             out["baselines_c2_spmm"] = {"error": "%s: %s" % (type(e).__name__, e)}
     if rank == 0 and world == 1 and not args.no_extended:
         # the other configurations, untimed by the headline (one GPU, after it)
-        for key, fn in (("vnm_stage_c2", bench_vnm_stage), ("c3_batch", bench_batch_c3),
+        for key, fn in (("c1_plain_small", bench_plain_c1), ("vnm_stage_c2", bench_vnm_stage), ("c3_batch", bench_batch_c3),
                         ("c4_learned", bench_learned_c4), ("c5_gcn", bench_gcn_c5),
                         ("s1_structured_spmm", bench_structured_spmm)):
             try:
@@ -836,6 +850,57 @@ def bench_vnm_stage(ctx, reps=5):
     out["port_1core_ms"] = 1000.0 * (time.perf_counter() - t0)
     out["same_as_port"] = o5.tolist() == out5.tolist()
     return out
+
+
+C1_WORKLOAD = "C1: uniform 512x512, ~2 % density (seed 0), U[-1,1]; 2:8, V=64, maxiter 10, schedule 0"
+
+
+def bench_plain_c1(ctx, reps=3):
+    """C1 through the drop-in `spmm` command (find_best_2toX, then 10 rounds
+    of the VNM stage and the NM reorder): process wall time, the CSV line's
+    counts, the retained-nnz of the written matrix, and the same command
+    composed by the oracle on one host thread, whose 15 CSV fields and
+    output text must match."""
+    import tempfile
+    from vnm_gb300 import synth
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    N, M, Vc, maxiter = 2, 8, 64, 10
+    n, r, c, v = synth.uniform_c1(0)
+    exe = os.path.join(PKG, "spmm")
+    with tempfile.TemporaryDirectory() as td:
+        mtx, out = os.path.join(td, "c1.mtx"), os.path.join(td, "out.mtx")
+        synth.write_mtx(mtx, n, r, c, v)
+        walls = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            p = subprocess.run([exe, "--mtxfile", mtx, "--outmtxfile", out, "--maxiter", str(maxiter), "--n", "64",
+                                "--sched", "0", "--v", str(Vc), "--N", str(N), "--M", str(M)],
+                               cwd=td, capture_output=True, text=True, timeout=600)
+            walls.append(time.perf_counter() - t0)
+            if p.returncode != 0:
+                return {"error": p.stderr[-500:]}
+        f = [float(x) for x in p.stdout.strip().split(",")]
+        with open(out) as fh:
+            text = fh.read()
+        oracle.set_threads(1)
+        t0 = time.perf_counter()
+        csv, best, onr, orr, occ, ovv = oracle.spmm_cli(mtx, N, M, Vc, maxiter)
+        ot = time.perf_counter() - t0
+        oracle.set_threads(oracle.max_threads())
+        op = os.path.join(td, "oracle_out.mtx")
+        oracle.write_mtx(op, onr, onr, orr, occ, ovv)
+        with open(op) as fh:
+            otext = fh.read()
+    same = bool(np.allclose(f[:15], csv[:15], rtol=1e-5, atol=1e-6)) and text == otext
+    return {"workload": C1_WORKLOAD, "nnz": int(len(r)), "process_wall_ms": 1000.0 * _median(walls),
+            "hybrid_ms": f[15], "best_sched": int(best), "init_cnt": f[5], "final_cnt": f[6],
+            "init_vblocks": f[8], "final_vblocks": f[9], "nm_rounds": f[12], "vnm_rounds": f[13],
+            "retained_nm": int(oracle.retained_nm(onr, orr, occ, ovv, N, M)),
+            "retained_vnm": int(oracle.retained_vnm(onr, orr, occ, ovv, N, M, Vc)),
+            "csv_and_output_match_oracle": same,
+            "oracle_one_thread": {"seconds": ot, "cores": 1, "kind": "port",
+                                  "what": "the oracle's composition of the spmm command (orc_spmm_cli)"}}
 
 
 def hybrid_cli(n, r, c, v, N, M, Vc, maxiter):

@@ -78,8 +78,10 @@ float vnm_last_main_kernel_ms(const vnm_ctx* ctx);
  * were in shared-memory tables (summed over jobs), out[8..14] kilocycles
  * spent per round phase (select, choose, gather, process, heap entries,
  * swap heaps and walk overlapped, apply) summed over jobs, out[15] rounds
- * whose tables ran out of slots and gathered into global memory instead.
- * n <= 16 values. */
+ * whose tables ran out of slots and gathered into global memory instead,
+ * out[16] kilocycles from the round kernel's start to its end summed over
+ * jobs (out[8..14] plus the set-up and the final write-back).
+ * n <= 20 values. */
 vnm_status vnm_last_stats(const vnm_ctx* ctx, long long* out, int n);
 
 /* ---------------------------------------------------------------------------

@@ -65,6 +65,9 @@ def lib():
         L.orc_spmm_cli.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                    ctypes.c_int, _f64p, _i32p, _i32p, _i32p, ctypes.POINTER(_i32p),
                                    ctypes.POINTER(_i32p), ctypes.POINTER(_f32p)]
+        L.orc_spmm_cli_sched.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_int, _f64p, _i32p, _i32p, _i32p,
+                                         ctypes.POINTER(_i32p), ctypes.POINTER(_i32p), ctypes.POINTER(_f32p)]
         L.orc_retained_nm.argtypes = [ctypes.c_int, ctypes.c_int, _i32p, _i32p, _f32p, ctypes.c_int, ctypes.c_int]
         L.orc_retained_nm.restype = ctypes.c_int64
         L.orc_retained_vnm.argtypes = [ctypes.c_int, ctypes.c_int, _i32p, _i32p, _f32p, ctypes.c_int,
@@ -219,13 +222,16 @@ def find_best(nrows, row, col, val, N, M, nscheds=4):
     return best.value, out.reshape(4, 12)
 
 
-def spmm_cli(mtxfile, N, M, V, maxiter, init_mb_path=None):
-    """Whole `spmm` command; returns (csv16, best, nrows, row, col, val)."""
+def spmm_cli(mtxfile, N, M, V, maxiter, init_mb_path=None, sched=None):
+    """Whole `spmm` command; returns (csv16, best, nrows, row, col, val).
+    `sched` fixes the schedule instead of find_best_2toX's choice (the
+    reference breaks its ties by wall time, main.cu:90-99)."""
     csv = np.zeros(16, np.float64)
     best, onr, onz = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
     r, c, v = _i32p(), _i32p(), _f32p()
-    _check(lib().orc_spmm_cli(os.fsencode(mtxfile), os.fsencode(init_mb_path) if init_mb_path else None, N, M, V,
-                              maxiter, _p(csv, _f64p), best, onr, onz, r, c, v), "spmm_cli")
+    _check(lib().orc_spmm_cli_sched(os.fsencode(mtxfile), os.fsencode(init_mb_path) if init_mb_path else None, N, M,
+                                    V, maxiter, -1 if sched is None else int(sched), _p(csv, _f64p), best, onr, onz,
+                                    r, c, v), "spmm_cli")
     n = onz.value
     return csv, best.value, onr.value, _take(r, n, np.int32), _take(c, n, np.int32), _take(v, n, np.float32)
 

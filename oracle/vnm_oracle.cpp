@@ -958,13 +958,21 @@ int orc_find_best(int nrows, int nnz, const int* row, const int* col, const floa
 
 int orc_spmm_cli(const char* mtxfile, const char* init_mb_path, int N, int M, int V, int maxiter, double* csv16,
                  int* best_sched, int* out_nrows, int* out_nnz, int** out_row, int** out_col, float** out_val) {
-  if (M < 2 || M > 8 || N < 1 || N >= M || V < 1 || maxiter < 0) return ORC_ERR_ARG;
+  return orc_spmm_cli_sched(mtxfile, init_mb_path, N, M, V, maxiter, -1, csv16, best_sched, out_nrows, out_nnz,
+                            out_row, out_col, out_val);
+}
+
+int orc_spmm_cli_sched(const char* mtxfile, const char* init_mb_path, int N, int M, int V, int maxiter,
+                       int force_sched, double* csv16, int* best_sched, int* out_nrows, int* out_nnz, int** out_row,
+                       int** out_col, float** out_val) {
+  if (M < 2 || M > 8 || N < 1 || N >= M || V < 1 || maxiter < 0 || force_sched > 3) return ORC_ERR_ARG;
   Coo a0;
   int st = read_mtx_file(mtxfile, M, a0);
   if (st) return st;
   int best = 0;
   st = find_best_impl(a0, N, M, 4, &best, nullptr);
   if (st) return st;
+  if (force_sched >= 0) best = force_sched;  // a schedule the reference picked by wall time among tied ones
   *best_sched = best;
   for (int i = 0; i < 16; ++i) csv16[i] = 0;
   // hybrid_reordering (main.cu:195-337)

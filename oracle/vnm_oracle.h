@@ -127,6 +127,16 @@ int orc_spmm_cli(const char* mtxfile, const char* init_mb_path, int N, int M,
                  int* out_nrows, int* out_nnz, int** out_row, int** out_col,
                  float** out_val);
 
+/* The same with the schedule fixed (force_sched 0..3; -1 = search).
+ * find_best_2toX breaks ties on improve rate by measured wall time
+ * (main.cu:90-99), so a recorded run of the reference command is
+ * reproduced by giving the schedule it picked. */
+int orc_spmm_cli_sched(const char* mtxfile, const char* init_mb_path, int N,
+                       int M, int V, int maxiter, int force_sched,
+                       double* csv16, int* best_sched, int* out_nrows,
+                       int* out_nnz, int** out_row, int** out_col,
+                       float** out_val);
+
 /* Retained-nnz (project metric): N:M = sum over (row, seg) of min(popc, N);
  * V:N:M = per (V-block, seg) keep the 4 columns with most nonzeros (ties to
  * the lower offset), then sum over rows of min(popc(row & kept), N). */

@@ -145,8 +145,10 @@ def test_oracle_cli_matches_reference_command(tmp_path, goldens):
     (tests/golden/cli_ref_goldens.npz: main.cu built from its sources, its
     VNM stage the real reordering.py; temp.mtx in its working directory a
     copy of the input, so the stale first evaluation of main.cu:207 reads
-    the input): the 15 CSV fields other than the time and the output text."""
-    from golden_cases import CLI_CASES, cli_input
+    the input): the 15 CSV fields other than the time and the output text,
+    with the schedule fixed to one of those tied at the largest improve
+    rate (the reference's own pick among them depends on timing)."""
+    from golden_cases import CLI_CASES, cli_input, tied_schedules
     from vnm_gb300 import synth
     p = os.path.join(REPO, "tests", "golden", "cli_ref_goldens.npz")
     if not os.path.exists(p):
@@ -158,9 +160,13 @@ def test_oracle_cli_matches_reference_command(tmp_path, goldens):
             continue
         p = str(tmp_path / (case + ".mtx"))
         synth.write_mtx(p, *cli_input(name, goldens))
-        csv, best, nr, r, c, v = oracle.spmm_cli(p, N, M, V, maxiter, init_mb_path=p)
         want = [float(x) for x in str(g["csv__" + case]).split(",")]
-        np.testing.assert_allclose(csv[:15], want[:15], rtol=1e-5, atol=1e-6, err_msg=case)
-        q = str(tmp_path / (case + "_out.mtx"))
-        oracle.write_mtx(q, nr, nr, r, c, v)
-        assert open(q, "rb").read() == g["out__" + case].tobytes(), case
+        matched = []
+        for s in tied_schedules(p, N, M):
+            csv, best, nr, r, c, v = oracle.spmm_cli(p, N, M, V, maxiter, init_mb_path=p, sched=s)
+            q = str(tmp_path / (case + "_out.mtx"))
+            oracle.write_mtx(q, nr, nr, r, c, v)
+            if np.allclose(csv[:15], want[:15], rtol=1e-5, atol=1e-6) and \
+                    open(q, "rb").read() == g["out__" + case].tobytes():
+                matched.append(s)
+        assert matched, case

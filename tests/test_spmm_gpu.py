@@ -106,6 +106,36 @@ def test_spmm_hybrid_split_and_hub_rows(ctx, n):
     assert err < TOL, (err, info)
 
 
+@pytest.mark.parametrize("n", [64, 192, 256])
+def test_spmm_row_of_hundreds_of_chunks(ctx, n):
+    """A hub row of 60000 nonzeros (235 chunks of 256, more than a thread
+    group of the partial-sum kernel covers in one pass at every n) beside
+    short rows: per-row error against FP64, and two runs bit-identical
+    (the partial rows are added in a fixed order)."""
+    import torch
+    import vnm_gb300
+    nr = 65536
+    rng = np.random.default_rng(11)
+    hub_c = rng.choice(nr, 60000, replace=False)
+    sr = rng.integers(0, nr, 200000)
+    sc = rng.integers(0, nr, 200000)
+    key = np.unique(np.concatenate([np.full(60000, 4321, np.int64) * nr + hub_c, sr.astype(np.int64) * nr + sc]))
+    r, c = (key // nr).astype(np.int32), (key % nr).astype(np.int32)
+    v = rng.standard_normal(len(r)).astype(np.float32)
+    B = torch.randn((nr, n), generator=torch.Generator().manual_seed(3)).to(torch.bfloat16)
+    with _dense_min(RESIDUAL_ONLY):
+        A = vnm_gb300.SpmmMatrix(ctx, nr, r, c, v, 8, 64, "bf16")
+    info = A.info()
+    assert info["split_chunks"] >= 235, info
+    Bd = B.cuda()
+    C1 = A.run(Bd).cpu().numpy()
+    C2 = A.run(Bd).cpu().numpy()
+    assert np.array_equal(C1.view(np.uint32), C2.view(np.uint32))
+    ref = oracle.spmm_f64(nr, r, c, v.astype(np.float64), B.float().numpy().astype(np.float64))
+    err = oracle.rowwise_rel_err(C1.astype(np.float64), ref)
+    assert err < TOL, (err, info)
+
+
 @pytest.mark.parametrize("split", [TENSOR_ONLY, RESIDUAL_ONLY, 4])
 def test_spmm_partial_last_tile_and_empty_tiles(ctx, split):
     nr = 328   # 3 tiles, the last one partly outside the matrix

@@ -1,5 +1,6 @@
-"""A bounded wait inside the round kernel that runs out fails the job with
-VNM_ERR_INTERNAL instead of hanging, and the context keeps working.
+"""A bounded wait inside the round kernel (or the tensor-core SpMM) that
+runs out fails the job (or the call) with VNM_ERR_INTERNAL instead of
+hanging, and the context keeps working.
 
 The walk (one warp) waits for the swap heaps' pops with a poll limit.  The
 test hooks VNM_NM_TEST_HOLD_HEAPS=1 (the heaps publish nothing: a flag that
@@ -65,3 +66,30 @@ def test_walk_wait_that_runs_out_fails_the_job(ctx, goldens, cluster):
             ores, _, _, opos = oracle.nm_run(gnr, gr, gc, gv, 2, 4, s)
             res, pos = ctx.nm_reorder(gnr, gr, gc, gv, 2, 4, s)
             assert np.array_equal(res, ores) and np.array_equal(pos, opos), s
+
+
+def test_spmm_pipeline_wait_that_runs_out_fails_the_call(ctx):
+    """The tensor-core SpMM's pipeline waits (copies -> MMA, MMA -> copies)
+    with a limit of one poll (test hook VNM_SPMM_TEST_WAIT_LIMIT): the
+    kernel stops issuing, lets the copies in flight land (that wait keeps
+    its full limit), skips the epilogue and reports VNM_ERR_INTERNAL; the
+    same operand afterwards gives the oracle's product."""
+    import torch
+    import vnm_gb300
+    from vnm_gb300 import synth
+    nr, r, c, v = synth.vnm_structured(1024, 8, 128, seed=5)  # 32 K-steps a tile: more than the stages
+    B = torch.randn((nr, 128), generator=torch.Generator().manual_seed(2)).to(torch.bfloat16)
+    ref = oracle.spmm_f64(nr, r, c, v.astype(np.float64), B.float().numpy().astype(np.float64))
+    with _env(VNM_SPMM_DENSE_MIN=0):
+        A = vnm_gb300.SpmmMatrix(ctx, nr, r, c, v, 8, 128, "bf16")
+    assert A.info()["residual_nnz"] == 0 and A.info()["ksteps"] > 8
+    Bd = B.cuda()
+    C = A.run(Bd).cpu().numpy().astype(np.float64)  # also picks the column-block width
+    assert oracle.rowwise_rel_err(C, ref) < 1e-2
+    with _env(VNM_SPMM_TEST_WAIT_LIMIT=1):
+        with pytest.raises(vnm_gb300.VnmError) as e:
+            A.run(Bd)
+        assert e.value.status == 6  # VNM_ERR_INTERNAL
+    C = A.run(Bd).cpu().numpy().astype(np.float64)
+    assert oracle.rowwise_rel_err(C, ref) < 1e-2
+    A.close()

@@ -83,7 +83,8 @@ struct NMJob {
   int* touched;       // [R] scratch
   int* res;           // [24]: init_size, final_size, init_cnt, final_cnt, rounds, status,
                       //       swaps, gathered entries (lo, hi), touched rows (lo, hi),
-                      //       [16..22] kilocycles per round phase
+                      //       [16..22] kilocycles per round phase, [23] kilocycles
+                      //       from the kernel's start to its end (leader, thread 0)
   int* trace_pairs;   // optional: swaps in commit order (v1, v2)
   int* trace_rounds;  // optional: pairs committed by the end of each round
   int trace_cap_pairs;
@@ -1335,6 +1336,7 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
   const int rank = cs > 1 ? (int)cl.block_rank() : 0;
   const bool lead = rank == 0;
   const Slice sl{rank, cs};
+  const long long t_start = clock64();
   const NMJob J = jobs[blockIdx.x / cs];
   const int tid = threadIdx.x;
   int* cnt = cnt_in_smem ? smem_cnt : J.cnt;
@@ -1511,6 +1513,7 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     J.res[11] = table_rounds;
     J.res[12] = fallback_rounds;
     for (int q = 0; q < 7; ++q) J.res[16 + q] = (int)(tph[q] >> 10);  // kilocycles
+    J.res[23] = (int)((clock64() - t_start) >> 10);
   }
 }
 
@@ -1884,7 +1887,7 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
   VNM_CUDA_TRY(cudaEventElapsedTime(&ctx->main_ms, ctx->ev_main0, ctx->ev_main1));
   int hres_copy[96];
   memcpy(hres_copy, hres, sizeof(int) * 24 * nsched);
-  for (int q = 0; q < 16; ++q) ctx->stats[q] = 0;
+  for (int q = 0; q < 20; ++q) ctx->stats[q] = 0;
   ctx->stats[3] = P.nseg;
   ctx->stats[4] = nsched;
   ctx->stats[5] = P.np;
@@ -1899,6 +1902,7 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
     for (int q = 0; q < 7; ++q) ctx->stats[8 + q] += h[16 + q];
     ctx->stats[7] += h[11];
     ctx->stats[15] += h[12];
+    ctx->stats[16] += h[23];
   }
   if (trace) {
     const int committed = hres_copy[6];
@@ -2087,7 +2091,7 @@ static vnm_status run_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int6
   }
   VNM_TRY(end_call(ctx));
   VNM_CUDA_TRY(cudaEventElapsedTime(&ctx->main_ms, ctx->ev_main0, ctx->ev_main1));
-  for (int q = 0; q < 16; ++q) ctx->stats[q] = 0;
+  for (int q = 0; q < 20; ++q) ctx->stats[q] = 0;
   ctx->stats[3] = max_nseg;
   ctx->stats[4] = nmat;
   ctx->stats[5] = P.np;
@@ -2099,6 +2103,7 @@ static vnm_status run_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int6
     ctx->stats[1] += (long long)h[7] + ((long long)h[8] << 31);
     ctx->stats[2] += (long long)h[9] + ((long long)h[10] << 31);
     for (int q = 0; q < 7; ++q) ctx->stats[8 + q] += h[16 + q];
+    ctx->stats[16] += h[23];
   }
   return VNM_OK;
 }

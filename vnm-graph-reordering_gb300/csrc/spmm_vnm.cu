@@ -26,8 +26,11 @@
 //     V rows), and the epilogue multiplies each output row back by it.
 //   - the nonzeros of sparser blocks form the residual: a row-major CSR with
 //     FP32 values, cut into tasks of at most 256 nonzeros of one row (a row
-//     with more is split into up to 32 chunks whose partial rows are added
-//     in chunk order afterwards, so the sums do not depend on timing).
+//     with more is split into chunks whose partial rows are added in a fixed
+//     order afterwards, so the sums do not depend on timing).  No cap on the
+//     chunks of a row: on a power-law graph (Chung-Lu 262144, max degree
+//     72098, n=256) a cap of 32 left one warp walking 2254 entries while the
+//     other SMs idled: 0.60 ms a product on GB300, 0.39 ms without the cap.
 // On graph sparsity most blocks hold one or two nonzeros; a 128 x 16
 // tensor-core tile for them would be >99 % padding, while a CUDA-core
 // gather reads one B row per nonzero.  `dense_min` (VNM_SPMM_DENSE_MIN in the
@@ -92,7 +95,6 @@ constexpr int SP_KSTEP_BYTES = 4096;
 constexpr int SP_THREADS = 128;
 constexpr uint32_t SP_WAIT_LIMIT = 1u << 22;  // polls before a wait gives up
 constexpr int RES_CHUNK = 256;    // residual nonzeros per task, at most
-constexpr int RES_MAXCH = 32;     // chunks of one row, at most
 constexpr int RES_THREADS = 256;
 constexpr int RES_U = 8;          // entries in flight per lane group (8 measured ahead of 4)
 // A block runs on the tensor cores when it holds at least V nonzeros (one
@@ -263,12 +265,10 @@ __global__ void k_res_gather(const int* src, const int* col, const float* val, i
 // Residual tasks of a row: none when its tile runs on the tensor cores and
 // holds no residual entry (the tensor kernel then writes the rows), else one
 // per chunk of at most RES_CHUNK entries (one task for an empty row, which
-// writes zeros), at most RES_MAXCH chunks.
+// writes zeros).
 __device__ __forceinline__ int res_chunks(int len, bool needed) {
   if (!needed) return 0;
-  if (len <= RES_CHUNK) return 1;
-  const int c = (len + RES_CHUNK - 1) / RES_CHUNK;
-  return c < RES_MAXCH ? c : RES_MAXCH;
+  return len <= RES_CHUNK ? 1 : (len + RES_CHUNK - 1) / RES_CHUNK;
 }
 
 __global__ void k_res_task_count(const int* rptr, int R, const int* tile_has, const int* tile_res, int* nmt, int* nst,
@@ -463,20 +463,52 @@ __global__ void __launch_bounds__(RES_THREADS)
   }
 }
 
-// C row of a split row = its partial rows added in chunk order.
-__global__ void k_spmm_fin(const int4* __restrict__ multi, const float* __restrict__ P, int ldp, float* C, int ldc,
-                           int n) {
+// C row of a split row = the sum of its partial rows in a fixed order: the
+// block's threads cover the row's float4 columns qpb at a time, and the
+// ng = FIN_THREADS / qpb thread groups of a column sum every ng-th chunk
+// (group g: chunks g, g + ng, ...) before the group sums are added in group
+// order.  A row of a few hundred chunks (a hub of a power-law graph) is then
+// not one thread's serial chain of loads.
+constexpr int FIN_THREADS = 256;
+__device__ __forceinline__ void add4(float4& s, const float4 x) {
+  s.x += x.x;
+  s.y += x.y;
+  s.z += x.z;
+  s.w += x.w;
+}
+__global__ void __launch_bounds__(FIN_THREADS)
+    k_spmm_fin(const int4* __restrict__ multi, const float* __restrict__ P, int ldp, float* C, int ldc, int n) {
+  __shared__ float4 red[FIN_THREADS];
   const int4 m = multi[blockIdx.x];
-  for (int q = threadIdx.x; q < n / 4; q += blockDim.x) {
+  const int nq = n / 4;
+  const int qpb = nq < FIN_THREADS ? nq : FIN_THREADS;
+  const int ng = FIN_THREADS / qpb;
+  const int g = threadIdx.x / qpb, qi = threadIdx.x % qpb;
+  for (int q0 = 0; q0 < nq; q0 += qpb) {
+    const int q = q0 + qi;
     float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int j = 0; j < m.z; ++j) {
-      const float4 x = reinterpret_cast<const float4*>(P + (size_t)(m.y + j) * ldp)[q];
-      s.x += x.x;
-      s.y += x.y;
-      s.z += x.z;
-      s.w += x.w;
+    if (g < ng && q < nq) {
+      const float4* src = reinterpret_cast<const float4*>(P + (size_t)m.y * ldp) + q;
+      const size_t step = (size_t)ng * (ldp / 4);
+      int j = g;
+      for (; j + 3 * ng < m.z; j += 4 * ng) {  // four loads in flight, added in chunk order
+        const float4 x0 = src[(size_t)j * (ldp / 4)], x1 = src[(size_t)j * (ldp / 4) + step],
+                     x2 = src[(size_t)j * (ldp / 4) + 2 * step], x3 = src[(size_t)j * (ldp / 4) + 3 * step];
+        add4(s, x0);
+        add4(s, x1);
+        add4(s, x2);
+        add4(s, x3);
+      }
+      for (; j < m.z; j += ng) add4(s, src[(size_t)j * (ldp / 4)]);
     }
-    reinterpret_cast<float4*>(C + (size_t)m.x * ldc)[q] = s;
+    red[threadIdx.x] = s;
+    __syncthreads();
+    if (g == 0 && q < nq) {
+      float4 t = red[qi];
+      for (int h = 1; h < ng; ++h) add4(t, red[h * qpb + qi]);
+      reinterpret_cast<float4*>(C + (size_t)m.x * ldc)[q] = t;
+    }
+    __syncthreads();
   }
 }
 
@@ -495,6 +527,7 @@ struct SpmmArgs {
   int R, n, ldc;
   uint32_t idesc;
   int* err;
+  uint32_t wait_limit;  // polls of a pipeline wait (copies <-> MMAs) before it gives up
 };
 
 // K-steps in flight per CTA.  16 stages were measured slower on a full
@@ -511,9 +544,16 @@ struct SpmmSmem {
   alignas(8) uint64_t full[SP_STAGES];
   alignas(8) uint64_t empty[SP_STAGES];
   alignas(8) uint64_t done;
+  int last_k[SP_STAGES];  // the last K-step whose copies were issued into each stage
   uint32_t tmem_base;
   int abort;
 };
+
+// Warps that issue the copies: every warp but warp 1, whose lane 0 issues
+// the MMAs.  K-step i is copied by producer i % SP_PRODUCERS.  One producer
+// warp left the tensor pipe idle ~80 % of the time on a full V:2:8 operand
+// (16 B-row copies, their shuffles and addresses per K-step on one warp).
+constexpr int SP_PRODUCERS = SP_THREADS / 32 - 1;
 
 template <int NT>
 __global__ void __launch_bounds__(SP_THREADS, 1)
@@ -532,6 +572,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
     for (int s = 0; s < SP_STAGES; ++s) {
       ptx::mbar_init(&sm.full[s], 1 + 32);  // the A copy's expect-tx arrival + one per producer lane
       ptx::mbar_init(&sm.empty[s], 1);
+      sm.last_k[s] = -1;
     }
     ptx::mbar_init(&sm.done, 1);
     sm.abort = 0;
@@ -546,34 +587,41 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
   ptx::tc_fence_after();
   const uint32_t tmem = sm.tmem_base;
 
-  int issued = 0;  // K-steps whose copies were issued (producer warp)
   if (nsteps > 0) {
-    if (warp == 0) {
-      // producer warp.  Lane l holds column id (l & 15) of K-step
-      // i + 2q + (l >> 4) for the SP_PF pairs q ahead (coalesced 128-byte
-      // loads issued 2*SP_PF steps before use); lane 0 issues the A tile by
-      // bulk copy, and every lane copies its 16-byte pieces of the 16 B rows.
+    if (warp != 1) {
+      // producer warps.  Producer pw copies K-steps pw, pw + P, pw + 2P, ...
+      // (P = SP_PRODUCERS), two at a time.  Lane l holds column id (l & 15)
+      // of the (l >> 4)-th K-step of each of the SP_PF pairs ahead
+      // (coalesced 64-byte loads issued well before use); lane 0 issues the
+      // A tile by bulk copy, and every lane copies its 16-byte pieces of the
+      // 16 B rows.
+      const int pw = warp == 0 ? 0 : warp - 1;
+      constexpr int P = SP_PRODUCERS;
       const uint64_t pol_a = ptx::policy_evict_first(), pol_b = ptx::policy_evict_last();
       int pf[SP_PF];
 #pragma unroll
       for (int q = 0; q < SP_PF; ++q) {
-        const int st = 2 * q + (lane >> 4);
+        const int st = pw + P * (2 * q + (lane >> 4));
         pf[q] = st < nsteps ? p.cols[(size_t)(s0 + st) * 16 + (lane & 15)] : 0;
       }
       bool stop = false;
-      for (int i = 0; i < nsteps && !stop; i += 2) {
+      for (int j = 0; pw + P * j < nsteps && !stop; j += 2) {
         const int cur = pf[0];
 #pragma unroll
         for (int q = 0; q + 1 < SP_PF; ++q) pf[q] = pf[q + 1];
         {
-          const int st = i + 2 * SP_PF + (lane >> 4);
+          const int st = pw + P * (j + 2 * SP_PF + (lane >> 4));
           pf[SP_PF - 1] = st < nsteps ? p.cols[(size_t)(s0 + st) * 16 + (lane & 15)] : 0;
         }
-        for (int d = 0; d < 2 && i + d < nsteps; ++d) {
-          const int ii = i + d, s = ii % SP_STAGES;
+        for (int d = 0; d < 2; ++d) {
+          const int ii = pw + P * (j + d), s = ii % SP_STAGES;
+          if (ii >= nsteps) break;
           int ok = 1;
-          if (lane == 0 && ii >= SP_STAGES)
-            ok = ptx::mbar_wait(&sm.empty[s], ((ii / SP_STAGES) - 1) & 1, SP_WAIT_LIMIT) ? 1 : 0;
+          if (lane == 0) {
+            if (*reinterpret_cast<volatile int*>(&sm.abort)) ok = 0;
+            else if (ii >= SP_STAGES)
+              ok = ptx::mbar_wait(&sm.empty[s], ((ii / SP_STAGES) - 1) & 1, p.wait_limit) ? 1 : 0;
+          }
           ok = __shfl_sync(0xffffffffu, ok, 0);
           if (!ok) {
             if (lane == 0) {
@@ -584,6 +632,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             break;
           }
           if (lane == 0) {
+            sm.last_k[s] = ii;
             // A tiles are read once: evict-first, so that they do not push
             // the B rows (read by every tile) out of L2
             ptx::mbar_arrive_expect_tx(&sm.full[s], SP_KSTEP_BYTES);
@@ -611,14 +660,13 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             ptx::cp_async_mbar_arrive(&sm.full[s]);
           }
           __syncwarp();
-          issued = ii + 1;
         }
       }
     } else if (tid == 32) {
       // MMA issuer
       for (int i = 0; i < nsteps; ++i) {
         const int s = i % SP_STAGES;
-        if (!ptx::mbar_wait(&sm.full[s], (i / SP_STAGES) & 1, SP_WAIT_LIMIT)) {
+        if (!ptx::mbar_wait(&sm.full[s], (i / SP_STAGES) & 1, p.wait_limit)) {
           atomicOr(p.err, 2);
           sm.abort = 1;
           break;
@@ -638,10 +686,12 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
     // everybody waits for the last MMA
     bool ok = ptx::mbar_wait(&sm.done, 0, SP_WAIT_LIMIT);
     if (!ok && tid == 0) atomicOr(p.err, 4);
-    if (tid == 0 && issued < nsteps && issued > 0) {
-      // the producer stopped early: let its last copies land before exit
-      for (int i = (issued > SP_STAGES ? issued - SP_STAGES : 0); i < issued; ++i)
-        ptx::mbar_wait(&sm.full[i % SP_STAGES], (i / SP_STAGES) & 1, SP_WAIT_LIMIT);
+    __syncthreads();
+    if (tid == 0 && (sm.abort || !ok)) {
+      // a wait gave up: let every stage's last issued copies land before exit
+      // (the last K-step of a stage is the only one whose phase can be open)
+      for (int s = 0; s < SP_STAGES; ++s)
+        if (sm.last_k[s] >= 0) ptx::mbar_wait(&sm.full[s], (sm.last_k[s] / SP_STAGES) & 1, SP_WAIT_LIMIT);
     }
     __syncthreads();
     ptx::tc_fence_after();
@@ -686,6 +736,18 @@ static int spmm_dense_min(int V) {
     if (v >= 0) return v;
   }
   return V;
+}
+
+// Poll limit of the tensor kernel's pipeline waits.  A test hook,
+// VNM_SPMM_TEST_WAIT_LIMIT, sets a small one so that a wait runs out and the
+// kernel takes its error path (stop issuing, let the copies in flight land,
+// report); the wait for the last MMA and the drain keep the full limit.
+static uint32_t spmm_wait_limit() {
+  if (const char* e = getenv("VNM_SPMM_TEST_WAIT_LIMIT")) {
+    const long v = atol(e);
+    if (v > 0) return (uint32_t)v;
+  }
+  return SP_WAIT_LIMIT;
 }
 
 // Arena bytes compress_t takes for nnz entries and R rows.
@@ -978,6 +1040,7 @@ static vnm_status spmm_enqueue(vnm_ctx* ctx, const vnm_spmm_matrix* A, const voi
   p.n = n;
   p.ldc = n;
   p.err = err;
+  p.wait_limit = spmm_wait_limit();
   // the CUDA-core part: lanes per task so that 8 columns a lane tile n
   auto launch_res = [&]() -> vnm_status {
     if (A->ntask > 0) {
@@ -998,10 +1061,7 @@ static vnm_status spmm_enqueue(vnm_ctx* ctx, const vnm_spmm_matrix* A, const voi
       }
 #undef VNM_RES
     }
-    if (A->nmulti > 0) {
-      const int nt = n / 4 < 256 ? ((n / 4 + 31) / 32) * 32 : 256;
-      VNM_LAUNCH(ctx, k_spmm_fin, A->nmulti, nt, 0, A->multi, P, n, dC, n, n);
-    }
+    if (A->nmulti > 0) VNM_LAUNCH(ctx, k_spmm_fin, A->nmulti, FIN_THREADS, 0, A->multi, P, n, dC, n, n);
     return VNM_OK;
   };
   const long long key[3] = {A->R, A->nsteps, n};

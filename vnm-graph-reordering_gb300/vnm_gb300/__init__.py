@@ -151,13 +151,14 @@ class Context:
         return lib().vnm_last_main_kernel_ms(self.h)
 
     def last_stats(self):
-        out = (ctypes.c_longlong * 16)()
-        _check(lib().vnm_last_stats(self.h, out, 16), "vnm_last_stats")
+        out = (ctypes.c_longlong * 20)()
+        _check(lib().vnm_last_stats(self.h, out, 20), "vnm_last_stats")
         keys = ("rounds", "gathered", "touched", "nseg", "jobs", "pattern_nnz", "blocks_per_job", "table_rounds")
         d = dict(zip(keys, list(out)[:8]))
         d["phase_kcycles"] = dict(zip(("select", "choose", "gather", "process", "heap_entries", "heaps_and_walk", "apply"),
                                       list(out)[8:15]))
         d["table_fallback_rounds"] = out[15]
+        d["kernel_kcycles"] = out[16]
         return d
 
     # ---- array plumbing: numpy arrays (host) or torch CUDA tensors (device)
