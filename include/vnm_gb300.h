@@ -13,7 +13,9 @@
  *   - Matrices are COO, 0-based, int32 indices, float32 values, square with
  *     `nrows` already padded to a multiple of M (as Mtx::init_from_file does),
  *     sorted by (row, col) with no repeated (row, col) -- the state a matrix
- *     is in after the reference's reader (mtx/readMtx.hpp:354-425).
+ *     is in after the reference's reader (mtx/readMtx.hpp:354-425).  The NM
+ *     calls take nrows < 2^27 (a batch: the sum of its nrows), else
+ *     VNM_ERR_LIMIT.
  *   - `mem` says where the caller's arrays live: VNM_MEM_HOST (pageable or
  *     pinned host memory; the call copies them) or VNM_MEM_DEVICE (device
  *     memory of the context's GPU; nothing is copied).
@@ -74,13 +76,19 @@ float vnm_last_main_kernel_ms(const vnm_ctx* ctx);
  * out[0] rounds summed over jobs, out[1] column entries gathered,
  * out[2] row records touched, out[3] segments per job, out[4] jobs,
  * out[5] nonzero-valued entries of the pattern, out[6] thread blocks per
- * job (the cluster size the launch used), out[7] rounds whose row records
- * were in shared-memory tables (summed over jobs), out[8..14] kilocycles
- * spent per round phase (select, choose, gather, process, heap entries,
- * swap heaps and walk overlapped, apply) summed over jobs, out[15] rounds
- * whose tables ran out of slots and gathered into global memory instead,
- * out[16] kilocycles from the round kernel's start to its end summed over
- * jobs (out[8..14] plus the set-up and the final write-back).
+ * job (the cluster size the launch used), out[7] block-rounds whose row
+ * records were in the block's shared-memory table (a block keeps the
+ * records of the rows it owns; summed over blocks and jobs), out[8..14]
+ * kilocycles spent per round phase (select, choose, gather, process, heap
+ * entries, swap heaps and walk overlapped, apply) summed over jobs,
+ * out[15] block-rounds whose row records were in global memory (the
+ * block's entries would have filled more than 3/4 of its table), out[16]
+ * kilocycles from the round kernel's start to its end summed over jobs
+ * (out[8..14] plus the set-up and the final write-back), out[17] the
+ * spread of the jobs' start times and out[18] the span from the first
+ * start to the last end, in microseconds (jobs that run at once start
+ * together), out[19] how many clusters of the launched size the GPU can
+ * hold at once by the occupancy query (0 for single-block launches).
  * n <= 20 values. */
 vnm_status vnm_last_stats(const vnm_ctx* ctx, long long* out, int n);
 
@@ -160,7 +168,7 @@ vnm_status vnm_nm_get_trace(vnm_ctx* ctx, int* pairs, int cap_pairs, int* npairs
  *     streams or host threads) race; serialise them. */
 #define VNM_NOALLOC_MAX_ROWS 32768
 #define VNM_NOALLOC_MAX_NNZ 524288
-#define VNM_NOALLOC_SCRATCH_BYTES (10u << 20)
+#define VNM_NOALLOC_SCRATCH_BYTES (16u << 20)
 vnm_status vnm_nm_reorder_noalloc(int nrows, int nnz, const int* row, const int* col, const float* val, int N, int M,
                                   int sched, int nm_maxiter, int* res5, int* newpos, void* stream);
 

@@ -129,24 +129,29 @@ def test_errors_are_reported(ctx):
 @pytest.mark.parametrize("M", [4, 8])
 def test_cluster_sizes_agree(ctx, M, table):
     """Each job runs on a thread-block cluster whose size depends on the
-    matrix, with the round's row records in the blocks' shared-memory tables
-    (each row owned by one block, reached over DSMEM) or, with
-    VNM_NM_CLUSTER_TABLE=0, in global memory; every size and both places
-    give the oracle's result bit for bit."""
+    matrix; each block owns the rows whose group (row & 15 rotated by a hash
+    of the higher bits) is in its share of the 16 and keeps their records
+    in its shared-memory table or, with
+    VNM_NM_ROW_TABLE=0, in global memory; every size and both places give
+    the oracle's result bit for bit."""
     import os
     from vnm_gb300 import synth
     n, r, c, v = synth.rmat(12, 4096 * 8, 17 + M, "normal")
     ores, _, _, opos = oracle.nm_run(n, r, c, v, 2, M, 1)
-    old = {k: os.environ.get(k) for k in ("VNM_NM_CLUSTER", "VNM_NM_CLUSTER_TABLE")}
+    old = {k: os.environ.get(k) for k in ("VNM_NM_CLUSTER", "VNM_NM_ROW_TABLE")}
     try:
-        os.environ["VNM_NM_CLUSTER_TABLE"] = table
+        os.environ["VNM_NM_ROW_TABLE"] = table
         for cs in ("1", "2", "4", "8", "16"):
             os.environ["VNM_NM_CLUSTER"] = cs
             res, newpos = ctx.nm_reorder(n, r, c, v, 2, M, 1)
             assert np.array_equal(res, ores), cs
             assert np.array_equal(newpos, opos), cs
-            if cs != "1" and table == "1":
-                assert ctx.last_stats()["table_rounds"] > 0
+            st = ctx.last_stats()
+            assert st["blocks_per_job"] == int(cs)
+            if table == "1":
+                assert st["table_rounds"] > 0, st
+            else:
+                assert st["table_rounds"] == 0 and st["global_rounds"] == res[4] * int(cs), st
     finally:
         for k, v0 in old.items():
             if v0 is None:
@@ -207,29 +212,31 @@ def test_other_group_sizes_match_oracle(ctx, M):
             os.environ["VNM_NM_CLUSTER"] = old
 
 
-def test_table_overflow_falls_back_to_global_records(ctx):
-    """With VNM_NM_CLUSTER_TABLE=1 cluster jobs keep a round's row records in
-    the blocks' shared-memory tables, row r in block r % 16.  Here the only invalid segment touches
-    4608 rows that are all multiples of 16, more than block 0's 4096 slots:
-    that block's table overflows, the round gathers into global memory
-    instead, and the result is still the oracle's."""
+def test_uneven_rows_mix_table_and_global_records(ctx):
+    """With clusters of 16 blocks, block b owns the rows of group b
+    (row_group).  Here the only invalid segment touches 4608 rows that all
+    fall in group 0: block 0's entries are more than 3/4 of its table, so it
+    keeps its records in global memory while the other blocks use their
+    tables in the same rounds, and the result is still the oracle's."""
     import os
     R = 81920
-    rows = np.arange(4608, dtype=np.int64) * 16
+    hi = np.arange(4608, dtype=np.uint64)
+    rot = ((hi * np.uint64(2654435761)) & np.uint64(0xffffffff)) >> np.uint64(28)  # row_group's rotation
+    rows = (hi * np.uint64(16) + ((np.uint64(16) - rot) & np.uint64(15))).astype(np.int64)  # one group-0 row per 16
     r = np.concatenate([np.repeat(rows, 3), rows])
     c = np.concatenate([np.tile([0, 1, 2], len(rows)), np.full(len(rows), 5)])  # three nodes of segment 0, one of 1
     key = np.unique(r * R + c)
     r, c = (key // R).astype(np.int32), (key % R).astype(np.int32)
     v = np.ones(len(r), np.float32)
     ores, _, _, opos = oracle.nm_run(R, r, c, v, 2, 4, 0)
-    old = {k: os.environ.get(k) for k in ("VNM_NM_CLUSTER", "VNM_NM_CLUSTER_TABLE")}
+    old = {k: os.environ.get(k) for k in ("VNM_NM_CLUSTER", "VNM_NM_ROW_TABLE")}
     try:
         os.environ["VNM_NM_CLUSTER"] = "16"
-        os.environ["VNM_NM_CLUSTER_TABLE"] = "1"
+        os.environ.pop("VNM_NM_ROW_TABLE", None)
         res, newpos = ctx.nm_reorder(R, r, c, v, 2, 4, 0)
         st = ctx.last_stats()
         assert st["blocks_per_job"] == 16
-        assert st["table_fallback_rounds"] > 0, st
+        assert st["global_rounds"] > 0 and st["table_rounds"] > 0, st
         assert np.array_equal(res, ores) and np.array_equal(newpos, opos)
     finally:
         for k, v0 in old.items():

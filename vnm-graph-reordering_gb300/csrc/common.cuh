@@ -66,6 +66,7 @@ struct vnm_ctx {
   float last_ms = 0.f;
   float main_ms = 0.f;
   long long stats[20] = {0};  // work counters of the last call
+  int last_clusters_fit = 0;  // clusters of the launched size the GPU can hold at once (occupancy query)
   int launches = 0;
   int last_cluster = 1;  // blocks per job of the last NM round launch
   // SpMM column-block widths measured fastest, by (rows, K-steps, B width)
@@ -133,7 +134,8 @@ struct Pattern {
   int* prow = nullptr;
   int* pcol = nullptr;
   int* cptr = nullptr;
-  int* crow = nullptr;
+  int* crow = nullptr;    // rows of each column, grouped by row group (nm_reorder.cu row_group)
+  int* csplit = nullptr;  // [16 R + 1] start of each (column, row group) in crow
   int* inv0 = nullptr;
   int* pres0 = nullptr;
 };

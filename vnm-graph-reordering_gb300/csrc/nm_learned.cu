@@ -994,7 +994,7 @@ vnm_status vnm_nm_learned(vnm_ctx* ctx, int nrows, int nnz, const int* row, cons
   if (nrows < 0 || nnz < 0 || (nrows % M) != 0) return VNM_ERR_ARG;
   if (mem != VNM_MEM_HOST && mem != VNM_MEM_DEVICE) return VNM_ERR_ARG;
   if (nnz > 0 && (!row || !col || !val)) return VNM_ERR_ARG;
-  if (nrows > (1 << 28)) return VNM_ERR_LIMIT;
+  if (nrows >= (1 << 27)) return VNM_ERR_LIMIT;  // 16 nrows + 1 row groups fit an int
   const int mode = prm->mode, KT = prm->targets;
   if (mode < VNM_LEARNED_MLP || mode > VNM_LEARNED_RANDOM) return VNM_ERR_ARG;
   if (mode == VNM_LEARNED_MLP && !net) return VNM_ERR_ARG;

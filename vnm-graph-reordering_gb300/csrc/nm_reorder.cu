@@ -62,12 +62,26 @@ constexpr unsigned FULL = 0xffffffffu;
 constexpr int JOB_OK = 0;
 constexpr int JOB_EMPTY_HEAP = 1;   // reference would call top() on an empty queue
 constexpr int JOB_WAIT_LIMIT = 4;   // the walk waited too long for a swap heap's pops
+constexpr int JOB_TABLE_FULL = 8;   // a row found no free table slot (cannot happen: at most 3/4 are taken)
 
 // The part of a job's row work one thread block does: block `rank` of the
-// `cs` blocks (a thread-block cluster) that share the job.
+// `cs` blocks (a thread-block cluster, cs a power of two <= 16) that share
+// the job.  Rows are dealt to blocks in 16 groups: block `rank` owns the
+// rows whose group lies in [rank * 16 / cs, (rank + 1) * 16 / cs).
 struct Slice {
   int rank, cs;
 };
+constexpr int ROW_GROUPS = 16;
+
+// A row's group: row & 15 rotated by a hash of row >> 4.  Within every
+// aligned run of 16 rows each group occurs once, so a window of n rows puts
+// at most ceil(n / 16) + 1 in a group; and the rows that share their low
+// bits land in different groups.  (row & 15 alone gave the block owning
+// group 0 the R-MAT hubs, whose low bits are 0: find_best at R-MAT 16384
+// 2:4 took 13.6 ms.)
+__host__ __device__ __forceinline__ int row_group(int row) {
+  return (int)(((unsigned)row + (((unsigned)row >> 4) * 2654435761u >> 28)) & (ROW_GROUPS - 1));
+}
 
 struct NMJob {
   int R;              // padded rows = columns
@@ -75,14 +89,20 @@ struct NMJob {
   int sched;          // 0..3
   int maxiter;        // reorderUtil MAXITER before it is raised to init_size
   const int* cptr;    // [R+1] column pointers of the nonzero pattern (original ids)
-  const int* crow;    // rows of each column
+  const int* crow;    // rows of each column, grouped by row_group
+  const int* csplit;  // [16 R + 1] start of each (column, row group) in crow
   int* orig;          // [R] original node at each position (identity on entry)
   int* cnt;           // [nseg] invalid rows per segment
   int* zc;            // [nseg] all-zero rows per segment
   uint4* rec;         // [R] per-row scratch, zero on entry and on exit
-  int* touched;       // [R] scratch
+  int* touched;       // [R + 32] scratch: block `rank` lists its touched rows from
+                      //   rank * (ceil(R / 16) + 1) * (16 / cs) on
   int* res;           // [24]: init_size, final_size, init_cnt, final_cnt, rounds, status,
                       //       swaps, gathered entries (lo, hi), touched rows (lo, hi),
+                      //       [11] block-rounds with the records in a shared-memory
+                      //       table, [12] block-rounds with them in global memory,
+                      //       [13], [14] the job's start and end on the global timer
+                      //       (units of 1024 ns, low 31 bits),
                       //       [16..22] kilocycles per round phase, [23] kilocycles
                       //       from the kernel's start to its end (leader, thread 0)
   int* trace_pairs;   // optional: swaps in commit order (v1, v2)
@@ -117,24 +137,33 @@ __global__ void k_nonzero_flags(const float* val, int nnz, int* flags) {
     flags[i] = val[i] != 0.0f;  // reorder/reorder.h:93: the bitmap bit is (val != 0)
 }
 
-// Keep the entries with nonzero value, in order; count entries per column.
+// Keep the entries with nonzero value, in order; count entries per
+// (column, row group).
 __global__ void k_compact(const int* row, const int* col, const float* val, const int* pos, int nnz, int* prow,
-                          int* pcol, int* coldeg) {
+                          int* pcol, int* gdeg) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += gridDim.x * blockDim.x) {
     if (val[i] != 0.0f) {
       int p = pos[i];
       prow[p] = row[i];
       pcol[p] = col[i];
-      atomicAdd(&coldeg[col[i]], 1);
+      atomicAdd(&gdeg[(size_t)ROW_GROUPS * col[i] + row_group(row[i])], 1);
     }
   }
 }
 
-__global__ void k_csc_scatter(const int* prow, const int* pcol, int np, const int* cptr, int* cfill, int* crow) {
+// cptr[c] = the start of column c's first group (c = 0 .. R)
+__global__ void k_cptr_from_split(const int* csplit, int R, int* cptr) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c <= R; c += gridDim.x * blockDim.x)
+    cptr[c] = csplit[(size_t)ROW_GROUPS * c];
+}
+
+// Column lists of the pattern, each grouped by row_group (the order inside
+// a group is whatever the atomics give; nothing depends on it).
+__global__ void k_csc_scatter(const int* prow, const int* pcol, int np, const int* csplit, int* cfill, int* crow) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
-    int c = pcol[i];
-    int slot = atomicAdd(&cfill[c], 1);
-    crow[cptr[c] + slot] = prow[i];
+    const size_t g = (size_t)ROW_GROUPS * pcol[i] + row_group(prow[i]);
+    const int slot = atomicAdd(&cfill[g], 1);
+    crow[csplit[g] + slot] = prow[i];
   }
 }
 
@@ -203,8 +232,8 @@ struct RoundSmem {
   int use_table;    // this round's records are in `table` (else in J.rec)
   int* tlist;       // the slots of `table` claimed this round, densely (ts_max entries)
   int tcount;       // how many
-  int tover;        // a block's table ran out of slots this round (the leader's copy is read)
-  int tfall;        // ... so this round gathers into global memory after all
+  int toff;         // this block's part of J.touched
+  unsigned long long acc[4];  // leader: the helpers' work counters, added at the end
   uint4* rcache;    // the process phase's first pass of touched rows, kept for the apply phase
   int* rcrow;       //   (NM_THREADS x 4 records and their rows), or null
   int status;
@@ -525,19 +554,23 @@ __device__ void clear_round_smem(RoundSmem<M>& sm) {
   if (threadIdx.x == 0) {
     sm.ntouched = 0;
     sm.nswaps = 0;
-    sm.tover = 0;
   }
 }
 
-// OR the bitmaps of the round's segments into per-row records.
+// OR the bitmaps of the round's segments into the records of the rows this
+// block owns.  Every column's rows are stored grouped by row_group (csplit),
+// so the block's entries of a column are one contiguous run of it, and no
+// other block touches these records: the process and apply phases that
+// follow need no cluster barrier.  The records go to the block's
+// shared-memory table when its entries fill at most 3/4 of it, else to
+// J.rec in global memory.
 template <int M>
-__device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J, Slice sl = Slice{0, 1}, int* ntp = nullptr,
-                             bool force_global = false) {
+__device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J, Slice sl = Slice{0, 1}) {
   constexpr int K = M + 1;
   const int tid = threadIdx.x;
-  if (!ntp) ntp = &sm.ntouched;
   const int KM = sm.K_ * M;
-  if (tid < 32) {  // columns of the round and their prefix sums, on one warp
+  const int g0 = sl.rank * (ROW_GROUPS / sl.cs), g1 = g0 + ROW_GROUPS / sl.cs;
+  if (tid < 32) {  // this block's run of each column of the round and their prefix sums, on one warp
     constexpr int CPL = (K * M + 31) / 32;  // columns per lane
     int len[CPL], tot = 0;
 #pragma unroll
@@ -546,9 +579,9 @@ __device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J, Slice sl = Slice{
       len[q] = 0;
       if (col < KM) {
         const int u = J.orig[sm.xseg[col / M] * M + col % M];
-        const int b = J.cptr[u];
+        const int b = J.csplit[(size_t)ROW_GROUPS * u + g0];
         sm.colstart[col] = b;
-        len[q] = J.cptr[u + 1] - b;
+        len[q] = J.csplit[(size_t)ROW_GROUPS * u + g1] - b;
       }
       tot += len[q];
     }
@@ -568,31 +601,20 @@ __device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J, Slice sl = Slice{
     if (tid == 31) {
       sm.colpre[KM] = incl;
       sm.E = incl;
-      // a single block's table takes the round when it can hold every row
-      // (E <= 3/4 of it); a cluster's tables when the expected load of
-      // each is at most half (rows are dealt by row % cs), with the
-      // overflow fallback of the round loop behind it
-      sm.use_table = !force_global && sm.ts_max > 0 &&
-                     (sl.cs == 1 ? incl <= (sm.ts_max >> 2) * 3 : incl <= (sm.ts_max >> 1) * sl.cs);
+      sm.use_table = sm.ts_max > 0 && incl <= (sm.ts_max >> 2) * 3;
     }
   }
   __syncthreads();
   const int E = sm.E;
   if (sm.use_table) {
     // open addressing, linear probing; a slot is claimed by CAS on its row
-    // key and appended to its table's list of claimed slots, which the
-    // process and apply phases walk in full 32-row chunks.  In a cluster,
-    // row r's record lives in the table of block r % cs (reached over
-    // DSMEM), so each block later processes and clears the rows it owns
-    // from its own shared memory; the entries are dealt over every thread
-    // of the cluster.  A cluster entry that finds no free slot within 64
-    // probes raises the leader's overflow flag instead (the round loop then
-    // redoes the gather into global memory).
+    // key and appended to the list of claimed slots, which the process and
+    // apply phases walk in full 32-row chunks.  At most 3/4 of the slots
+    // are taken, so a free one is always found.
     const unsigned mask = (unsigned)sm.ts_max - 1u;
-    const int plim = sl.cs > 1 ? 64 : (int)mask + 1;
-    const int gthreads = sl.cs * NM_THREADS;
-    for (int e = sl.rank * NM_THREADS + tid; e < E; e += gthreads) {
-      int lo = 0, hi = KM - 1;
+    unsigned* tw = reinterpret_cast<unsigned*>(sm.table);
+    for (int e = tid; e < E; e += NM_THREADS) {
+      int lo = 0, hi = KM - 1;  // last q with colpre[q] <= e
       while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
         if (sm.colpre[mid] <= e) lo = mid;
@@ -601,49 +623,37 @@ __device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J, Slice sl = Slice{
       const int q = lo, xi = q / M, k = q % M;
       const int row = J.crow[sm.colstart[q] + (e - sm.colpre[q])];
       const unsigned key = (unsigned)row + 1u;
-      unsigned* tw = reinterpret_cast<unsigned*>(sm.table);
-      int* tl = sm.tlist;
-      int* tc = &sm.tcount;
-      if (sl.cs > 1) {
-        cg::cluster_group cl = cg::this_cluster();
-        const unsigned owner = (unsigned)(row % sl.cs);
-        tw = cl.map_shared_rank(tw, owner);
-        tl = cl.map_shared_rank(tl, owner);
-        tc = cl.map_shared_rank(tc, owner);
-      }
       unsigned h = (key * 2654435761u) >> sm.ts_shift;
       bool placed = false;
-      for (int probe = 0; probe < plim; ++probe) {
+      for (int probe = 0; probe <= (int)mask; ++probe) {
         const unsigned cur = atomicCAS(&tw[4 * h + 3], 0u, key);
         if (cur == 0u || cur == key) {
           atomicOr(&tw[4 * h + (xi >> 2)], (1u << k) << ((xi & 3) * 8));
-          if (cur == 0u) {
-            tl[atomicAdd(tc, 1)] = (int)h;
-            atomicAdd(ntp, 1);
-          }
+          if (cur == 0u) sm.tlist[atomicAdd(&sm.tcount, 1)] = (int)h;
           placed = true;
           break;
         }
         h = (h + 1u) & mask;
       }
-      if (!placed) atomicOr(cg::this_cluster().map_shared_rank(&sm.tover, 0), 1);
+      if (!placed) atomicOr(sl.cs > 1 ? cg::this_cluster().map_shared_rank(&sm.status, 0) : &sm.status, JOB_TABLE_FULL);
     }
+    __syncthreads();
+    if (tid == 0) sm.ntouched = sm.tcount;
     __syncthreads();
     return;
   }
   unsigned* recw = reinterpret_cast<unsigned*>(J.rec);
+  int* tl = J.touched + sm.toff;
   // GATHER_U entries per thread per step: their row loads, their bitmap ORs
   // (no result used, so they issue as reductions) and their first-touch
   // atomics are all in flight together instead of one chain at a time.
-  // The entries are dealt out over all threads of the job's blocks.
   constexpr int GATHER_U = 4;
-  const int gthreads = sl.cs * NM_THREADS;
-  for (int base = sl.rank * NM_THREADS + tid; base < E; base += gthreads * GATHER_U) {
+  for (int base = tid; base < E; base += NM_THREADS * GATHER_U) {
     int rr[GATHER_U];
     unsigned word[GATHER_U], bit[GATHER_U];
 #pragma unroll
     for (int u = 0; u < GATHER_U; ++u) {
-      const int e = base + u * gthreads;
+      const int e = base + u * NM_THREADS;
       rr[u] = -1;
       word[u] = 0;
       bit[u] = 0;
@@ -668,7 +678,7 @@ __device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J, Slice sl = Slice{
     for (int u = 0; u < GATHER_U; ++u) first[u] = rr[u] >= 0 ? atomicOr(&recw[4 * rr[u] + 3], 1u) : 1u;
 #pragma unroll
     for (int u = 0; u < GATHER_U; ++u)
-      if (first[u] == 0u) J.touched[atomicAdd(ntp, 1)] = rr[u];
+      if (first[u] == 0u) tl[atomicAdd(&sm.ntouched, 1)] = rr[u];
   }
   __syncthreads();
 }
@@ -689,14 +699,13 @@ __device__ __forceinline__ unsigned rec_byte(const uint4& w, int xi) {
 // touched rows and their records do not change in between.
 constexpr int TOUCH_U = 4;
 template <int M, int CM, class F>
-__device__ __forceinline__ void for_touched_warp(const RoundSmem<M>& sm, const NMJob& J, Slice sl, F&& f) {
+__device__ __forceinline__ void for_touched_warp(const RoundSmem<M>& sm, const NMJob& J, F&& f) {
   constexpr int NW = NM_THREADS / 32;
   const int nt = sm.ntouched;
-  // 32-row chunks dealt round-robin over the job's blocks first, then over
-  // their warps, so a round with few touched rows still spreads over every
-  // SM of the cluster (the phases are issue-bound per SM)
-  const int NWt = sl.cs * NW;
-  const int lane = threadIdx.x & 31, w = (threadIdx.x >> 5) * sl.cs + sl.rank;
+  const int* tl = J.touched + sm.toff;  // the rows this block owns and the round touched
+  // 32-row chunks dealt round-robin over the block's warps
+  constexpr int NWt = NW;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   bool first = true;
   for (int c0 = w; c0 * 32 < nt; c0 += NWt * TOUCH_U) {
     int rv[TOUCH_U];
@@ -711,7 +720,7 @@ __device__ __forceinline__ void for_touched_warp(const RoundSmem<M>& sm, const N
 #pragma unroll
       for (int u = 0; u < TOUCH_U; ++u) {
         const int t = (c0 + u * NWt) * 32 + lane;
-        rv[u] = t < nt ? J.touched[t] : -1;
+        rv[u] = t < nt ? tl[t] : -1;
       }
 #pragma unroll
       for (int u = 0; u < TOUCH_U; ++u) wv[u] = rv[u] >= 0 ? J.rec[rv[u]] : make_uint4(0u, 0u, 0u, 0u);
@@ -733,7 +742,7 @@ __device__ __forceinline__ void for_touched_warp(const RoundSmem<M>& sm, const N
 // slots (index = slot) when the records are in shared memory, else the
 // touched rows (index = row).  Warp-uniform like for_touched_warp.
 template <int M, int CM, class F>
-__device__ __forceinline__ void for_rows_warp(const RoundSmem<M>& sm, const NMJob& J, Slice sl, F&& f) {
+__device__ __forceinline__ void for_rows_warp(const RoundSmem<M>& sm, const NMJob& J, F&& f) {
   if (sm.use_table) {  // the rows this block's table holds, from its list of claimed slots
     constexpr int NW = NM_THREADS / 32;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -745,7 +754,7 @@ __device__ __forceinline__ void for_rows_warp(const RoundSmem<M>& sm, const NMJo
       f(slot, v, i < n);
     }
   } else {
-    for_touched_warp<M, CM>(sm, J, sl, f);
+    for_touched_warp<M, CM>(sm, J, f);
   }
 }
 
@@ -767,7 +776,7 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
   // this warp's row masks: VL[x][k] at vw[2x * M + k], VE[x][k] at vw[(2x + 1) * M + k]
   extern __shared__ uint4 smem_heap[];
   unsigned* vw = reinterpret_cast<unsigned*>(smem_heap) + (threadIdx.x >> 5) * (2 * K * M);
-  for_rows_warp<M, 1>(sm, J, sl, [&](int r, const uint4& w, bool valid) {
+  for_rows_warp<M, 1>(sm, J, [&](int r, const uint4& w, bool valid) {
     (void)r;
     unsigned b[K];
     int p[K];
@@ -1249,7 +1258,7 @@ __device__ void apply_recount(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl)
     bitmove[xi][h][v] = make_uint4(o[0], o[1], o[2], 0u);
   }
   __syncthreads();
-  for_rows_warp<M, 2>(sm, J, sl, [&](int r, const uint4& w, bool valid) {
+  for_rows_warp<M, 2>(sm, J, [&](int r, const uint4& w, bool valid) {
     // the row's groups after the swaps, packed like the record
     unsigned n0 = 0, n1 = 0, n2 = 0;
 #pragma unroll 1
@@ -1308,10 +1317,13 @@ __device__ void cluster_push(cg::cluster_group& cl, int* mine, int n) {
 // All rounds of a job.  With cs == 1 one thread block runs the job; with
 // cs > 1 the job runs on a thread-block cluster of cs blocks: the leader
 // (rank 0) runs the sequential parts (segment choice, heaps, walk, counts)
-// and every block gathers, scores and recounts its share of the rows, the
-// partial sums meeting in the leader's shared memory.  Every block of a
-// cluster runs the same sequence of cluster barriers: the leader's decision
-// to run a round is copied to every block before the barrier that opens it.
+// and every block gathers, scores and recounts the rows it owns (row_group
+// in its share of the 16 groups), the partial sums meeting in the leader's
+// shared memory.  A round has four cluster barriers: after the round's
+// segments reach every block, after the partial sums of the scores, after
+// the swaps reach every block, and after the partial recounts.  Every
+// block runs the same sequence of them: the leader's decision to run a
+// round is copied to every block before the barrier that opens it.
 template <int M>
 __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __restrict__ jobs, int N,
                                                               int cnt_in_smem, int ts_max, int cs, int rcache_on) {
@@ -1336,7 +1348,12 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
   const int rank = cs > 1 ? (int)cl.block_rank() : 0;
   const bool lead = rank == 0;
   const Slice sl{rank, cs};
-  const long long t_start = clock64();
+  __shared__ long long t_start;  // the kernel's start (thread 0 of the leader)
+  __shared__ unsigned long long g_start;  // the same on the global timer (ns)
+  if (threadIdx.x == 0) {
+    t_start = clock64();
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g_start));
+  }
   const NMJob J = jobs[blockIdx.x / cs];
   const int tid = threadIdx.x;
   int* cnt = cnt_in_smem ? smem_cnt : J.cnt;
@@ -1350,7 +1367,8 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     sm.rcache = rcache_on ? smem_rcache : nullptr;
     sm.rcrow = rcache_on ? smem_rcrow : nullptr;
     sm.tcount = 0;
-    sm.tfall = 0;
+    sm.toff = rank * ((J.R + ROW_GROUPS - 1) / ROW_GROUPS + 1) * (ROW_GROUPS / cs);
+    for (int q = 0; q < 4; ++q) sm.acc[q] = 0ull;
     sm.ts_max = ts_max;
     sm.ts_shift = 32 - (31 - __clz(ts_max > 0 ? ts_max : 1));
     sm.use_table = 0;
@@ -1363,9 +1381,12 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
   const int MAXITER = J.maxiter > init_size ? J.maxiter : init_size;  // reorder.h:1819
   int round = 1;
   int committed = 0;
-  unsigned long long sumE = 0, sumT = 0;
-  int table_rounds = 0;  // rounds whose row records were in shared-memory tables
-  int fallback_rounds = 0;  // rounds whose tables overflowed and gathered into global memory
+  // this block's work counters: gathered entries, touched rows, rounds with
+  // the records in the shared-memory table, rounds with them in global
+  // memory (thread 0; in shared memory, as registers are scarce)
+  __shared__ unsigned long long wk[4];
+  if (tid == 0)
+    for (int q = 0; q < 4; ++q) wk[q] = 0ull;
   // cycles spent in each phase of a round, measured by thread 0 of the
   // leader at the barriers that end the phases: select, choose, gather,
   // process, heap, walk, apply
@@ -1412,30 +1433,12 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
       clear_round_smem<M>(sm);
       __syncthreads();
     }
-    int* ntp = lead ? &sm.ntouched : cl.map_shared_rank(&sm.ntouched, 0);
-    gather_phase<M>(sm, J, sl, ntp);
-    if (cs > 1) {
-      cl.sync();
-      if (tid == 0) {
-        if (!lead) sm.ntouched = *cl.map_shared_rank(&sm.ntouched, 0);
-        sm.tfall = sm.use_table && *cl.map_shared_rank(&sm.tover, 0) != 0;
-      }
-      __syncthreads();
-      if (sm.tfall) {
-        // a block's table ran out of slots: empty every table and gather
-        // this round's records into global memory instead
-        for (int i = tid; i < sm.ts_max; i += NM_THREADS) sm.table[i] = make_uint4(0u, 0u, 0u, 0u);
-        if (tid == 0) {
-          sm.tcount = 0;
-          if (lead) sm.ntouched = 0;
-        }
-        __syncthreads();
-        cl.sync();
-        gather_phase<M>(sm, J, sl, ntp, true);
-        cl.sync();
-        if (!lead && tid == 0) sm.ntouched = *cl.map_shared_rank(&sm.ntouched, 0);
-        __syncthreads();
-      }
+    // the block's own rows: no barrier between its gather and its process phase
+    gather_phase<M>(sm, J, sl);
+    if (tid == 0) {
+      wk[0] += (unsigned)sm.E;
+      wk[1] += (unsigned)sm.ntouched;
+      wk[sm.use_table ? 2 : 3] += 1;
     }
     VNM_PHASE(2);
     process_phase<M>(sm, J, N, sl);
@@ -1466,10 +1469,6 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
         }
         if (round - 1 < J.trace_cap_rounds) J.trace_rounds[round - 1] = committed;
       }
-      sumE += (unsigned)sm.E;
-      sumT += (unsigned)sm.ntouched;
-      table_rounds += sm.use_table ? 1 : 0;
-      fallback_rounds += sm.tfall ? 1 : 0;
       // where each bit of the round's segments goes, to every block (one
       // remote word store a thread)
       constexpr int DW = RoundSmem<M>::DEST_W;
@@ -1495,7 +1494,16 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     round += 1;
   }
 #undef VNM_PHASE
+  if (cs > 1) {  // the helpers' counters to the leader
+    if (!lead && tid == 0) {
+      unsigned long long* acc = cl.map_shared_rank(&sm.acc[0], 0);
+      for (int q = 0; q < 4; ++q) atomicAdd(acc + q, wk[q]);
+    }
+    cl.sync();
+  }
   if (!lead) return;
+  if (tid == 0)
+    for (int q = 0; q < 4; ++q) wk[q] += sm.acc[q];
   if (cnt_in_smem)
     for (int s = tid; s < J.nseg; s += NM_THREADS) J.cnt[s] = smem_cnt[s];
   if (tid == 0) {
@@ -1506,14 +1514,18 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     J.res[4] = round - 1;
     J.res[5] = sm.status;
     J.res[6] = committed;
-    J.res[7] = (int)(sumE & 0x7fffffffull);
-    J.res[8] = (int)(sumE >> 31);
-    J.res[9] = (int)(sumT & 0x7fffffffull);
-    J.res[10] = (int)(sumT >> 31);
-    J.res[11] = table_rounds;
-    J.res[12] = fallback_rounds;
+    J.res[7] = (int)(wk[0] & 0x7fffffffull);
+    J.res[8] = (int)(wk[0] >> 31);
+    J.res[9] = (int)(wk[1] & 0x7fffffffull);
+    J.res[10] = (int)(wk[1] >> 31);
+    J.res[11] = (int)wk[2];
+    J.res[12] = (int)wk[3];
     for (int q = 0; q < 7; ++q) J.res[16 + q] = (int)(tph[q] >> 10);  // kilocycles
     J.res[23] = (int)((clock64() - t_start) >> 10);
+    unsigned long long g_end;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g_end));
+    J.res[13] = (int)((g_start >> 10) & 0x7fffffffull);  // start and end, in units of 1024 ns
+    J.res[14] = (int)((g_end >> 10) & 0x7fffffffull);
   }
 }
 
@@ -1527,6 +1539,7 @@ __global__ void __launch_bounds__(NM_THREADS) k_pair_score(NMJob J, int N, int s
     sm.table = nullptr;
     sm.ts_max = 0;
     sm.use_table = 0;
+    sm.toff = 0;
     sm.rcache = nullptr;
     sm.rcrow = nullptr;
     sm.xseg[0] = s1;
@@ -1570,11 +1583,13 @@ size_t pattern_bytes(int R, int nnz) {
   b += arena_bytes(1, sizeof(int));              // error word
   b += arena_bytes(nnz, sizeof(int));            // flags / positions
   b += 2 * arena_bytes(nnz, sizeof(int));        // prow, pcol
-  b += arena_bytes(R + 1, sizeof(int)) * 2;      // coldeg->cptr, cfill
+  const size_t ng = (size_t)ROW_GROUPS * R + 1;
+  b += arena_bytes(R + 1, sizeof(int));          // cptr
+  b += 2 * arena_bytes(ng, sizeof(int));         // group counts -> csplit, cfill
   b += arena_bytes(nnz, sizeof(int));            // crow
   b += 2 * arena_bytes(R / 2 + 1, sizeof(int));  // inv0, pres0 (nseg <= R/2)
   b += arena_bytes(1, sizeof(int)) * 2;          // totals
-  b += scan_scratch_bytes(nnz > R + 1 ? nnz : R + 1) * 2;
+  b += scan_scratch_bytes((size_t)nnz > ng ? nnz : (int)ng) * 2;
   return b;
 }
 
@@ -1587,19 +1602,21 @@ static vnm_status build_pattern_t(vnm_ctx* ctx, int R, int nnz, const int* d_row
   int* pos = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
   P.prow = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
   P.pcol = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
+  const size_t ng = (size_t)ROW_GROUPS * R + 1;
   P.cptr = arena_take<int>(ctx, R + 1);
-  int* cfill = arena_take<int>(ctx, R + 1);
+  P.csplit = arena_take<int>(ctx, ng);
+  int* cfill = arena_take<int>(ctx, ng);
   P.crow = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
   P.inv0 = arena_take<int>(ctx, R / 2 + 1);
   P.pres0 = arena_take<int>(ctx, R / 2 + 1);
   int* d_np = arena_take<int>(ctx, 1);
   int* d_tot = arena_take<int>(ctx, 1);
-  if (!err || !pos || !P.prow || !P.pcol || !P.cptr || !cfill || !P.crow || !P.inv0 || !P.pres0 || !d_np ||
-      !d_tot)
+  if (!err || !pos || !P.prow || !P.pcol || !P.cptr || !P.csplit || !cfill || !P.crow || !P.inv0 || !P.pres0 ||
+      !d_np || !d_tot)
     return VNM_ERR_NOMEM;
   VNM_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
-  VNM_CUDA_TRY(cudaMemsetAsync(P.cptr, 0, sizeof(int) * (R + 1), ctx->stream));
-  VNM_CUDA_TRY(cudaMemsetAsync(cfill, 0, sizeof(int) * (R + 1), ctx->stream));
+  VNM_CUDA_TRY(cudaMemsetAsync(P.csplit, 0, sizeof(int) * ng, ctx->stream));
+  VNM_CUDA_TRY(cudaMemsetAsync(cfill, 0, sizeof(int) * ng, ctx->stream));
   VNM_CUDA_TRY(cudaMemsetAsync(P.inv0, 0, sizeof(int) * (P.nseg + 1), ctx->stream));
   VNM_CUDA_TRY(cudaMemsetAsync(P.pres0, 0, sizeof(int) * (P.nseg + 1), ctx->stream));
   if (nnz > 0) {
@@ -1611,16 +1628,18 @@ static vnm_status build_pattern_t(vnm_ctx* ctx, int R, int nnz, const int* d_row
     if (h_scratch[0] & 1) return VNM_ERR_UNSORTED;
     VNM_LAUNCH(ctx, k_nonzero_flags, grid_for(ctx, nnz), 256, 0, d_val, nnz, pos);
     VNM_TRY(exclusive_scan(ctx, pos, pos, nnz, d_np));
-    VNM_LAUNCH(ctx, k_compact, grid_for(ctx, nnz), 256, 0, d_row, d_col, d_val, pos, nnz, P.prow, P.pcol, P.cptr);
+    VNM_LAUNCH(ctx, k_compact, grid_for(ctx, nnz), 256, 0, d_row, d_col, d_val, pos, nnz, P.prow, P.pcol,
+               P.csplit);
   } else {
     VNM_CUDA_TRY(cudaMemsetAsync(d_np, 0, sizeof(int), ctx->stream));
   }
-  VNM_TRY(exclusive_scan(ctx, P.cptr, P.cptr, R + 1, d_tot));
+  VNM_TRY(exclusive_scan(ctx, P.csplit, P.csplit, (int)ng, d_tot));
+  VNM_LAUNCH(ctx, k_cptr_from_split, grid_for(ctx, (long long)R + 1), 256, 0, P.csplit, R, P.cptr);
   VNM_CUDA_TRY(cudaMemcpyAsync(h_scratch + 1, d_np, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   VNM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   P.np = h_scratch[1];
   if (P.np > 0) {
-    VNM_LAUNCH(ctx, k_csc_scatter, grid_for(ctx, P.np), 256, 0, P.prow, P.pcol, P.np, P.cptr, cfill, P.crow);
+    VNM_LAUNCH(ctx, k_csc_scatter, grid_for(ctx, P.np), 256, 0, P.prow, P.pcol, P.np, P.csplit, cfill, P.crow);
     VNM_LAUNCH(ctx, k_locate<M>, grid_for(ctx, P.np), 256, 0, P.prow, P.pcol, P.np, N, P.inv0, P.pres0);
   }
   return VNM_OK;
@@ -1643,7 +1662,7 @@ vnm_status build_pattern(vnm_ctx* ctx, int R, int nnz, const int* d_row, const i
 size_t job_bytes(int R) {
   const int nseg = R / 2 + 1;
   return arena_bytes(R, sizeof(int)) + 2 * arena_bytes(nseg, sizeof(int)) + arena_bytes(R, sizeof(uint4)) +
-         arena_bytes(R, sizeof(int)) + arena_bytes(24, sizeof(int));
+         arena_bytes((size_t)R + 2 * ROW_GROUPS, sizeof(int)) + arena_bytes(24, sizeof(int));
 }
 
 // Carve one job's state out of the arena and initialise it.
@@ -1654,11 +1673,12 @@ static vnm_status make_job(vnm_ctx* ctx, const Pattern& P, int sched, int maxite
   J.maxiter = maxiter;
   J.cptr = P.cptr;
   J.crow = P.crow;
+  J.csplit = P.csplit;
   J.orig = arena_take<int>(ctx, P.R > 0 ? P.R : 1);
   J.cnt = arena_take<int>(ctx, P.nseg + 1);
   J.zc = arena_take<int>(ctx, P.nseg + 1);
   J.rec = arena_take<uint4>(ctx, P.R > 0 ? P.R : 1);
-  J.touched = arena_take<int>(ctx, P.R > 0 ? P.R : 1);
+  J.touched = arena_take<int>(ctx, (size_t)P.R + 2 * ROW_GROUPS);
   J.res = arena_take<int>(ctx, 24);
   J.trace_pairs = nullptr;
   J.trace_rounds = nullptr;
@@ -1690,9 +1710,9 @@ static vnm_status make_job(vnm_ctx* ctx, const Pattern& P, int sched, int maxite
 // 256-matrix 2:8 batch 4 % slower when it used one block per job).
 constexpr size_t NM_SMEM_BUDGET = 150u << 10;
 
-// k_nm_rounds<M>'s dynamic shared-memory ceiling depends on the launch shape
-// (a single-block job keeps a row table on chip, a cluster job does not), and
-// it is a property of the function shared by every host thread: one lock
+// k_nm_rounds<M>'s dynamic shared-memory ceiling depends on the call (the
+// segment counts and the table size), and it is a property of the function
+// shared by every host thread: one lock
 // covers each setting of it together with the launch it is for, so that a
 // call on another thread cannot lower it in between.
 static std::mutex g_round_launch_mu;
@@ -1700,6 +1720,7 @@ static std::mutex g_round_launch_mu;
 template <int M>
 static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, int N, int max_nseg, int cs) {
   std::lock_guard<std::mutex> launch_lock(g_round_launch_mu);
+  ctx->last_clusters_fit = 0;
   const size_t cbytes = (size_t)max_nseg * sizeof(int);
   const int in_smem = cbytes <= (64u << 10) ? 1 : 0;
   const size_t hbytes = (size_t)RoundSmem<M>::SCR_U4 * sizeof(uint4);
@@ -1708,16 +1729,12 @@ static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, 
   int ts = 8192;
   while (ts >= 1024 && fixed + (size_t)ts * SLOT > NM_SMEM_BUDGET) ts >>= 1;
   if (ts < 1024) ts = 0;
-  // Cluster jobs keep the round's row records in global memory (L2) unless
-  // VNM_NM_CLUSTER_TABLE=1 puts them in the blocks' shared-memory tables.
-  // Measured on GB300, R-MAT 16384 2:4 find_best: global 10.59 ms; tables
-  // for rounds of at most 3/4 of a table's slots 10.68, at most 1/8 of the
-  // cluster's slots 10.70, at most 1/2 12.51 -- the DSMEM atomics of the
-  // inserts cost what the process and apply phases gain.
-  if (cs > 1) {
-    const char* e = getenv("VNM_NM_CLUSTER_TABLE");
-    if (!(e && atoi(e) == 1)) ts = 0;
-  }
+  // Each block keeps the records of the rows it owns in its own table (a
+  // round whose entries would fill more than 3/4 of it uses J.rec in global
+  // memory instead).  VNM_NM_ROW_TABLE=0 keeps every round's records in
+  // global memory, for measurement.
+  if (const char* e = getenv("VNM_NM_ROW_TABLE"))
+    if (atoi(e) == 0) ts = 0;
   // the record cache of the apply phase, when the budget allows it
   constexpr size_t RCACHE = (size_t)NM_THREADS * TOUCH_U * (sizeof(uint4) + sizeof(int));
   int rc = fixed + (size_t)ts * SLOT + RCACHE <= NM_SMEM_BUDGET ? 1 : 0;
@@ -1751,9 +1768,13 @@ static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, 
         (void)cudaGetLastError();
         continue;
       }
-      if (nclusters >= 1 && fallback == 1) fallback = c;
+      if (nclusters >= 1 && fallback == 1) {
+        fallback = c;
+        ctx->last_clusters_fit = nclusters;
+      }
       if (nclusters >= njobs) {
         pick = c;
+        ctx->last_clusters_fit = nclusters;
         break;
       }
     }
@@ -1766,14 +1787,8 @@ static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, 
       ctx->last_cluster = pick;
       return VNM_OK;
     }
-    // no cluster fits: one block per job, with the shared-memory row table
-    ts = 8192;
-    while (ts >= 1024 && fixed + (size_t)ts * SLOT > NM_SMEM_BUDGET) ts >>= 1;
-    if (ts < 1024) ts = 0;
-    rc = fixed + (size_t)ts * SLOT + RCACHE <= NM_SMEM_BUDGET ? 1 : 0;
-    const size_t dyn1 = hbytes + (size_t)ts * SLOT + (rc ? RCACHE : 0) + (in_smem ? cbytes : 0);
-    VNM_CUDA_TRY(cudaFuncSetAttribute(k_nm_rounds<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn1));
-    VNM_LAUNCH(ctx, k_nm_rounds<M>, njobs, NM_THREADS, dyn1, d_jobs, N, in_smem, ts, 1, rc);
+    // no cluster fits: one block per job
+    VNM_LAUNCH(ctx, k_nm_rounds<M>, njobs, NM_THREADS, dyn, d_jobs, N, in_smem, ts, 1, rc);
     ctx->last_cluster = 1;
     return VNM_OK;
   }
@@ -1790,9 +1805,9 @@ static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, 
 // cluster size) from 128 K pattern entries on, 8 below.  VNM_NM_CLUSTER
 // (1..16) in the environment overrides the choice.
 static int nm_cluster_size(long long np) {
-  if (const char* e = getenv("VNM_NM_CLUSTER")) {
+  if (const char* e = getenv("VNM_NM_CLUSTER")) {  // rounded down to a power of two (rows are dealt in 16 groups)
     const int v = atoi(e);
-    if (v >= 1 && v <= 16) return v;
+    if (v >= 1 && v <= 16) return v >= 16 ? 16 : v >= 8 ? 8 : v >= 4 ? 4 : v >= 2 ? 2 : 1;
   }
   return np >= (1ll << 17) ? 16 : 8;
 }
@@ -1817,7 +1832,7 @@ static vnm_status check_nm_args(int nrows, int nnz, const int* row, const int* c
   if (nrows < 0 || nnz < 0 || (nrows % M) != 0) return VNM_ERR_ARG;
   if (mem != VNM_MEM_HOST && mem != VNM_MEM_DEVICE) return VNM_ERR_ARG;
   if (nnz > 0 && (!row || !col || !val)) return VNM_ERR_ARG;
-  if (nrows > (1 << 28)) return VNM_ERR_LIMIT;
+  if (nrows >= (1 << 27)) return VNM_ERR_LIMIT;  // 16 nrows + 1 row groups fit an int
   return VNM_OK;
 }
 
@@ -1892,6 +1907,18 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
   ctx->stats[4] = nsched;
   ctx->stats[5] = P.np;
   ctx->stats[6] = ctx->last_cluster;
+  {  // when the jobs ran: spread of their starts and the span of all of them (us)
+    int s0 = hres_copy[13], s1 = hres_copy[13], e1 = hres_copy[14];
+    for (int s = 1; s < nsched; ++s) {
+      const int* h = hres_copy + 24 * s;
+      if ((int)((unsigned)h[13] - (unsigned)s0) < 0) s0 = h[13];
+      if ((int)((unsigned)h[13] - (unsigned)s1) > 0) s1 = h[13];
+      if ((int)((unsigned)h[14] - (unsigned)e1) > 0) e1 = h[14];
+    }
+    ctx->stats[17] = (long long)(((unsigned)s1 - (unsigned)s0) & 0x7fffffffu) * 1024 / 1000;
+    ctx->stats[18] = (long long)(((unsigned)e1 - (unsigned)s0) & 0x7fffffffu) * 1024 / 1000;
+    ctx->stats[19] = ctx->last_clusters_fit;
+  }
   for (int s = 0; s < nsched; ++s) {
     const int* h = hres_copy + 24 * s;
     if (h[5] != 0) return VNM_ERR_INTERNAL;
@@ -1997,14 +2024,14 @@ static vnm_status run_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int6
   }
   row_off[nmat] = (int)totR;
   const long long nnz = nnz_offset[nmat] - nnz_offset[0];
-  if (nnz_offset[0] != 0 || totR > (1 << 28) || nnz > (1ll << 31) - 1) return VNM_ERR_LIMIT;
+  if (nnz_offset[0] != 0 || totR >= (1 << 27) || nnz > (1ll << 31) - 1) return VNM_ERR_LIMIT;
   if (nnz > 0 && (!row || !col || !val)) return VNM_ERR_ARG;
   const int R = (int)totR, n = (int)nnz;
   size_t need = pattern_bytes(R, n) + 5 * arena_bytes(n, sizeof(int)) + arena_bytes(nmat + 1, 8) +
                 3 * arena_bytes(nmat + 1, sizeof(int)) + arena_bytes(nmat, sizeof(NMJob)) +
-                2 * arena_bytes(R, sizeof(int)) + arena_bytes(R, sizeof(uint4)) +
-                2 * arena_bytes(R / M + nmat, sizeof(int)) + arena_bytes((size_t)24 * nmat, sizeof(int)) +
-                arena_bytes(R, sizeof(int)) + 8192;
+                arena_bytes(R, sizeof(int)) + arena_bytes((size_t)R + (size_t)2 * ROW_GROUPS * nmat, sizeof(int)) +
+                arena_bytes(R, sizeof(uint4)) + 2 * arena_bytes(R / M + nmat, sizeof(int)) +
+                arena_bytes((size_t)24 * nmat, sizeof(int)) + arena_bytes(R, sizeof(int)) + 8192;
   VNM_TRY(arena_reserve(ctx, need));
   VNM_TRY(pinned_reserve(ctx, 256 + (size_t)24 * nmat));
   VNM_TRY(begin_call(ctx));
@@ -2039,7 +2066,7 @@ static vnm_status run_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int6
   VNM_TRY(build_pattern(ctx, R, n, grow, gcol, d_val, N, M, P, ctx->h_pinned));
   // per-job state, one allocation per field for the whole batch
   int* orig = arena_take<int>(ctx, R > 0 ? R : 1);
-  int* touched = arena_take<int>(ctx, R > 0 ? R : 1);
+  int* touched = arena_take<int>(ctx, (size_t)R + (size_t)2 * ROW_GROUPS * nmat);  // 32 of slack per job
   uint4* rec = arena_take<uint4>(ctx, R > 0 ? R : 1);
   int* cnt = arena_take<int>(ctx, R / M + nmat);
   int* zc = arena_take<int>(ctx, R / M + nmat);
@@ -2058,11 +2085,12 @@ static vnm_status run_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int6
     J.maxiter = maxiter;
     J.cptr = P.cptr + row_off[b];
     J.crow = P.crow;
+    J.csplit = P.csplit + (size_t)ROW_GROUPS * row_off[b];
     J.orig = orig + row_off[b];
     J.cnt = cnt + seg_off[b] + b;
     J.zc = zc + seg_off[b] + b;
     J.rec = rec;
-    J.touched = touched + row_off[b];
+    J.touched = touched + row_off[b] + 2 * ROW_GROUPS * b;
     J.res = res + 24 * b;
     J.trace_pairs = nullptr;
     J.trace_rounds = nullptr;
@@ -2103,6 +2131,8 @@ static vnm_status run_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int6
     ctx->stats[1] += (long long)h[7] + ((long long)h[8] << 31);
     ctx->stats[2] += (long long)h[9] + ((long long)h[10] << 31);
     for (int q = 0; q < 7; ++q) ctx->stats[8 + q] += h[16 + q];
+    ctx->stats[7] += h[11];
+    ctx->stats[15] += h[12];
     ctx->stats[16] += h[23];
   }
   return VNM_OK;
@@ -2284,7 +2314,7 @@ namespace vnm {
 
 constexpr int NOALLOC_MAX_ROWS = 32768;
 constexpr int NOALLOC_MAX_NNZ = 1 << 19;
-constexpr size_t NOALLOC_BYTES = size_t(10) << 20;  // 10 MiB
+constexpr size_t NOALLOC_BYTES = size_t(16) << 20;  // 16 MiB
 
 // The scratch itself.  Host code must not use this symbol as an address
 // (in host code it names a host-side shadow); it asks the runtime for the

@@ -157,8 +157,11 @@ class Context:
         d = dict(zip(keys, list(out)[:8]))
         d["phase_kcycles"] = dict(zip(("select", "choose", "gather", "process", "heap_entries", "heaps_and_walk", "apply"),
                                       list(out)[8:15]))
-        d["table_fallback_rounds"] = out[15]
+        d["global_rounds"] = out[15]
         d["kernel_kcycles"] = out[16]
+        d["job_start_spread_us"] = out[17]
+        d["jobs_span_us"] = out[18]
+        d["clusters_fit"] = out[19]
         return d
 
     # ---- array plumbing: numpy arrays (host) or torch CUDA tensors (device)
