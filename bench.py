@@ -510,8 +510,8 @@ def run_ours(args, rank, world, local):
         for k in tot:
             tot[k] += t[k]
         launches += t["launches"]
-        st = dict(t["stats"])
-        ph = st.pop("phase_kcycles")
+        st = {k: x for k, x in t["stats"].items() if not isinstance(x, dict)}
+        ph = t["stats"]["phase_us"]
         stats_sum = st if stats_sum is None else {k: stats_sum[k] + st[k] for k in st}
         phase_sum = ph if phase_sum is None else {k: phase_sum[k] + ph[k] for k in ph}
     barrier()
@@ -609,13 +609,13 @@ def run_ours(args, rank, world, local):
                      "incremental_frac": inc_bytes / kt / 1e9 / peak if kt > 0 else 0.0,
                      "note": "latency-bound sequential greedy (4 jobs x cluster of %d blocks); see profiles/"
                              % int(t["stats"]["blocks_per_job"]),
-                     # shares of the leaders' cycles from the kernel's start to its end
-                     "round_phase_share": dict({k: round(vv / max(1, stt.get("kernel_kcycles", 0),
+                     # shares of the leaders' time from the kernel's start to its end
+                     "round_phase_share": dict({k: round(vv / max(1, stt.get("kernel_us", 0),
                                                                   sum(phase_sum.values())), 4)
                                                 for k, vv in phase_sum.items()},
-                                               outside_rounds=round(max(0, stt.get("kernel_kcycles", 0) -
+                                               outside_rounds=round(max(0, stt.get("kernel_us", 0) -
                                                                         sum(phase_sum.values())) /
-                                                                    max(1, stt.get("kernel_kcycles", 0)), 4))},
+                                                                    max(1, stt.get("kernel_us", 0)), 4))},
         "spmm": {"kernel": ("k_spmm_vnm<64|128|256> (column-block width picked by timing on the first call) + "
                             "k_spmm_res" if info["tensor_tiles"] > 0 else "k_spmm_res + k_spmm_fin (CUDA cores)"),
                  "routing": "%d tensor-core tiles; %d residual nonzeros on the CUDA cores (V-blocks with fewer "

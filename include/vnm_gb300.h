@@ -79,17 +79,21 @@ float vnm_last_main_kernel_ms(const vnm_ctx* ctx);
  * job (the cluster size the launch used), out[7] block-rounds whose row
  * records were in the block's shared-memory table (a block keeps the
  * records of the rows it owns; summed over blocks and jobs), out[8..14]
- * kilocycles spent per round phase (select, choose, gather, process, heap
- * entries, swap heaps and walk overlapped, apply) summed over jobs,
+ * time spent per round phase (select, choose, gather, process, heap
+ * entries, swap heaps and walk overlapped, apply) in units of 1024 ns,
+ * summed over jobs,
  * out[15] block-rounds whose row records were in global memory (the
  * block's entries would have filled more than 3/4 of its table), out[16]
- * kilocycles from the round kernel's start to its end summed over jobs
- * (out[8..14] plus the set-up and the final write-back), out[17] the
+ * the time from the round kernel's start to its end in units of 1024 ns
+ * summed over jobs (out[8..14] plus the set-up and the final write-back),
+ * out[17] the
  * spread of the jobs' start times and out[18] the span from the first
  * start to the last end, in microseconds (jobs that run at once start
  * together), out[19] how many clusters of the launched size the GPU can
- * hold at once by the occupancy query (0 for single-block launches).
- * n <= 20 values. */
+ * hold at once by the occupancy query (0 for single-block launches),
+ * out[20], out[21] the leaders' own work in the process and apply phases
+ * (before the barriers that close them), units of 1024 ns summed over
+ * jobs.  n <= 24 values. */
 vnm_status vnm_last_stats(const vnm_ctx* ctx, long long* out, int n);
 
 /* ---------------------------------------------------------------------------

@@ -64,6 +64,12 @@ constexpr int JOB_EMPTY_HEAP = 1;   // reference would call top() on an empty qu
 constexpr int JOB_WAIT_LIMIT = 4;   // the walk waited too long for a swap heap's pops
 constexpr int JOB_TABLE_FULL = 8;   // a row found no free table slot (cannot happen: at most 3/4 are taken)
 
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 // The part of a job's row work one thread block does: block `rank` of the
 // `cs` blocks (a thread-block cluster, cs a power of two <= 16) that share
 // the job.  Rows are dealt to blocks in 16 groups: block `rank` owns the
@@ -72,6 +78,7 @@ struct Slice {
   int rank, cs;
 };
 constexpr int ROW_GROUPS = 16;
+constexpr int JOB_RES = 32;  // ints of a job's result record (NMJob::res)
 
 // A row's group: row & 15 rotated by a hash of row >> 4.  Within every
 // aligned run of 16 rows each group occurs once, so a window of n rows puts
@@ -97,14 +104,16 @@ struct NMJob {
   uint4* rec;         // [R] per-row scratch, zero on entry and on exit
   int* touched;       // [R + 32] scratch: block `rank` lists its touched rows from
                       //   rank * (ceil(R / 16) + 1) * (16 / cs) on
-  int* res;           // [24]: init_size, final_size, init_cnt, final_cnt, rounds, status,
+  int* res;           // [JOB_RES]: init_size, final_size, init_cnt, final_cnt, rounds, status,
                       //       swaps, gathered entries (lo, hi), touched rows (lo, hi),
                       //       [11] block-rounds with the records in a shared-memory
                       //       table, [12] block-rounds with them in global memory,
                       //       [13], [14] the job's start and end on the global timer
                       //       (units of 1024 ns, low 31 bits),
-                      //       [16..22] kilocycles per round phase, [23] kilocycles
-                      //       from the kernel's start to its end (leader, thread 0)
+                      //       [16..22] time per round phase, [23] from the kernel's
+                      //       start to its end (leader, thread 0), in units of 1024 ns,
+                      //       [24], [25] the leader's own work in the process and
+                      //       apply phases (before their barriers), same units
   int* trace_pairs;   // optional: swaps in commit order (v1, v2)
   int* trace_rounds;  // optional: pairs committed by the end of each round
   int trace_cap_pairs;
@@ -1348,12 +1357,8 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
   const int rank = cs > 1 ? (int)cl.block_rank() : 0;
   const bool lead = rank == 0;
   const Slice sl{rank, cs};
-  __shared__ long long t_start;  // the kernel's start (thread 0 of the leader)
-  __shared__ unsigned long long g_start;  // the same on the global timer (ns)
-  if (threadIdx.x == 0) {
-    t_start = clock64();
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g_start));
-  }
+  __shared__ unsigned long long g_start;  // the kernel's start (thread 0 of the leader), global timer
+  if (threadIdx.x == 0) g_start = global_ns();
   const NMJob J = jobs[blockIdx.x / cs];
   const int tid = threadIdx.x;
   int* cnt = cnt_in_smem ? smem_cnt : J.cnt;
@@ -1387,20 +1392,24 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
   __shared__ unsigned long long wk[4];
   if (tid == 0)
     for (int q = 0; q < 4; ++q) wk[q] = 0ull;
-  // cycles spent in each phase of a round, measured by thread 0 of the
-  // leader at the barriers that end the phases: select, choose, gather,
-  // process, heap, walk, apply
-  // (in shared memory: only thread 0 uses them, and registers are scarce)
+  // time spent in each phase of a round (ns, global timer), measured by
+  // thread 0 of the leader at the barriers that end the phases: select,
+  // choose, gather, process, heap, walk, apply.  (The SM cycle counter
+  // undercounted the waits at cluster barriers: its phase sums fell short of
+  // the kernel's time by up to 40 %.)  In shared memory: only thread 0 uses
+  // them, and registers are scarce.
   __shared__ unsigned long long tph[7];
-  __shared__ long long t0;
+  __shared__ unsigned long long tpo[2];  // the leader's own work in the process and apply phases
+  __shared__ unsigned long long t0;
   if (tid == 0) {
     for (int q = 0; q < 7; ++q) tph[q] = 0;
-    t0 = clock64();
+    tpo[0] = tpo[1] = 0;
+    t0 = global_ns();
   }
 #define VNM_PHASE(i)                                     \
   if (tid == 0) {                                        \
-    const long long t1 = clock64();                      \
-    tph[i] += (unsigned long long)(t1 - t0);             \
+    const unsigned long long t1 = global_ns();           \
+    tph[i] += t1 - t0;                                   \
     t0 = t1;                                             \
   }
   if (cs > 1) cl.sync();  // every block's shared memory is set up before any remote access
@@ -1442,7 +1451,11 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     }
     VNM_PHASE(2);
     process_phase<M>(sm, J, N, sl);
+    if (tid == 0) tpo[0] += global_ns() - t0;  // the leader's own part of the process phase
     if (cs > 1) {
+      // (the leader pulling the helpers' sums over DSMEM instead was slower:
+      // 8.92 against 8.55 ms at R-MAT 16384 2:4, 200.5 against 197.2 ms at
+      // R-MAT 65536 2:8)
       if (!lead) cluster_push(cl, &sm.S[0][0], NSUM);
       cl.sync();
       if (!lead) {  // while the leader runs the heaps and the walk: next round's scan
@@ -1479,6 +1492,7 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     }
     if (cs > 1) cl.sync();
     apply_recount<M>(sm, J, N, sl);
+    if (tid == 0) tpo[1] += global_ns() - t0;  // the leader's own part of the apply phase
     if (cs > 1) {
       if (!lead) cluster_push(cl, &sm.newinv[0], 2 * K);
       cl.sync();
@@ -1520,10 +1534,11 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     J.res[10] = (int)(wk[1] >> 31);
     J.res[11] = (int)wk[2];
     J.res[12] = (int)wk[3];
-    for (int q = 0; q < 7; ++q) J.res[16 + q] = (int)(tph[q] >> 10);  // kilocycles
-    J.res[23] = (int)((clock64() - t_start) >> 10);
-    unsigned long long g_end;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g_end));
+    for (int q = 0; q < 7; ++q) J.res[16 + q] = (int)(tph[q] >> 10);  // units of 1024 ns
+    J.res[24] = (int)(tpo[0] >> 10);
+    J.res[25] = (int)(tpo[1] >> 10);
+    const unsigned long long g_end = global_ns();
+    J.res[23] = (int)((g_end - g_start) >> 10);
     J.res[13] = (int)((g_start >> 10) & 0x7fffffffull);  // start and end, in units of 1024 ns
     J.res[14] = (int)((g_end >> 10) & 0x7fffffffull);
   }
@@ -1662,7 +1677,7 @@ vnm_status build_pattern(vnm_ctx* ctx, int R, int nnz, const int* d_row, const i
 size_t job_bytes(int R) {
   const int nseg = R / 2 + 1;
   return arena_bytes(R, sizeof(int)) + 2 * arena_bytes(nseg, sizeof(int)) + arena_bytes(R, sizeof(uint4)) +
-         arena_bytes((size_t)R + 2 * ROW_GROUPS, sizeof(int)) + arena_bytes(24, sizeof(int));
+         arena_bytes((size_t)R + 2 * ROW_GROUPS, sizeof(int)) + arena_bytes(JOB_RES, sizeof(int));
 }
 
 // Carve one job's state out of the arena and initialise it.
@@ -1679,7 +1694,7 @@ static vnm_status make_job(vnm_ctx* ctx, const Pattern& P, int sched, int maxite
   J.zc = arena_take<int>(ctx, P.nseg + 1);
   J.rec = arena_take<uint4>(ctx, P.R > 0 ? P.R : 1);
   J.touched = arena_take<int>(ctx, (size_t)P.R + 2 * ROW_GROUPS);
-  J.res = arena_take<int>(ctx, 24);
+  J.res = arena_take<int>(ctx, JOB_RES);
   J.trace_pairs = nullptr;
   J.trace_rounds = nullptr;
   J.trace_cap_pairs = 0;
@@ -1697,7 +1712,7 @@ static vnm_status make_job(vnm_ctx* ctx, const Pattern& P, int sched, int maxite
   if (const char* e = getenv("VNM_NM_TEST_HOLD_HEAPS")) J.hold_heaps = atoi(e) == 1 ? 1 : 0;
   if (!J.orig || !J.cnt || !J.zc || !J.rec || !J.touched || !J.res) return VNM_ERR_NOMEM;
   VNM_CUDA_TRY(cudaMemsetAsync(J.rec, 0, sizeof(uint4) * (P.R > 0 ? P.R : 1), ctx->stream));
-  VNM_CUDA_TRY(cudaMemsetAsync(J.res, 0, sizeof(int) * 24, ctx->stream));
+  VNM_CUDA_TRY(cudaMemsetAsync(J.res, 0, sizeof(int) * JOB_RES, ctx->stream));
   if (P.R > 0)
     VNM_LAUNCH(ctx, k_init_job, grid_for(ctx, P.R), 256, 0, J.orig, J.cnt, J.zc, P.inv0, P.pres0, P.R, P.nseg);
   return VNM_OK;
@@ -1735,6 +1750,7 @@ static vnm_status launch_rounds_t(vnm_ctx* ctx, const NMJob* d_jobs, int njobs, 
   // global memory, for measurement.
   if (const char* e = getenv("VNM_NM_ROW_TABLE"))
     if (atoi(e) == 0) ts = 0;
+
   // the record cache of the apply phase, when the budget allows it
   constexpr size_t RCACHE = (size_t)NM_THREADS * TOUCH_U * (sizeof(uint4) + sizeof(int));
   int rc = fixed + (size_t)ts * SLOT + RCACHE <= NM_SMEM_BUDGET ? 1 : 0;
@@ -1897,12 +1913,13 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
   VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main1, ctx->stream));
   int* hres = ctx->h_pinned;
   for (int s = 0; s < nsched; ++s)
-    VNM_CUDA_TRY(cudaMemcpyAsync(hres + 24 * s, hj[s].res, sizeof(int) * 24, cudaMemcpyDeviceToHost, ctx->stream));
+    VNM_CUDA_TRY(cudaMemcpyAsync(hres + JOB_RES * s, hj[s].res, sizeof(int) * JOB_RES, cudaMemcpyDeviceToHost,
+                                 ctx->stream));
   VNM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   VNM_CUDA_TRY(cudaEventElapsedTime(&ctx->main_ms, ctx->ev_main0, ctx->ev_main1));
-  int hres_copy[96];
-  memcpy(hres_copy, hres, sizeof(int) * 24 * nsched);
-  for (int q = 0; q < 20; ++q) ctx->stats[q] = 0;
+  int hres_copy[4 * JOB_RES];
+  memcpy(hres_copy, hres, sizeof(int) * JOB_RES * nsched);
+  for (int q = 0; q < 24; ++q) ctx->stats[q] = 0;
   ctx->stats[3] = P.nseg;
   ctx->stats[4] = nsched;
   ctx->stats[5] = P.np;
@@ -1910,7 +1927,7 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
   {  // when the jobs ran: spread of their starts and the span of all of them (us)
     int s0 = hres_copy[13], s1 = hres_copy[13], e1 = hres_copy[14];
     for (int s = 1; s < nsched; ++s) {
-      const int* h = hres_copy + 24 * s;
+      const int* h = hres_copy + JOB_RES * s;
       if ((int)((unsigned)h[13] - (unsigned)s0) < 0) s0 = h[13];
       if ((int)((unsigned)h[13] - (unsigned)s1) > 0) s1 = h[13];
       if ((int)((unsigned)h[14] - (unsigned)e1) > 0) e1 = h[14];
@@ -1920,7 +1937,7 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
     ctx->stats[19] = ctx->last_clusters_fit;
   }
   for (int s = 0; s < nsched; ++s) {
-    const int* h = hres_copy + 24 * s;
+    const int* h = hres_copy + JOB_RES * s;
     if (h[5] != 0) return VNM_ERR_INTERNAL;
     for (int q = 0; q < 5; ++q) res5_out[5 * s + q] = h[q];
     ctx->stats[0] += h[4];
@@ -1930,6 +1947,8 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
     ctx->stats[7] += h[11];
     ctx->stats[15] += h[12];
     ctx->stats[16] += h[23];
+    ctx->stats[20] += h[24];
+    ctx->stats[21] += h[25];
   }
   if (trace) {
     const int committed = hres_copy[6];
@@ -2031,9 +2050,9 @@ static vnm_status run_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int6
                 3 * arena_bytes(nmat + 1, sizeof(int)) + arena_bytes(nmat, sizeof(NMJob)) +
                 arena_bytes(R, sizeof(int)) + arena_bytes((size_t)R + (size_t)2 * ROW_GROUPS * nmat, sizeof(int)) +
                 arena_bytes(R, sizeof(uint4)) + 2 * arena_bytes(R / M + nmat, sizeof(int)) +
-                arena_bytes((size_t)24 * nmat, sizeof(int)) + arena_bytes(R, sizeof(int)) + 8192;
+                arena_bytes((size_t)JOB_RES * nmat, sizeof(int)) + arena_bytes(R, sizeof(int)) + 8192;
   VNM_TRY(arena_reserve(ctx, need));
-  VNM_TRY(pinned_reserve(ctx, 256 + (size_t)24 * nmat));
+  VNM_TRY(pinned_reserve(ctx, 256 + (size_t)JOB_RES * nmat));
   VNM_TRY(begin_call(ctx));
   const int *d_row, *d_col;
   const float* d_val;
@@ -2070,11 +2089,11 @@ static vnm_status run_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int6
   uint4* rec = arena_take<uint4>(ctx, R > 0 ? R : 1);
   int* cnt = arena_take<int>(ctx, R / M + nmat);
   int* zc = arena_take<int>(ctx, R / M + nmat);
-  int* res = arena_take<int>(ctx, (size_t)24 * nmat);
+  int* res = arena_take<int>(ctx, (size_t)JOB_RES * nmat);
   NMJob* d_jobs = arena_take<NMJob>(ctx, nmat);
   if (!orig || !touched || !rec || !cnt || !zc || !res || !d_jobs) return VNM_ERR_NOMEM;
   VNM_CUDA_TRY(cudaMemsetAsync(rec, 0, sizeof(uint4) * (R > 0 ? R : 1), ctx->stream));
-  VNM_CUDA_TRY(cudaMemsetAsync(res, 0, sizeof(int) * 24 * nmat, ctx->stream));
+  VNM_CUDA_TRY(cudaMemsetAsync(res, 0, sizeof(int) * JOB_RES * nmat, ctx->stream));
   std::vector<NMJob> hj(nmat);
   int max_nseg = 0;
   for (int b = 0; b < nmat; ++b) {
@@ -2091,7 +2110,7 @@ static vnm_status run_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int6
     J.zc = zc + seg_off[b] + b;
     J.rec = rec;
     J.touched = touched + row_off[b] + 2 * ROW_GROUPS * b;
-    J.res = res + 24 * b;
+    J.res = res + JOB_RES * b;
     J.trace_pairs = nullptr;
     J.trace_rounds = nullptr;
     J.trace_cap_pairs = 0;
@@ -2110,7 +2129,7 @@ static vnm_status run_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int6
   VNM_TRY(launch_rounds(ctx, d_jobs, nmat, N, M, max_nseg, 2));
   VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main1, ctx->stream));
   int* hres = ctx->h_pinned + 256;
-  VNM_CUDA_TRY(cudaMemcpyAsync(hres, res, sizeof(int) * 24 * nmat, cudaMemcpyDeviceToHost, ctx->stream));
+  VNM_CUDA_TRY(cudaMemcpyAsync(hres, res, sizeof(int) * JOB_RES * nmat, cudaMemcpyDeviceToHost, ctx->stream));
   if (newpos && R > 0) {
     int* d_np = arena_take<int>(ctx, R);
     if (!d_np) return VNM_ERR_NOMEM;
@@ -2119,12 +2138,12 @@ static vnm_status run_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int6
   }
   VNM_TRY(end_call(ctx));
   VNM_CUDA_TRY(cudaEventElapsedTime(&ctx->main_ms, ctx->ev_main0, ctx->ev_main1));
-  for (int q = 0; q < 20; ++q) ctx->stats[q] = 0;
+  for (int q = 0; q < 24; ++q) ctx->stats[q] = 0;
   ctx->stats[3] = max_nseg;
   ctx->stats[4] = nmat;
   ctx->stats[5] = P.np;
   for (int b = 0; b < nmat; ++b) {
-    const int* h = hres + 24 * b;
+    const int* h = hres + JOB_RES * b;
     if (h[5] != 0) return VNM_ERR_INTERNAL;
     for (int q = 0; q < 5; ++q) res5[5 * b + q] = h[q];
     ctx->stats[0] += h[4];

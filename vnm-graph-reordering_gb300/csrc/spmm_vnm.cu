@@ -936,11 +936,6 @@ static vnm_status launch_spmm(vnm_ctx* ctx, const vnm_spmm_matrix* A, SpmmArgs& 
   size_t smem = sizeof(SpmmSmem<NT>) + 1024;
   if (smem < floor_bytes) smem = floor_bytes;
   dim3 grid(A->ntt, p.n / NT);
-  // No more CTAs than SMs: one CTA an SM.  Otherwise the block scheduler
-  // may put two on one SM and leave another idle (a full V:2:8 operand of
-  // 152 tiles at NT = 256: SMs active 274 K cycles on average, 460 K at
-  // most).
-  if ((long long)grid.x * grid.y <= ctx->num_sms && smem < (228u << 10) / 2 + 1024) smem = (228u << 10) / 2 + 1024;
   VNM_CUDA_TRY(cudaFuncSetAttribute(k_spmm_vnm<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   p.idesc = ptx::idesc_f16(A->dtype == 1 ? 1u : 0u, 0u, 1u, SP_TM, NT);
   VNM_LAUNCH(ctx, k_spmm_vnm<NT>, grid, SP_THREADS, smem, p);

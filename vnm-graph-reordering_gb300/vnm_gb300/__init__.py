@@ -151,17 +151,18 @@ class Context:
         return lib().vnm_last_main_kernel_ms(self.h)
 
     def last_stats(self):
-        out = (ctypes.c_longlong * 20)()
-        _check(lib().vnm_last_stats(self.h, out, 20), "vnm_last_stats")
+        out = (ctypes.c_longlong * 24)()
+        _check(lib().vnm_last_stats(self.h, out, 24), "vnm_last_stats")
         keys = ("rounds", "gathered", "touched", "nseg", "jobs", "pattern_nnz", "blocks_per_job", "table_rounds")
         d = dict(zip(keys, list(out)[:8]))
-        d["phase_kcycles"] = dict(zip(("select", "choose", "gather", "process", "heap_entries", "heaps_and_walk", "apply"),
-                                      list(out)[8:15]))
+        d["phase_us"] = dict(zip(("select", "choose", "gather", "process", "heap_entries", "heaps_and_walk", "apply"),
+                                 [x * 1.024 for x in list(out)[8:15]]))
         d["global_rounds"] = out[15]
-        d["kernel_kcycles"] = out[16]
+        d["kernel_us"] = out[16] * 1.024
         d["job_start_spread_us"] = out[17]
         d["jobs_span_us"] = out[18]
         d["clusters_fit"] = out[19]
+        d["leader_own_us"] = {"process": out[20] * 1.024, "apply": out[21] * 1.024}
         return d
 
     # ---- array plumbing: numpy arrays (host) or torch CUDA tensors (device)
