@@ -65,7 +65,7 @@ struct vnm_ctx {
   cudaEvent_t ev_main0 = nullptr, ev_main1 = nullptr;  // around the call's main kernel
   float last_ms = 0.f;
   float main_ms = 0.f;
-  long long stats[24] = {0};  // work counters of the last call
+  long long stats[28] = {0};  // work counters of the last call (vnm_last_stats)
   int last_clusters_fit = 0;  // clusters of the launched size the GPU can hold at once (occupancy query)
   int launches = 0;
   int last_cluster = 1;  // blocks per job of the last NM round launch

@@ -236,7 +236,7 @@ float vnm_last_main_kernel_ms(const vnm_ctx* c) { return c ? c->main_ms : 0.f; }
 
 vnm_status vnm_last_stats(const vnm_ctx* c, long long* out, int n) {
   if (!c || !out || n < 0) return VNM_ERR_ARG;
-  for (int i = 0; i < n && i < 24; ++i) out[i] = c->stats[i];
+  for (int i = 0; i < n && i < 28; ++i) out[i] = c->stats[i];
   return VNM_OK;
 }
 

@@ -1140,7 +1140,7 @@ vnm_status vnm_nm_learned(vnm_ctx* ctx, int nrows, int nnz, const int* row, cons
   out->rounds = rounds;
   out->swaps = swaps;
   out->ndump = hci[3] < dcap ? hci[3] : dcap;
-  for (int q = 0; q < 24; ++q) ctx->stats[q] = 0;
+  for (int q = 0; q < 28; ++q) ctx->stats[q] = 0;
   ctx->stats[0] = rounds;
   ctx->stats[1] = out->exact_scored;
   ctx->stats[2] = swaps;

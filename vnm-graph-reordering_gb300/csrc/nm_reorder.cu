@@ -70,6 +70,12 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
+// Time (ns) inside phases, accumulated by single threads of a job's leader
+// block: [0] the walk warp, [1] the heap thread of pair 0, [2] warp 0's
+// rows in the process phase, [3] warp 0's rows in the apply phase, [4] and
+// [5] warp 0's per-segment masks and pair corrections in the process phase.
+__shared__ unsigned long long s_tin[6];
+
 // The part of a job's row work one thread block does: block `rank` of the
 // `cs` blocks (a thread-block cluster, cs a power of two <= 16) that share
 // the job.  Rows are dealt to blocks in 16 groups: block `rank` owns the
@@ -113,7 +119,8 @@ struct NMJob {
                       //       [16..22] time per round phase, [23] from the kernel's
                       //       start to its end (leader, thread 0), in units of 1024 ns,
                       //       [24], [25] the leader's own work in the process and
-                      //       apply phases (before their barriers), same units
+                      //       apply phases (before their barriers), [26..29] the
+                      //       times inside phases of s_tin, same units
   int* trace_pairs;   // optional: swaps in commit order (v1, v2)
   int* trace_rounds;  // optional: pairs committed by the end of each round
   int trace_cap_pairs;
@@ -785,8 +792,18 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
   // this warp's row masks: VL[x][k] at vw[2x * M + k], VE[x][k] at vw[(2x + 1) * M + k]
   extern __shared__ uint4 smem_heap[];
   unsigned* vw = reinterpret_cast<unsigned*>(smem_heap) + (threadIdx.x >> 5) * (2 * K * M);
+  const unsigned long long t_in = (threadIdx.x == 0 && sl.rank == 0) ? global_ns() : 0ull;
+  // At most one 32-row chunk a warp: every warp leaves its chunk's masks in
+  // its scratch and the sums are made afterwards, one thread an entry over
+  // all chunks (gathered), instead of a shared atomic per chunk, pair and
+  // entry: those atomics, and the mask loads queued behind them, were 90 %
+  // of the process phase at R-MAT 16384 2:4.
+  constexpr int NW = NM_THREADS / 32;
+  const int nchunks = ((sm.use_table ? sm.tcount : sm.ntouched) + 31) / 32;
+  const bool gathered = !self && nchunks <= NW;
   for_rows_warp<M, 1>(sm, J, [&](int r, const uint4& w, bool valid) {
     (void)r;
+    const unsigned long long t_a = (threadIdx.x == 0 && sl.rank == 0) ? global_ns() : 0ull;
     unsigned b[K];
     int p[K];
 #pragma unroll
@@ -820,7 +837,10 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
 #pragma unroll 1
     for (int xi = 0; xi < Kn; ++xi) {
       const unsigned bx = valid ? rec_byte(w, xi) : 0u;
-      if (__ballot_sync(FULL, bx != 0u) == 0u) continue;
+      if (__ballot_sync(FULL, bx != 0u) == 0u) {
+        if (gathered && lane < M) vw[(2 * xi) * M + lane] = vw[(2 * xi + 1) * M + lane] = 0u;
+        continue;
+      }
       const int px = __popc(bx);
       const unsigned p1 = __ballot_sync(FULL, px == N + 1), p0 = __ballot_sync(FULL, px == N);
       unsigned vl = 0u;
@@ -831,7 +851,7 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
       }
       if (lane < M) {
         const unsigned so = vl & p1;
-        if (so) atomicAdd(&sm.S[xi][lane], __popc(so));
+        if (so && !gathered) atomicAdd(&sm.S[xi][lane], __popc(so));
         vw[(2 * xi) * M + lane] = vl;
         vw[(2 * xi + 1) * M + lane] = so | (~vl & p0);
       }
@@ -843,6 +863,13 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
     // VE[a][i] lies inside NZ[a] (eL is empty when L is) and VL[c][j] inside
     // NZ[c], so CL(i, j) = popc(VE[a][i] & VL[c][j]) and likewise
     // CR(i, j) = popc(VL[a][i] & VE[c][j]).
+    const bool timed = threadIdx.x == 0 && sl.rank == 0;
+    const unsigned long long t_b = timed ? global_ns() : 0ull;
+    if (timed) s_tin[4] += t_b - t_a;
+    if (gathered) {  // the masks stay in this warp's scratch for the sums below
+      __syncwarp();
+      return;
+    }
     unsigned segs = 0;
 #pragma unroll
     for (int xi = 0; xi < K; ++xi) segs |= (b[xi] != 0u ? 1u : 0u) << xi;
@@ -878,8 +905,48 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
       }
     }
     __syncwarp();  // the masks are read before the next chunk writes them
+    if (timed) s_tin[5] += global_ns() - t_b;
   });
   __syncthreads();
+  if (gathered) {
+    // one thread an entry of S, CL, CR (in that order, as laid out), summed
+    // over the chunks' masks; warp w's chunk left them at w * 2KM
+    const unsigned long long t_g = (threadIdx.x == 0 && sl.rank == 0) ? global_ns() : 0ull;
+    const unsigned* vb = reinterpret_cast<const unsigned*>(smem_heap);
+    constexpr int NP = RoundSmem<M>::NPAIR;
+    constexpr int NSUM = K * M + 2 * NP * MM;
+    for (int e = threadIdx.x; e < NSUM; e += NM_THREADS) {
+      int sum = 0;
+      if (e < K * M) {  // S[x][k] = rows with bit k and popcount N+1 = popc(VL & VE)
+        const int xi = e / M, k = e % M;
+        if (xi < Kn)
+          for (int w = 0; w < nchunks; ++w) {
+            const unsigned* v = vb + w * (2 * K * M);
+            sum += __popc(v[(2 * xi) * M + k] & v[(2 * xi + 1) * M + k]);
+          }
+        if (sum) atomicAdd(&sm.S[xi][k], sum);
+      } else {
+        const int f = e - K * M, side = f / (NP * MM), rem = f % (NP * MM);
+        const int pid = rem / MM, idx = rem % MM, i = idx / M, j = idx % M;
+        int a = 0, q = pid;  // pair (a, c), a < c, of pair_id
+        while (q >= K - 1 - a) {
+          q -= K - 1 - a;
+          ++a;
+        }
+        const int c = a + 1 + q;
+        if (c < Kn)
+          for (int w = 0; w < nchunks; ++w) {
+            const unsigned* v = vb + w * (2 * K * M);
+            sum += side == 0 ? __popc(v[(2 * a + 1) * M + i] & v[(2 * c) * M + j])   // CL: VE[a][i] & VL[c][j]
+                             : __popc(v[(2 * a) * M + i] & v[(2 * c + 1) * M + j]);  // CR: VL[a][i] & VE[c][j]
+          }
+        if (sum) atomicAdd(side == 0 ? &sm.CL[pid][idx] : &sm.CR[pid][idx], sum);
+      }
+    }
+    if (threadIdx.x == 0 && sl.rank == 0) s_tin[5] += global_ns() - t_g;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && sl.rank == 0) s_tin[2] += global_ns() - t_in;
 }
 
 // Pop order of every ordered pair's swap heap (fact 4).  The sift steps are
@@ -1267,6 +1334,7 @@ __device__ void apply_recount(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl)
     bitmove[xi][h][v] = make_uint4(o[0], o[1], o[2], 0u);
   }
   __syncthreads();
+  const unsigned long long t_in = (threadIdx.x == 0 && sl.rank == 0) ? global_ns() : 0ull;
   for_rows_warp<M, 2>(sm, J, [&](int r, const uint4& w, bool valid) {
     // the row's groups after the swaps, packed like the record
     unsigned n0 = 0, n1 = 0, n2 = 0;
@@ -1298,6 +1366,7 @@ __device__ void apply_recount(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl)
       else J.rec[r] = make_uint4(0u, 0u, 0u, 0u);
     }
   });
+  if (threadIdx.x == 0 && sl.rank == 0) s_tin[3] += global_ns() - t_in;
   __syncthreads();
   if (threadIdx.x == 0) sm.tcount = 0;  // the table is empty again (before the next round's inserts)
 }
@@ -1404,6 +1473,7 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
   if (tid == 0) {
     for (int q = 0; q < 7; ++q) tph[q] = 0;
     tpo[0] = tpo[1] = 0;
+    for (int q = 0; q < 6; ++q) s_tin[q] = 0;
     t0 = global_ns();
   }
 #define VNM_PHASE(i)                                     \
@@ -1468,8 +1538,11 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     if (lead) {
       rank_phase<M>(sm);
       VNM_PHASE(4);
+      const unsigned long long t_in = global_ns();
       if (tid >= NM_THREADS - 32) walk_phase<M>(sm, J.sched, J.walk_wait_limit);  // the last warp walks ...
       else if (!J.hold_heaps) heap_sift<M>(sm);                                   // ... while the heaps pop
+      if (tid == NM_THREADS - 32) s_tin[0] += global_ns() - t_in;
+      else if (tid == 0) s_tin[1] += global_ns() - t_in;
       __syncthreads();
       VNM_PHASE(5);
       if (tid == 0 && J.trace_pairs) {
@@ -1537,6 +1610,7 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     for (int q = 0; q < 7; ++q) J.res[16 + q] = (int)(tph[q] >> 10);  // units of 1024 ns
     J.res[24] = (int)(tpo[0] >> 10);
     J.res[25] = (int)(tpo[1] >> 10);
+    for (int q = 0; q < 6; ++q) J.res[26 + q] = (int)(s_tin[q] >> 10);
     const unsigned long long g_end = global_ns();
     J.res[23] = (int)((g_end - g_start) >> 10);
     J.res[13] = (int)((g_start >> 10) & 0x7fffffffull);  // start and end, in units of 1024 ns
@@ -1919,7 +1993,7 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
   VNM_CUDA_TRY(cudaEventElapsedTime(&ctx->main_ms, ctx->ev_main0, ctx->ev_main1));
   int hres_copy[4 * JOB_RES];
   memcpy(hres_copy, hres, sizeof(int) * JOB_RES * nsched);
-  for (int q = 0; q < 24; ++q) ctx->stats[q] = 0;
+  for (int q = 0; q < 28; ++q) ctx->stats[q] = 0;
   ctx->stats[3] = P.nseg;
   ctx->stats[4] = nsched;
   ctx->stats[5] = P.np;
@@ -1949,6 +2023,7 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
     ctx->stats[16] += h[23];
     ctx->stats[20] += h[24];
     ctx->stats[21] += h[25];
+    for (int q = 0; q < 6; ++q) ctx->stats[22 + q] += h[26 + q];
   }
   if (trace) {
     const int committed = hres_copy[6];
@@ -2138,7 +2213,7 @@ static vnm_status run_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int6
   }
   VNM_TRY(end_call(ctx));
   VNM_CUDA_TRY(cudaEventElapsedTime(&ctx->main_ms, ctx->ev_main0, ctx->ev_main1));
-  for (int q = 0; q < 24; ++q) ctx->stats[q] = 0;
+  for (int q = 0; q < 28; ++q) ctx->stats[q] = 0;
   ctx->stats[3] = max_nseg;
   ctx->stats[4] = nmat;
   ctx->stats[5] = P.np;

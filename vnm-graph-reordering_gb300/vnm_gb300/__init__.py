@@ -151,8 +151,8 @@ class Context:
         return lib().vnm_last_main_kernel_ms(self.h)
 
     def last_stats(self):
-        out = (ctypes.c_longlong * 24)()
-        _check(lib().vnm_last_stats(self.h, out, 24), "vnm_last_stats")
+        out = (ctypes.c_longlong * 28)()
+        _check(lib().vnm_last_stats(self.h, out, 28), "vnm_last_stats")
         keys = ("rounds", "gathered", "touched", "nseg", "jobs", "pattern_nnz", "blocks_per_job", "table_rounds")
         d = dict(zip(keys, list(out)[:8]))
         d["phase_us"] = dict(zip(("select", "choose", "gather", "process", "heap_entries", "heaps_and_walk", "apply"),
@@ -163,6 +163,8 @@ class Context:
         d["jobs_span_us"] = out[18]
         d["clusters_fit"] = out[19]
         d["leader_own_us"] = {"process": out[20] * 1.024, "apply": out[21] * 1.024}
+        d["inside_us"] = dict(zip(("walk", "heap0", "process_warp0", "apply_warp0", "process_warp0_masks",
+                                   "process_warp0_pairs"), [x * 1.024 for x in list(out)[22:28]]))
         return d
 
     # ---- array plumbing: numpy arrays (host) or torch CUDA tensors (device)
