@@ -834,8 +834,9 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
     // VE[x][k] = (VL[x][k] & P1) | (~VL[x][k] & P0) and the solo rows of
     // bit k are VL[x][k] & P1.  Lane k < M keeps the masks of bit k in this
     // warp's scratch.
-#pragma unroll 1
-    for (int xi = 0; xi < Kn; ++xi) {
+#pragma unroll
+    for (int xi = 0; xi < K; ++xi) {
+      if (xi >= Kn) break;
       const unsigned bx = valid ? rec_byte(w, xi) : 0u;
       if (__ballot_sync(FULL, bx != 0u) == 0u) {
         if (gathered && lane < M) vw[(2 * xi) * M + lane] = vw[(2 * xi + 1) * M + lane] = 0u;
@@ -1302,6 +1303,7 @@ __device__ void walk_phase(RoundSmem<M>& sm, int sched, int wait_limit) {
 // slice of the touched rows into newinv / newpres.
 template <int M>
 __device__ void apply_recount(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl) {
+  constexpr int K = M + 1;
   const int tid = threadIdx.x;
   // a round's swaps are disjoint transpositions (the walk never reuses a
   // visited position), so each thread applies one of them
@@ -1338,9 +1340,9 @@ __device__ void apply_recount(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl)
   for_rows_warp<M, 2>(sm, J, [&](int r, const uint4& w, bool valid) {
     // the row's groups after the swaps, packed like the record
     unsigned n0 = 0, n1 = 0, n2 = 0;
-#pragma unroll 1
-    for (int xi = 0; xi < Kn; ++xi) {
-      const unsigned bb = valid ? rec_byte(w, xi) : 0u;
+#pragma unroll
+    for (int xi = 0; xi < K; ++xi) {
+      const unsigned bb = (valid && xi < Kn) ? rec_byte(w, xi) : 0u;
 #pragma unroll
       for (int h = 0; h < NH; ++h) {
         const unsigned nib = (bb >> (4 * h)) & 15u;
@@ -1353,8 +1355,9 @@ __device__ void apply_recount(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl)
       }
     }
     // non-empty and invalid groups per segment, one shared add per warp
-#pragma unroll 1
-    for (int xi = 0; xi < Kn; ++xi) {
+#pragma unroll
+    for (int xi = 0; xi < K; ++xi) {
+      if (xi >= Kn) break;
       const unsigned nb = ((xi < 4 ? n0 : (xi < 8 ? n1 : n2)) >> ((xi & 3) * 8)) & 0xffu;
       const unsigned pres = __ballot_sync(FULL, nb != 0u);
       const unsigned inv = __ballot_sync(FULL, __popc(nb) > N);
