@@ -94,7 +94,7 @@ float vnm_last_main_kernel_ms(const vnm_ctx* ctx);
  * out[20], out[21] the leaders' own work in the process and apply phases
  * (before the barriers that close them), units of 1024 ns summed over
  * jobs, out[22..27] times inside phases in the same units: the walk warp,
- * the heap thread of the first pair, warp 0 of the leader over its rows in
+ * its waits for swap-heap pops, warp 0 of the leader over its rows in
  * the process phase and in the apply phase, and that warp's per-segment
  * masks and pair corrections in the process phase.  n <= 28 values. */
 vnm_status vnm_last_stats(const vnm_ctx* ctx, long long* out, int n);

@@ -71,7 +71,7 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 // Time (ns) inside phases, accumulated by single threads of a job's leader
-// block: [0] the walk warp, [1] the heap thread of pair 0, [2] warp 0's
+// block: [0] the walk warp, [1] its waits for swap-heap pops, [2] warp 0's
 // rows in the process phase, [3] warp 0's rows in the apply phase, [4] and
 // [5] warp 0's per-segment masks and pair corrections in the process phase.
 __shared__ unsigned long long s_tin[6];
@@ -1165,13 +1165,20 @@ __device__ void walk_phase(RoundSmem<M>& sm, int sched, int wait_limit) {
   const unsigned* ent = reinterpret_cast<const unsigned*>(smem_heap) + MM * HS;  // [MM][HS], as rank_phase wrote
   bool dead = false;  // a wait ran out: the job is failed, finish without reading ord
   // pops of pair column `col` published so far, once at least `need`; -1 at the limit
+  unsigned long long waited = 0;  // ns spent waiting for pops (lane 0)
   auto wait_pops = [&](int col, int need) -> int {
     int avail = __shfl_sync(FULL, prog[col], 0);
+    if (avail >= need) {
+      __threadfence_block();
+      return avail;
+    }
+    const unsigned long long t_w = global_ns();
     for (int spin = 0; avail < need; ++spin) {
       if (spin >= wait_limit) return -1;
       avail = __shfl_sync(FULL, prog[col], 0);
     }
     __threadfence_block();
+    waited += global_ns() - t_w;
     return avail;
   };
   // bit moves of the swaps for the recount (identity elsewhere)
@@ -1296,6 +1303,7 @@ __device__ void walk_phase(RoundSmem<M>& sm, int sched, int wait_limit) {
     sm.nswaps = nsw;
     if (dead) sm.status |= JOB_WAIT_LIMIT;
     *(volatile int*)&sm.hstop = 1;
+    s_tin[1] += waited;
   }
 }
 
@@ -1545,7 +1553,6 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
       if (tid >= NM_THREADS - 32) walk_phase<M>(sm, J.sched, J.walk_wait_limit);  // the last warp walks ...
       else if (!J.hold_heaps) heap_sift<M>(sm);                                   // ... while the heaps pop
       if (tid == NM_THREADS - 32) s_tin[0] += global_ns() - t_in;
-      else if (tid == 0) s_tin[1] += global_ns() - t_in;
       __syncthreads();
       VNM_PHASE(5);
       if (tid == 0 && J.trace_pairs) {

@@ -163,7 +163,7 @@ class Context:
         d["jobs_span_us"] = out[18]
         d["clusters_fit"] = out[19]
         d["leader_own_us"] = {"process": out[20] * 1.024, "apply": out[21] * 1.024}
-        d["inside_us"] = dict(zip(("walk", "heap0", "process_warp0", "apply_warp0", "process_warp0_masks",
+        d["inside_us"] = dict(zip(("walk", "walk_waits", "process_warp0", "apply_warp0", "process_warp0_masks",
                                    "process_warp0_pairs"), [x * 1.024 for x in list(out)[22:28]]))
         return d
 
