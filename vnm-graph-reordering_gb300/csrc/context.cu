@@ -53,8 +53,10 @@ vnm_status end_call(vnm_ctx* ctx) {
 }
 
 // ---------------------------------------------------------------------------
-// Exclusive prefix sum: block-local scans of 2048 elements, a scan of the
-// block totals (recursively), then a uniform add.
+// Exclusive prefix sum: block-local scans of 2048 elements (one launch when
+// that is all), then each block adds the sum of the tiles before it, read
+// straight from the tile totals (up to 2048 tiles: two launches); longer
+// arrays scan the tile totals recursively first.
 // ---------------------------------------------------------------------------
 constexpr int SCAN_NT = 512;
 constexpr int SCAN_PER = 4;
@@ -101,6 +103,31 @@ __global__ void __launch_bounds__(SCAN_NT) k_scan_tiles(const int* in, int* out,
   if (threadIdx.x == SCAN_NT - 1) tile_sums[blockIdx.x] = run;
 }
 
+// Block b: add tiles 0 .. b-1's totals to its tile; the last block also
+// writes the grand total.
+__global__ void __launch_bounds__(SCAN_NT) k_scan_fix(int* out, int n, const int* tile_sums, int tiles, int* total) {
+  __shared__ int warp_tot[SCAN_NT / 32];
+  const int b = blockIdx.x;
+  int s = 0;
+  for (int t = threadIdx.x; t < b; t += SCAN_NT) s += tile_sums[t];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) warp_tot[threadIdx.x >> 5] = s;
+  __syncthreads();
+  int off = 0;
+#pragma unroll
+  for (int w = 0; w < SCAN_NT / 32; ++w) off += warp_tot[w];
+  if (b > 0) {
+    const int i = b * SCAN_TILE + threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < SCAN_PER; ++q) {
+      const int k = i + q * SCAN_NT;
+      if (k < n) out[k] += off;
+    }
+  }
+  if (total && b == tiles - 1 && threadIdx.x == 0) *total = off + tile_sums[b];
+}
+
 __global__ void k_scan_add(int* out, int n, const int* tile_off) {
   const int i = blockIdx.x * SCAN_TILE + threadIdx.x;
   const int add = tile_off[blockIdx.x];
@@ -118,6 +145,14 @@ __global__ void k_scan_total(const int* in_last, const int* out_last, int* total
 vnm_status exclusive_scan(vnm_ctx* ctx, const int* d_in, int* d_out, int n, int* d_total) {
   if (n <= 0) {
     if (d_total) VNM_CUDA_TRY(cudaMemsetAsync(d_total, 0, sizeof(int), ctx->stream));
+    return VNM_OK;
+  }
+  const int ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+  if (ntiles <= SCAN_TILE) {  // up to 4 M elements: the tile scans, then one fix-up launch
+    int* sums = arena_take<int>(ctx, ntiles);
+    if (!sums) return VNM_ERR_NOMEM;
+    VNM_LAUNCH(ctx, k_scan_tiles, ntiles, SCAN_NT, 0, d_in, d_out, n, sums);
+    if (ntiles > 1 || d_total) VNM_LAUNCH(ctx, k_scan_fix, ntiles, SCAN_NT, 0, d_out, n, sums, ntiles, d_total);
     return VNM_OK;
   }
   // the last input is read back for the total before d_out may overwrite it
@@ -138,7 +173,7 @@ vnm_status exclusive_scan(vnm_ctx* ctx, const int* d_in, int* d_out, int n, int*
 
 // upper bound of the arena scratch exclusive_scan takes for n elements
 size_t scan_scratch_bytes(int n) {
-  size_t b = 0;
+  size_t b = arena_bytes((n + SCAN_TILE - 1) / SCAN_TILE + 1, sizeof(int));
   while (true) {
     b += arena_bytes(1, sizeof(int));
     int tiles = (n + SCAN_TILE - 1) / SCAN_TILE;

@@ -142,10 +142,28 @@ __global__ void k_cmp_group_start(const int* flag_scan, const unsigned long long
     if (i == 0 || keys[i] / VM != keys[i - 1] / VM) gstart[flag_scan[i]] = i;
 }
 
-__global__ void k_cmp_scale(const int* row, const float* val, int nnz, int V, unsigned* bmax) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += gridDim.x * blockDim.x) {
-    const float a = fabsf(val[i]);
-    if (a > 0.f) atomicMax(&bmax[row[i] / V], __float_as_uint(a));
+// max |a| per block row of V rows, over the entries in sorted order: a
+// thread takes SCALE_RUN consecutive entries (nearly always of one block
+// row) and issues one atomic per block row it saw, instead of one per entry
+// all landing on a few hundred words.
+constexpr int SCALE_RUN = 16;
+__global__ void k_cmp_scale(const unsigned long long* skeys, const int* spos, const float* val, int nnz, int VM,
+                            int nseg, unsigned* bmax) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t * SCALE_RUN < nnz;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int b = (int)(t * SCALE_RUN), e = min(b + SCALE_RUN, nnz);
+    long long cur = -1;
+    unsigned m = 0;
+    for (int i = b; i < e; ++i) {
+      const long long br = (long long)((skeys[i] / (unsigned long long)VM) / (unsigned long long)nseg);
+      if (br != cur) {
+        if (m) atomicMax(&bmax[cur], m);
+        cur = br;
+        m = 0;
+      }
+      m = max(m, __float_as_uint(fabsf(val[spos[i]])));  // non-negative floats order like their bits
+    }
+    if (m) atomicMax(&bmax[cur], m);
   }
 }
 
@@ -821,7 +839,8 @@ static vnm_status compress_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, con
     VNM_LAUNCH(ctx, k_cmp_heads, sp_grid(ctx, nnz), 256, 0, skeys, nnz, V * M, flag);
     VNM_TRY(exclusive_scan(ctx, flag, flag, nnz, counters));
     VNM_LAUNCH(ctx, k_cmp_group_start, sp_grid(ctx, nnz), 256, 0, flag, skeys, nnz, V * M, gstart);
-    VNM_LAUNCH(ctx, k_cmp_scale, sp_grid(ctx, nnz), 256, 0, d_row, d_val, nnz, V, bmax);
+    VNM_LAUNCH(ctx, k_cmp_scale, sp_grid(ctx, (nnz + SCALE_RUN - 1) / SCALE_RUN), 256, 0, skeys, spos, d_val, nnz,
+               V * M, nseg, bmax);
     VNM_CUDA_TRY(cudaMemcpyAsync(h, counters, sizeof(int), cudaMemcpyDeviceToHost, st));
     VNM_CUDA_TRY(cudaStreamSynchronize(st));
     ngroups = h[0];
