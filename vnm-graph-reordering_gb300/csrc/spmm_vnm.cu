@@ -97,6 +97,7 @@ constexpr uint32_t SP_WAIT_LIMIT = 1u << 22;  // polls before a wait gives up
 constexpr int RES_CHUNK = 256;    // residual nonzeros per task, at most
 constexpr int RES_THREADS = 256;
 constexpr int RES_U = 8;          // entries in flight per lane group (8 measured ahead of 4)
+constexpr int RES_BLOCKS_PER_SM = 4;  // resident blocks of k_spmm_res an SM (64 registers a thread)
 // A block runs on the tensor cores when it holds at least V nonzeros (one
 // a row on average), else on the CUDA cores.  Measured on GB300 with the
 // R-MAT 16384 (V=64, n=128) and Chung-Lu 262144 (V=128, n=256) operands,
@@ -435,49 +436,68 @@ __device__ __forceinline__ void fma8(float (&acc)[8], uint4 b, float w) {
   }
 }
 
-// One task per group of LW lanes (32 / LW tasks per warp); each lane owns 8
-// consecutive columns of the block's 8 * LW.  Every lane of a group reads
-// the same (column, value) record (one 8-byte load served once for the
-// group) and gathers its 16 bytes of that B row, RES_U entries in flight.
-// Loop trip counts are the warp's maximum; a group past its end reads a
-// zero weight and a zero row, so the arithmetic needs no predicate.
+// Groups of LW lanes (32 / LW per warp) walk the task list with a stride
+// of every group of the grid (one wave of resident blocks); each lane owns 8
+// consecutive columns of the block's 8 * LW.  The records of a task are read
+// LW at a time, lane l of the group holding record l, and handed to the
+// lanes by shuffles; every lane gathers its 16 bytes of each B row, RES_U
+// rows in flight.  The next batch of records, and the next task with its
+// first batch, are loaded while the current ones are worked on, so a short
+// task costs about one round trip for its B rows.  Loop trip counts are the
+// warp's maximum; a group past its end reads a zero weight and a zero row,
+// so the arithmetic needs no predicate.
 template <int LW, bool BF16>
-__global__ void __launch_bounds__(RES_THREADS)
+__global__ void __launch_bounds__(RES_THREADS, RES_BLOCKS_PER_SM)
     k_spmm_res(const int4* __restrict__ task, int ntask, const int2* __restrict__ rcv,
                const unsigned char* __restrict__ B, size_t ldb, float* __restrict__ C, int ldc,
                float* __restrict__ P, int ldp) {
   constexpr int G = 32 / LW;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, grp = lane / LW, lid = lane % LW;
-  const int t = (blockIdx.x * (RES_THREADS / 32) + warp) * G + grp;
+  const int stride = gridDim.x * (RES_THREADS / 32) * G;
+  int t = (blockIdx.x * (RES_THREADS / 32) + warp) * G + grp;
   const int cb = blockIdx.y * (8 * LW) + lid * 8;  // this lane's first column
-  const int4 tk = t < ntask ? task[t] : make_int4(0, 0, 0, -1);
-  const int len = tk.z - tk.y;
-  const int maxlen = G == 1 ? len : __reduce_max_sync(0xffffffffu, len);
-  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   const unsigned char* bcol = B + (size_t)cb * 2;
-  const int2* ent = rcv + tk.y;
-  // the records of the next RES_U entries are loaded one iteration ahead,
-  // so an iteration waits on one global load (the B rows), not two
-  int2 e[RES_U];
+  int4 tk = t < ntask ? task[t] : make_int4(0, 0, 0, -1);
+  int2 rc = tk.y + lid < tk.z ? __ldg(rcv + tk.y + lid) : make_int2(0, 0);
+  int4 tkn = t + stride < ntask ? task[t + stride] : make_int4(0, 0, 0, -1);
+  while (__any_sync(0xffffffffu, t < ntask)) {
+    const int len = tk.z - tk.y;  // 0 past the end
+    const int maxlen = G == 1 ? len : __reduce_max_sync(0xffffffffu, len);
+    // the next task's first records, and the task after it
+    const int2 rc1 = tkn.y + lid < tkn.z ? __ldg(rcv + tkn.y + lid) : make_int2(0, 0);
+    const int4 tk2 = t + 2 * stride < ntask ? task[t + 2 * stride] : make_int4(0, 0, 0, -1);
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int k0 = 0; k0 < maxlen; k0 += LW) {
+      const int kn = k0 + LW + lid;
+      const int2 rcn = kn < len ? __ldg(rcv + tk.y + kn) : make_int2(0, 0);
+#pragma unroll 1
+      for (int u0 = 0; u0 < LW; u0 += RES_U) {
+        if (k0 + u0 >= maxlen) break;
+        uint4 b[RES_U];
 #pragma unroll
-  for (int u = 0; u < RES_U; ++u) e[u] = u < len ? __ldg(ent + u) : make_int2(0, 0);
-  for (int k = 0; k < maxlen; k += RES_U) {
-    uint4 b[RES_U];
+        for (int u = 0; u < RES_U; ++u) {
+          const int col = __shfl_sync(0xffffffffu, rc.x, grp * LW + u0 + u);
+          b[u] = k0 + u0 + u < len ? __ldg(reinterpret_cast<const uint4*>(bcol + (size_t)col * ldb))
+                                   : make_uint4(0, 0, 0, 0);
+        }
+        // the weights are fetched once the rows are in flight
 #pragma unroll
-    for (int u = 0; u < RES_U; ++u)
-      b[u] = k + u < len ? __ldg(reinterpret_cast<const uint4*>(bcol + (size_t)e[u].x * ldb)) : make_uint4(0, 0, 0, 0);
-    int2 en[RES_U];
-#pragma unroll
-    for (int u = 0; u < RES_U; ++u) en[u] = k + RES_U + u < len ? __ldg(ent + k + RES_U + u) : make_int2(0, 0);
-#pragma unroll
-    for (int u = 0; u < RES_U; ++u) fma8<BF16>(acc, b[u], __int_as_float(e[u].y));
-#pragma unroll
-    for (int u = 0; u < RES_U; ++u) e[u] = en[u];
-  }
-  if (t < ntask) {
-    float* dst = tk.w < 0 ? C + (size_t)tk.x * ldc + cb : P + (size_t)tk.w * ldp + cb;
-    reinterpret_cast<float4*>(dst)[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
-    reinterpret_cast<float4*>(dst)[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
+        for (int u = 0; u < RES_U; ++u) {
+          const int vbits = __shfl_sync(0xffffffffu, rc.y, grp * LW + u0 + u);
+          fma8<BF16>(acc, b[u], k0 + u0 + u < len ? __int_as_float(vbits) : 0.f);
+        }
+      }
+      rc = rcn;
+    }
+    if (t < ntask) {
+      float* dst = tk.w < 0 ? C + (size_t)tk.x * ldc + cb : P + (size_t)tk.w * ldp + cb;
+      reinterpret_cast<float4*>(dst)[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+      reinterpret_cast<float4*>(dst)[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
+    }
+    t += stride;
+    tk = tkn;
+    tkn = tk2;
+    rc = rc1;
   }
 }
 
@@ -1064,8 +1084,11 @@ static vnm_status spmm_enqueue(vnm_ctx* ctx, const vnm_spmm_matrix* A, const voi
   auto launch_res = [&]() -> vnm_status {
     if (A->ntask > 0) {
       const int lw = (n % 256) == 0 ? 32 : (n % 128) == 0 ? 16 : 8;
+      // one wave of resident blocks (the task list is walked with a stride)
       const int per_block = (RES_THREADS / 32) * (32 / lw);
-      dim3 grid((unsigned)((A->ntask + per_block - 1) / per_block), (unsigned)(n / (8 * lw)));
+      int bx = (A->ntask + per_block - 1) / per_block;
+      if (bx > ctx->num_sms * RES_BLOCKS_PER_SM) bx = ctx->num_sms * RES_BLOCKS_PER_SM;
+      dim3 grid((unsigned)bx, (unsigned)(n / (8 * lw)));
 #define VNM_RES(LWV, BFV)                                                                                   \
   VNM_LAUNCH(ctx, (k_spmm_res<LWV, BFV>), grid, RES_THREADS, 0, A->task, A->ntask, A->rcv, p.B, p.ldb, dC, \
              n, P, n)
