@@ -406,33 +406,29 @@ __global__ void k_cmp_rscale(const unsigned* bmax, int ntiles, int R, int V, flo
 // ---------------------------------------------------------------------------
 // Residual kernels (CUDA cores)
 // ---------------------------------------------------------------------------
-// acc[0..7] += w * the 8 16-bit values in b (element 0 in the low half of
-// b.x), as four packed FP32 FMAs (fma.rn.f32x2: two round-to-nearest FP32
-// FMAs, the same results as eight scalar ones in half the instructions).
-__device__ __forceinline__ void fma2(float& a0, float& a1, float w, float x0, float x1) {
-  unsigned long long acc = ((unsigned long long)__float_as_uint(a1) << 32) | __float_as_uint(a0);
-  const unsigned long long ww = ((unsigned long long)__float_as_uint(w) << 32) | __float_as_uint(w);
-  const unsigned long long xx = ((unsigned long long)__float_as_uint(x1) << 32) | __float_as_uint(x0);
-  asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(acc) : "l"(ww), "l"(xx));
-  a0 = __uint_as_float((unsigned)acc);
-  a1 = __uint_as_float((unsigned)(acc >> 32));
-}
-
+// acc[0..3] (4 pairs of FP32 accumulators, packed two to a 64-bit register,
+// element 0 in the low half) += w * the 8 16-bit values in b (element 0 in
+// the low half of b.x), as four packed FP32 FMAs (fma.rn.f32x2: two
+// round-to-nearest FP32 FMAs, the same results as eight scalar ones in half
+// the instructions); ww is w in both halves.  The accumulators stay packed
+// for a whole task.
 template <bool BF16>
-__device__ __forceinline__ void fma8(float (&acc)[8], uint4 b, float w) {
+__device__ __forceinline__ void fma8(unsigned long long (&acc)[4], uint4 b, unsigned long long ww) {
   const uint32_t q[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    float lo, hi;
+    uint32_t lo, hi;
     if (BF16) {
-      lo = __uint_as_float(q[i] << 16);
-      hi = __uint_as_float(q[i] & 0xffff0000u);
+      lo = q[i] << 16;
+      hi = q[i] & 0xffff0000u;
     } else {
       const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&q[i]));
-      lo = f.x;
-      hi = f.y;
+      lo = __float_as_uint(f.x);
+      hi = __float_as_uint(f.y);
     }
-    fma2(acc[2 * i], acc[2 * i + 1], w, lo, hi);
+    unsigned long long xx;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(xx) : "r"(lo), "r"(hi));
+    asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(acc[i]) : "l"(ww), "l"(xx));
   }
 }
 
@@ -466,7 +462,7 @@ __global__ void __launch_bounds__(RES_THREADS, RES_BLOCKS_PER_SM)
     // the next task's first records, and the task after it
     const int2 rc1 = tkn.y + lid < tkn.z ? __ldg(rcv + tkn.y + lid) : make_int2(0, 0);
     const int4 tk2 = t + 2 * stride < ntask ? task[t + 2 * stride] : make_int4(0, 0, 0, -1);
-    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    unsigned long long acc[4] = {0ull, 0ull, 0ull, 0ull};  // FP32 pairs
     for (int k0 = 0; k0 < maxlen; k0 += LW) {
       const int kn = k0 + LW + lid;
       const int2 rcn = kn < len ? __ldg(rcv + tk.y + kn) : make_int2(0, 0);
@@ -484,15 +480,24 @@ __global__ void __launch_bounds__(RES_THREADS, RES_BLOCKS_PER_SM)
 #pragma unroll
         for (int u = 0; u < RES_U; ++u) {
           const int vbits = __shfl_sync(0xffffffffu, rc.y, grp * LW + u0 + u);
-          fma8<BF16>(acc, b[u], k0 + u0 + u < len ? __int_as_float(vbits) : 0.f);
+          const uint32_t w = k0 + u0 + u < len ? (uint32_t)vbits : 0u;
+          unsigned long long ww;
+          asm("mov.b64 %0, {%1, %1};" : "=l"(ww) : "r"(w));
+          fma8<BF16>(acc, b[u], ww);
         }
       }
       rc = rcn;
     }
     if (t < ntask) {
       float* dst = tk.w < 0 ? C + (size_t)tk.x * ldc + cb : P + (size_t)tk.w * ldp + cb;
-      reinterpret_cast<float4*>(dst)[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
-      reinterpret_cast<float4*>(dst)[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
+      float f[8];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        f[2 * i] = __uint_as_float((uint32_t)acc[i]);
+        f[2 * i + 1] = __uint_as_float((uint32_t)(acc[i] >> 32));
+      }
+      reinterpret_cast<float4*>(dst)[0] = make_float4(f[0], f[1], f[2], f[3]);
+      reinterpret_cast<float4*>(dst)[1] = make_float4(f[4], f[5], f[6], f[7]);
     }
     t += stride;
     tk = tkn;
