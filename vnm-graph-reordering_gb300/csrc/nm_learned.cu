@@ -322,23 +322,31 @@ __global__ void __launch_bounds__(L_THREADS, 1)
   const int nwork = kPlain ? (nX + 127) / 128 : *nactive_p;
   const int ntile = kPlain ? 1 : (ncand + 127) / 128;
   uint32_t phase = 0;
+  // this thread's features of candidate `tid` of tile (a, tile); the next
+  // tile's are computed while the tensor core runs the current one's first
+  // layer, so their loads' latency is hidden behind it
+  auto feats = [&](int a, int tile, float (&f)[LF]) {
+    const int c = kPlain ? a * 128 + tid : tile * 128 + tid;
+    const bool live = a < nwork && (kPlain ? c < nX : c < ncand);
+    if (!live) {
+#pragma unroll
+      for (int k = 0; k < LF; ++k) f[k] = 0.f;
+    } else if (kPlain) {
+#pragma unroll
+      for (int k = 0; k < LF; ++k) f[k] = X[(size_t)c * LF + k];
+    } else {
+      int q, i, j;
+      cand_of(c, L.M, q, i, j);
+      const int p = active[a];
+      features(L, p, i, target_of(p, q, round, L.nseg, seed), j, f);
+    }
+  };
+  float f[LF];
+  feats(blockIdx.x, 0, f);
   for (int a = blockIdx.x; a < nwork; a += gridDim.x) {
-    const int p = kPlain ? 0 : active[a];
     for (int tile = 0; tile < ntile; ++tile) {
-      float f[LF];
       const int c = kPlain ? a * 128 + tid : tile * 128 + tid;
       const bool live = kPlain ? c < nX : c < ncand;
-      if (!live) {
-#pragma unroll
-        for (int k = 0; k < LF; ++k) f[k] = 0.f;
-      } else if (kPlain) {
-#pragma unroll
-        for (int k = 0; k < LF; ++k) f[k] = X[(size_t)c * LF + k];
-      } else {
-        int q, i, j;
-        cand_of(c, L.M, q, i, j);
-        features(L, p, i, target_of(p, q, round, L.nseg, seed), j, f);
-      }
 #pragma unroll
       for (int k = 0; k < LF; k += 2)
         *reinterpret_cast<__nv_bfloat162*>(sm.A1 + kmaj_off(tid, k, LF)) = __floats2bfloat162_rn(f[k], f[k + 1]);
@@ -354,6 +362,10 @@ __global__ void __launch_bounds__(L_THREADS, 1)
         }
         ptx::mma_commit(&sm.bar1);
       }
+      // the next tile's features (A1 is rewritten only after this tile's
+      // second barrier, by which time the first layer has read it)
+      if (tile + 1 < ntile) feats(a, tile + 1, f);
+      else feats(a + gridDim.x, 0, f);
       if (!ptx::mbar_wait(&sm.bar1, phase, L_WAIT)) sm.err = 1;
       ptx::tc_fence_after();
       // layer 1 epilogue: bias, ReLU, BF16 -> A2
