@@ -573,10 +573,11 @@ struct SpmmArgs {
   uint32_t wait_limit;  // polls of a pipeline wait (copies <-> MMAs) before it gives up
 };
 
-// K-steps in flight per CTA.  16 stages were measured slower on a full
-// V:2:8 operand (19456 rows, n=256: 0.29 vs 0.25 ms): their shared memory
-// leaves one CTA per SM at every column-block width.
-constexpr int SP_STAGES = 8;
+// K-steps in flight per CTA (192 KB of stages at NT = 256).  On a full
+// V:2:8 operand (19456 rows, n=256) with three producer warps: 8 stages
+// 0.161 ms, 10 0.145, 12 0.143, 14 0.133, 16 0.128 (one producer warp had
+// been faster with 8: 0.25 against 0.29 ms).
+constexpr int SP_STAGES = 16;
 constexpr int SP_PF = 8;      // pairs of K-steps whose column ids are loaded ahead (the ids come from DRAM)
 
 template <int NT>
@@ -739,12 +740,15 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
     __syncthreads();
     ptx::tc_fence_after();
     if (ok && !sm.abort) {
-      const int row = t * SP_TM + warp * 32 + lane;
+      // warp w reads TMEM lanes 32 (w % 4) ..; the SP_THREADS / 128 warps of
+      // a lane quarter split the columns
+      constexpr int EG = SP_THREADS / 128, CW = NT / EG;
+      const int row = t * SP_TM + (warp & 3) * 32 + lane;
       const float sc = row < p.R ? p.rscale[row] : 0.f;
 #pragma unroll 1
-      for (int c0 = 0; c0 < NT; c0 += 32) {
+      for (int c0 = (warp >> 2) * CW; c0 < (warp >> 2) * CW + CW; c0 += 32) {
         uint32_t v[32];
-        ptx::tmem_ld_32x32b_x32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+        ptx::tmem_ld_32x32b_x32(tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)c0, v);
         ptx::tmem_ld_wait();
         if (row < p.R) {
           float4* dst = reinterpret_cast<float4*>(p.C + (size_t)row * p.ldc + n0 + c0);
