@@ -184,16 +184,22 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("step", choices=["prepare", "run", "serve", "collect"])
     ap.add_argument("--ref", default=DEFAULT_REF)
-    ap.add_argument("--out", default=os.path.join(REPO, "gpurun_out", "cli_ref"))
-    ap.add_argument("--src", default=os.path.join(REPO, "gpurun_out", "cli_ref"))
+    ap.add_argument("--out", help="run: the folder the raw outputs go to (one that comes back from the GPU machine)")
+    ap.add_argument("--src", help="serve / collect: that folder, back where the checkout is")
     a = ap.parse_args()
     if a.step == "prepare":
         prepare(a.ref)
     elif a.step == "run":
+        if not a.out:
+            ap.error("run needs --out")
         sys.exit(run(a.out))
     elif a.step == "serve":
+        if not a.src:
+            ap.error("serve needs --src")
         serve(a.src, a.ref)
     else:
+        if not a.src:
+            ap.error("collect needs --src")
         collect(a.src)
 
 

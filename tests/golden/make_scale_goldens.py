@@ -30,8 +30,8 @@ output.txt, the (row, col) of the matrix it writes back in entry order,
 and its wall seconds (this machine's, for the record).
 
 usage: python tests/golden/make_scale_goldens.py oracle [--only c2|c4] [--threads T]
-       python tests/golden/make_scale_goldens.py ref-run [--out DIR]
-       python tests/golden/make_scale_goldens.py ref-collect [--src DIR]
+       python tests/golden/make_scale_goldens.py ref-run --out DIR
+       python tests/golden/make_scale_goldens.py ref-collect --src DIR
        python tests/golden/make_scale_goldens.py vnm-ref [--ref DIR]
 """
 import argparse
@@ -180,12 +180,16 @@ def main():
     ap.add_argument("--ref", default=DEFAULT_REF)
     ap.add_argument("--only", choices=sorted(WORKLOADS), default=None)
     ap.add_argument("--threads", type=int, default=max(1, (os.cpu_count() or 4) // 4))
-    ap.add_argument("--out", default=os.path.join(REPO, "gpurun_out", "ref_c2"))
-    ap.add_argument("--src", default=os.path.join(REPO, "gpurun_out", "ref_c2"))
+    ap.add_argument("--out", help="ref-run: the folder the raw outputs go to (one that comes back from the GPU machine)")
+    ap.add_argument("--src", help="ref-collect: that folder")
     a = ap.parse_args()
     if a.step == "ref-run":
+        if not a.out:
+            ap.error("ref-run needs --out")
         return ref_run(a.out)
     if a.step == "ref-collect":
+        if not a.src:
+            ap.error("ref-collect needs --src")
         return ref_collect(a.src)
     if a.step == "vnm-ref":
         return vnm_ref(a.ref)

@@ -2,8 +2,8 @@
 
 Error measure: the largest per-row relative error
 max_i ||C_i - C64_i||_inf / ||C64_i||_inf (oracle.rowwise_rel_err; a row whose
-reference is zero must come out zero), tolerance 1e-2 as the benchmark spec
-states for BF16/FP16 operands with FP32 accumulation.  Per row, so that a
+reference is zero must come out zero), tolerance 1e-2 for BF16/FP16
+operands with FP32 accumulation.  Per row, so that a
 low-degree row cannot hide behind the hub rows of a power-law graph."""
 import numpy as np
 import pytest

@@ -7,7 +7,7 @@
 // objective (fewer invalid M-groups, i.e. more retained nonzeros) built for a
 // GPU: every round, every invalid segment p proposes swaps with the nodes of
 // KT sampled target segments, the MLP scores all of them, only the best 8 per
-// segment are scored exactly (integer kernel, the judge), and a claim-based
+// segment are scored exactly (the integer kernel decides), and a claim-based
 // matching accepts at most one improving swap per segment, so the accepted
 // swaps touch disjoint segments and their exact gains add up.  An exhaustive
 // mode scores every candidate exactly instead (the fallback and the baseline
