@@ -281,9 +281,10 @@ class Context:
         return out, r, c, newpos
 
     # ---- batches
-    def nm_reorder_batch(self, mats, N, M, sched, nm_maxiter=10, want_newpos=True):
-        """Reorder many matrices [(nrows, row, col, val), ...] in one launch.
-        Returns (res5 [nmat, 5], list of newpos arrays or None)."""
+    @staticmethod
+    def pack_batch(mats):
+        """The arrays of vnm_nm_reorder_batch for [(nrows, row, col, val), ...]:
+        (nrows, nnz_offset, row, col, val), each matrix's entries in turn."""
         nmat = len(mats)
         nrows = np.array([m[0] for m in mats], np.int32)
         off = np.zeros(nmat + 1, np.int64)
@@ -291,6 +292,14 @@ class Context:
         row = np.ascontiguousarray(np.concatenate([m[1] for m in mats]) if nmat else np.zeros(0), np.int32)
         col = np.ascontiguousarray(np.concatenate([m[2] for m in mats]) if nmat else np.zeros(0), np.int32)
         val = np.ascontiguousarray(np.concatenate([m[3] for m in mats]) if nmat else np.zeros(0), np.float32)
+        return nrows, off, row, col, val
+
+    def nm_reorder_batch(self, mats, N, M, sched, nm_maxiter=10, want_newpos=True):
+        """Reorder many matrices [(nrows, row, col, val), ...] (or the arrays
+        of pack_batch) in one launch.  Returns (res5 [nmat, 5], list of
+        newpos arrays or None)."""
+        nrows, off, row, col, val = mats if isinstance(mats, tuple) else self.pack_batch(mats)
+        nmat = len(nrows)
         res = np.zeros(5 * max(nmat, 1), np.int32)
         tot = int(nrows.sum()) if nmat else 0
         newpos = np.zeros(max(tot, 1), np.int32) if want_newpos else None
