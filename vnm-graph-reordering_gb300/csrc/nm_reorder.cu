@@ -750,7 +750,7 @@ __device__ __forceinline__ void for_touched_warp(const RoundSmem<M>& sm, const N
     }
     first = false;
 #pragma unroll 1
-    for (int u = 0; u < TOUCH_U && (c0 + u * NWt) * 32 < nt; ++u) f(rv[u], wv[u], rv[u] >= 0);
+    for (int u = 0; u < TOUCH_U && (c0 + u * NWt) * 32 < nt; ++u) f(rv[u], wv[u], rv[u] >= 0, c0 + u * NWt);
   }
 }
 
@@ -767,7 +767,7 @@ __device__ __forceinline__ void for_rows_warp(const RoundSmem<M>& sm, const NMJo
       const int i = base + lane;
       const int slot = i < n ? sm.tlist[i] : 0;
       const uint4 v = i < n ? sm.table[slot] : make_uint4(0u, 0u, 0u, 0u);
-      f(slot, v, i < n);
+      f(slot, v, i < n, base >> 5);
     }
   } else {
     for_touched_warp<M, CM>(sm, J, f);
@@ -791,18 +791,21 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
   const int lane = threadIdx.x & 31;
   // this warp's row masks: VL[x][k] at vw[2x * M + k], VE[x][k] at vw[(2x + 1) * M + k]
   extern __shared__ uint4 smem_heap[];
-  unsigned* vw = reinterpret_cast<unsigned*>(smem_heap) + (threadIdx.x >> 5) * (2 * K * M);
+  unsigned* vw_warp = reinterpret_cast<unsigned*>(smem_heap) + (threadIdx.x >> 5) * (2 * K * M);
   const unsigned long long t_in = (threadIdx.x == 0 && sl.rank == 0) ? global_ns() : 0ull;
-  // At most one 32-row chunk a warp: every warp leaves its chunk's masks in
-  // its scratch and the sums are made afterwards, one thread an entry over
-  // all chunks (gathered), instead of a shared atomic per chunk, pair and
-  // entry: those atomics, and the mask loads queued behind them, were 90 %
-  // of the process phase at R-MAT 16384 2:4.
-  constexpr int NW = NM_THREADS / 32;
+  // When every 32-row chunk's masks fit the scratch, each chunk leaves them
+  // there and the sums are made afterwards over all chunks (gathered),
+  // instead of a shared atomic per chunk, pair and entry: those atomics, and
+  // the mask loads queued behind them, were 90 % of the process phase at
+  // R-MAT 16384 2:4.
+  constexpr int NCH = RoundSmem<M>::SCR_U4 * 16 / (2 * K * M * 4);  // chunks whose masks fit the scratch
+  static_assert(NCH >= NM_THREADS / 32, "one chunk a warp fits the scratch");
   const int nchunks = ((sm.use_table ? sm.tcount : sm.ntouched) + 31) / 32;
-  const bool gathered = !self && nchunks <= NW;
-  for_rows_warp<M, 1>(sm, J, [&](int r, const uint4& w, bool valid) {
+  const bool gathered = !self && nchunks <= NCH;
+  for_rows_warp<M, 1>(sm, J, [&](int r, const uint4& w, bool valid, int chunk) {
     (void)r;
+    // chunk c's masks at c * 2KM when they are summed afterwards, else this warp's
+    unsigned* vw = gathered ? reinterpret_cast<unsigned*>(smem_heap) + chunk * (2 * K * M) : vw_warp;
     const unsigned long long t_a = (threadIdx.x == 0 && sl.rank == 0) ? global_ns() : 0ull;
     unsigned b[K];
     int p[K];
@@ -910,38 +913,91 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
   });
   __syncthreads();
   if (gathered) {
-    // one thread an entry of S, CL, CR (in that order, as laid out), summed
-    // over the chunks' masks; warp w's chunk left them at w * 2KM
+    // sums over the chunks' masks (chunk c's at c * 2KM)
     const unsigned long long t_g = (threadIdx.x == 0 && sl.rank == 0) ? global_ns() : 0ull;
     const unsigned* vb = reinterpret_cast<const unsigned*>(smem_heap);
     constexpr int NP = RoundSmem<M>::NPAIR;
-    constexpr int NSUM = K * M + 2 * NP * MM;
-    for (int e = threadIdx.x; e < NSUM; e += NM_THREADS) {
-      int sum = 0;
-      if (e < K * M) {  // S[x][k] = rows with bit k and popcount N+1 = popc(VL & VE)
-        const int xi = e / M, k = e % M;
-        if (xi < Kn)
-          for (int w = 0; w < nchunks; ++w) {
-            const unsigned* v = vb + w * (2 * K * M);
-            sum += __popc(v[(2 * xi) * M + k] & v[(2 * xi + 1) * M + k]);
-          }
-        if (sum) atomicAdd(&sm.S[xi][k], sum);
-      } else {
-        const int f = e - K * M, side = f / (NP * MM), rem = f % (NP * MM);
-        const int pid = rem / MM, idx = rem % MM, i = idx / M, j = idx % M;
+    if constexpr (M % 4 == 0 && M >= 8) {
+      // thread (pair, i) makes CL(i, .) and CR(i, .) of its pair from
+      // VE[a][i], VL[a][i] and the 16-byte rows VL[c][.], VE[c][.] of each
+      // chunk; the K * M threads after them make S[x][k] = popc(VL & VE)
+      const int t = threadIdx.x;
+      if (t < NP * M) {
+        const int pid = t / M, i = t % M;
         int a = 0, q = pid;  // pair (a, c), a < c, of pair_id
         while (q >= K - 1 - a) {
           q -= K - 1 - a;
           ++a;
         }
         const int c = a + 1 + q;
-        if (c < Kn)
+        if (c < Kn) {
+          int cl[M], cr[M];
+#pragma unroll
+          for (int j = 0; j < M; ++j) cl[j] = cr[j] = 0;
           for (int w = 0; w < nchunks; ++w) {
             const unsigned* v = vb + w * (2 * K * M);
-            sum += side == 0 ? __popc(v[(2 * a + 1) * M + i] & v[(2 * c) * M + j])   // CL: VE[a][i] & VL[c][j]
-                             : __popc(v[(2 * a) * M + i] & v[(2 * c + 1) * M + j]);  // CR: VL[a][i] & VE[c][j]
+            const unsigned ea = v[(2 * a + 1) * M + i], la = v[(2 * a) * M + i];
+#pragma unroll
+            for (int h = 0; h < M / 4; ++h) {
+              const uint4 x = reinterpret_cast<const uint4*>(v + (2 * c) * M)[h];
+              const uint4 y = reinterpret_cast<const uint4*>(v + (2 * c + 1) * M)[h];
+              cl[4 * h] += __popc(ea & x.x);  // VE[a][i] & VL[c][j]
+              cl[4 * h + 1] += __popc(ea & x.y);
+              cl[4 * h + 2] += __popc(ea & x.z);
+              cl[4 * h + 3] += __popc(ea & x.w);
+              cr[4 * h] += __popc(la & y.x);  // VL[a][i] & VE[c][j]
+              cr[4 * h + 1] += __popc(la & y.y);
+              cr[4 * h + 2] += __popc(la & y.z);
+              cr[4 * h + 3] += __popc(la & y.w);
+            }
           }
-        if (sum) atomicAdd(side == 0 ? &sm.CL[pid][idx] : &sm.CR[pid][idx], sum);
+#pragma unroll
+          for (int j = 0; j < M; ++j) {
+            if (cl[j]) atomicAdd(&sm.CL[pid][i * M + j], cl[j]);
+            if (cr[j]) atomicAdd(&sm.CR[pid][i * M + j], cr[j]);
+          }
+        }
+      } else if (t < NP * M + K * M) {
+        const int e = t - NP * M, xi = e / M, k = e % M;
+        int sum = 0;
+        if (xi < Kn)
+          for (int w = 0; w < nchunks; ++w) {
+            const unsigned* v = vb + w * (2 * K * M);
+            sum += __popc(v[(2 * xi) * M + k] & v[(2 * xi + 1) * M + k]);
+          }
+        if (sum) atomicAdd(&sm.S[xi][k], sum);
+      }
+      static_assert(RoundSmem<M>::NPAIR * M + (M + 1) * M <= NM_THREADS, "a thread a (pair, i) and an S entry");
+    } else {
+      // one thread an entry of S, CL, CR (in that order, as laid out)
+      constexpr int NSUM = K * M + 2 * NP * MM;
+      for (int e = threadIdx.x; e < NSUM; e += NM_THREADS) {
+        int sum = 0;
+        if (e < K * M) {  // S[x][k] = rows with bit k and popcount N+1 = popc(VL & VE)
+          const int xi = e / M, k = e % M;
+          if (xi < Kn)
+            for (int w = 0; w < nchunks; ++w) {
+              const unsigned* v = vb + w * (2 * K * M);
+              sum += __popc(v[(2 * xi) * M + k] & v[(2 * xi + 1) * M + k]);
+            }
+          if (sum) atomicAdd(&sm.S[xi][k], sum);
+        } else {
+          const int f = e - K * M, side = f / (NP * MM), rem = f % (NP * MM);
+          const int pid = rem / MM, idx = rem % MM, i = idx / M, j = idx % M;
+          int a = 0, q = pid;  // pair (a, c), a < c, of pair_id
+          while (q >= K - 1 - a) {
+            q -= K - 1 - a;
+            ++a;
+          }
+          const int c = a + 1 + q;
+          if (c < Kn)
+            for (int w = 0; w < nchunks; ++w) {
+              const unsigned* v = vb + w * (2 * K * M);
+              sum += side == 0 ? __popc(v[(2 * a + 1) * M + i] & v[(2 * c) * M + j])   // CL: VE[a][i] & VL[c][j]
+                               : __popc(v[(2 * a) * M + i] & v[(2 * c + 1) * M + j]);  // CR: VL[a][i] & VE[c][j]
+            }
+          if (sum) atomicAdd(side == 0 ? &sm.CL[pid][idx] : &sm.CR[pid][idx], sum);
+        }
       }
     }
     if (threadIdx.x == 0 && sl.rank == 0) s_tin[5] += global_ns() - t_g;
@@ -1345,7 +1401,8 @@ __device__ void apply_recount(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl)
   }
   __syncthreads();
   const unsigned long long t_in = (threadIdx.x == 0 && sl.rank == 0) ? global_ns() : 0ull;
-  for_rows_warp<M, 2>(sm, J, [&](int r, const uint4& w, bool valid) {
+  for_rows_warp<M, 2>(sm, J, [&](int r, const uint4& w, bool valid, int chunk) {
+    (void)chunk;
     // the row's groups after the swaps, packed like the record
     unsigned n0 = 0, n1 = 0, n2 = 0;
 #pragma unroll
