@@ -138,12 +138,15 @@ struct Pattern {
   int* csplit = nullptr;  // [16 R + 1] start of each (column, row group) in crow
   int* inv0 = nullptr;
   int* pres0 = nullptr;
+  int* d_err = nullptr;  // [2] on the device: the input check's flag (bit 1 unsorted, bit 2 out of range), np
 };
 size_t pattern_bytes(int R, int nnz);
 // validates (row, col) order and range, then builds P in the arena;
-// h_scratch: at least 2 pinned ints
+// h_scratch: at least 2 pinned ints.  deferred: no host synchronisation;
+// P.np is left -1, the check's flag and np stay in P.d_err[0..1] for the
+// caller to read back, and the kernels skip their work on a flagged input.
 vnm_status build_pattern(vnm_ctx* ctx, int R, int nnz, const int* d_row, const int* d_col, const float* d_val,
-                         int N, int M, Pattern& P, int* h_scratch);
+                         int N, int M, Pattern& P, int* h_scratch, bool deferred = false);
 
 }  // namespace vnm
 

@@ -127,6 +127,7 @@ struct NMJob {
   int trace_cap_rounds;
   int walk_wait_limit;  // polls before a wait of the walk gives up (WALK_WAIT_LIMIT)
   int hold_heaps;       // test only: the swap heaps publish no pop, so a walk that waits runs out
+  const int* err;       // the input check's flag (k_validate): nonzero, the job does nothing; null, no check
 };
 
 // ---------------------------------------------------------------------------
@@ -154,9 +155,12 @@ __global__ void k_nonzero_flags(const float* val, int nnz, int* flags) {
 }
 
 // Keep the entries with nonzero value, in order; count entries per
-// (column, row group).
+// (column, row group).  This kernel and every later one that takes indices
+// as addresses do nothing when k_validate flagged the input (*err != 0): the
+// host reads the flag once, at the end of the call.
 __global__ void k_compact(const int* row, const int* col, const float* val, const int* pos, int nnz, int* prow,
-                          int* pcol, int* gdeg) {
+                          int* pcol, int* gdeg, const int* err) {
+  if (*err) return;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += gridDim.x * blockDim.x) {
     if (val[i] != 0.0f) {
       int p = pos[i];
@@ -175,7 +179,10 @@ __global__ void k_cptr_from_split(const int* csplit, int R, int* cptr) {
 
 // Column lists of the pattern, each grouped by row_group (the order inside
 // a group is whatever the atomics give; nothing depends on it).
-__global__ void k_csc_scatter(const int* prow, const int* pcol, int np, const int* csplit, int* cfill, int* crow) {
+__global__ void k_csc_scatter(const int* prow, const int* pcol, const int* d_np, const int* csplit, int* cfill,
+                              int* crow, const int* err) {
+  if (*err) return;
+  const int np = *d_np;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
     const size_t g = (size_t)ROW_GROUPS * pcol[i] + row_group(prow[i]);
     const int slot = atomicAdd(&cfill[g], 1);
@@ -187,7 +194,10 @@ __global__ void k_csc_scatter(const int* prow, const int* pcol, int np, const in
 // The pattern is sorted by (row, col), so a row's groups are runs of entries
 // with equal col / M; the last entry of each run does the counting.
 template <int M>
-__global__ void k_locate(const int* prow, const int* pcol, int np, int N, int* inv, int* pres) {
+__global__ void k_locate(const int* prow, const int* pcol, const int* d_np, int N, int* inv, int* pres,
+                         const int* err) {
+  if (*err) return;
+  const int np = *d_np;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
     const int r = prow[i], s = pcol[i] / M;
     const bool last = (i + 1 == np) || prow[i + 1] != r || pcol[i + 1] / M != s;
@@ -256,6 +266,7 @@ struct RoundSmem {
   int nswaps;
   int hprog[K * K];  // pops of each ordered pair's heap written to ord so far
   int hstop;         // the walk is done: the heaps may stop
+  uint8_t hsmall[K * K];  // the heap's entries hold the gains themselves ((l + r, r) in 12 + 12 bits)
   int go;           // the leader's decision to run another round (copied to every block)
   int S[K][M];                 // S_x(k): rows with bit k set and popcount == N+1
   int CL[NPAIR][MM];           // per unordered pair (a < b): left-side corrections
@@ -629,29 +640,46 @@ __device__ void gather_phase(RoundSmem<M>& sm, const NMJob& J, Slice sl = Slice{
     // are taken, so a free one is always found.
     const unsigned mask = (unsigned)sm.ts_max - 1u;
     unsigned* tw = reinterpret_cast<unsigned*>(sm.table);
-    for (int e = tid; e < E; e += NM_THREADS) {
-      int lo = 0, hi = KM - 1;  // last q with colpre[q] <= e
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (sm.colpre[mid] <= e) lo = mid;
-        else hi = mid - 1;
-      }
-      const int q = lo, xi = q / M, k = q % M;
-      const int row = J.crow[sm.colstart[q] + (e - sm.colpre[q])];
-      const unsigned key = (unsigned)row + 1u;
-      unsigned h = (key * 2654435761u) >> sm.ts_shift;
-      bool placed = false;
-      for (int probe = 0; probe <= (int)mask; ++probe) {
-        const unsigned cur = atomicCAS(&tw[4 * h + 3], 0u, key);
-        if (cur == 0u || cur == key) {
-          atomicOr(&tw[4 * h + (xi >> 2)], (1u << k) << ((xi & 3) * 8));
-          if (cur == 0u) sm.tlist[atomicAdd(&sm.tcount, 1)] = (int)h;
-          placed = true;
-          break;
+    // TABLE_U entries per thread per step, their row loads in flight together
+    constexpr int TABLE_U = 2;
+    for (int base = tid; base < E; base += NM_THREADS * TABLE_U) {
+      int rows[TABLE_U], qs[TABLE_U];
+#pragma unroll
+      for (int u = 0; u < TABLE_U; ++u) {
+        const int e = base + u * NM_THREADS;
+        rows[u] = -1;
+        qs[u] = 0;
+        if (e < E) {
+          int lo = 0, hi = KM - 1;  // last q with colpre[q] <= e
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (sm.colpre[mid] <= e) lo = mid;
+            else hi = mid - 1;
+          }
+          qs[u] = lo;
+          rows[u] = J.crow[sm.colstart[lo] + (e - sm.colpre[lo])];
         }
-        h = (h + 1u) & mask;
       }
-      if (!placed) atomicOr(sl.cs > 1 ? cg::this_cluster().map_shared_rank(&sm.status, 0) : &sm.status, JOB_TABLE_FULL);
+#pragma unroll
+      for (int u = 0; u < TABLE_U; ++u) {
+        if (rows[u] < 0) continue;
+        const int xi = qs[u] / M, k = qs[u] % M;
+        const unsigned key = (unsigned)rows[u] + 1u;
+        unsigned h = (key * 2654435761u) >> sm.ts_shift;
+        bool placed = false;
+        for (int probe = 0; probe <= (int)mask; ++probe) {
+          const unsigned cur = atomicCAS(&tw[4 * h + 3], 0u, key);
+          if (cur == 0u || cur == key) {
+            atomicOr(&tw[4 * h + (xi >> 2)], (1u << k) << ((xi & 3) * 8));
+            if (cur == 0u) sm.tlist[atomicAdd(&sm.tcount, 1)] = (int)h;
+            placed = true;
+            break;
+          }
+          h = (h + 1u) & mask;
+        }
+        if (!placed)
+          atomicOr(sl.cs > 1 ? cg::this_cluster().map_shared_rank(&sm.status, 0) : &sm.status, JOB_TABLE_FULL);
+      }
     }
     __syncthreads();
     if (tid == 0) sm.ntouched = sm.tcount;
@@ -1057,7 +1085,9 @@ __device__ void rank_phase(RoundSmem<M>& sm) {
         small = small && lr[q] >= -2047 && lr[q] <= 2047 && r >= -2047 && r <= 2047;
       }
     }
-    if (__all_sync(FULL, small)) {
+    const bool all_small = __all_sync(FULL, small);
+    if (lane == 0) sm.hsmall[c] = all_small ? 1 : 0;
+    if (all_small) {
       // the key itself, (l + r, r) in 12 + 12 bits, orders like swap_key
 #pragma unroll
       for (int q = 0; q < SL; ++q)
@@ -1275,21 +1305,30 @@ __device__ void walk_phase(RoundSmem<M>& sm, int sched, int wait_limit) {
       const unsigned ml = __reduce_max_sync(FULL, lh == mh ? ll : 0u);
       const int pxi = __ffs(__ballot_sync(FULL, inW && lh == mh && ll == ml)) - 1;
       int pc = __shfl_sync(FULL, cnt, pxi);
+      unsigned vp = __shfl_sync(FULL, vis, pxi);  // the primary's visited bits, on every lane
+      const int sp = __shfl_sync(FULL, seg, pxi);
       // targets: the rest of the list, by position in traversal order
       const unsigned Tm = Wm & ~(1u << pxi);
       const bool isT = (Tm >> lane) & 1u;
       const unsigned th = isT ? order_key_hi(cnt, trav_rev) : 0u, tl = isT ? order_key_lo(seg, trav_rev) : 0u;
       int pos = 0;
-      for (int q = 0; q < Kn; ++q) {
+#pragma unroll
+      for (int q = 0; q < K; ++q) {
         const unsigned qh = __shfl_sync(FULL, th, q), ql = __shfl_sync(FULL, tl, q);
         pos += (((Tm >> q) & 1u) && (qh > th || (qh == th && ql > tl))) ? 1 : 0;
+      }
+      // lane x: the lane of the x-th target
+      int tx = 0;
+#pragma unroll
+      for (int q = 0; q < K; ++q) {
+        const int pq = __shfl_sync(FULL, pos, q);
+        if (((Tm >> q) & 1u) && pq == lane) tx = q;
       }
       const int nT = __popc(Tm);
       unsigned Um = 0;
       for (int x = 0; x < nT; ++x) {
-        const unsigned vp = __shfl_sync(FULL, vis, pxi);
         if (pc <= 0 || vp == FULLM) break;
-        const int txi = __ffs(__ballot_sync(FULL, isT && pos == x)) - 1;
+        const int txi = __shfl_sync(FULL, tx, x);
         const unsigned vt = __shfl_sync(FULL, vis, txi);
         int tc = __shfl_sync(FULL, cnt, txi);
         // First pop of the pair whose two nodes are both unvisited.  A heap
@@ -1300,15 +1339,17 @@ __device__ void walk_phase(RoundSmem<M>& sm, int sched, int wait_limit) {
         const int col = pxi * K + txi;
         const uint8_t* ord = ord0 + col;
         int pick = -1, seen = 0;
+        unsigned pe = ~0u;  // the pick's entry word, when read off the entries
         {
+          unsigned eo[U];  // this lane's entries: entry k holds swap k
           unsigned kq[U];  // key + 1 of this lane's qualifying swaps, else 0
           unsigned best = 0;
 #pragma unroll
           for (int u = 0; u < U; ++u) {
             const int k = lane + 32 * u;
             const unsigned e = k < MM ? ent[k * HS + col] : 0u;
-            const int idx = (int)(e & 255u);
-            const bool ok = k < MM && !((vp >> (idx / M)) & 1u) && !((vt >> (idx % M)) & 1u);
+            eo[u] = e;
+            const bool ok = k < MM && !((vp >> (k / M)) & 1u) && !((vt >> (k % M)) & 1u);
             kq[u] = ok ? (e >> 8) + 1u : 0u;
             best = max(best, __reduce_max_sync(FULL, kq[u]));
           }
@@ -1319,7 +1360,14 @@ __device__ void walk_phase(RoundSmem<M>& sm, int sched, int wait_limit) {
             nbest += __popc(bb);
             if (bb && who < 0) who = 32 * u + __ffs(bb) - 1;
           }
-          if (nbest == 1) pick = who;  // swap index == entry position
+          if (nbest == 1) {  // swap index == entry position
+            pick = who;
+            unsigned ep = eo[0];
+#pragma unroll
+            for (int u = 1; u < U; ++u)
+              if ((pick >> 5) == u) ep = eo[u];
+            pe = __shfl_sync(FULL, ep, pick & 31);
+          }
         }
         while (pick < 0 && !dead) {
           if (seen >= MM) {  // unreachable: a scored target always has an unvisited node
@@ -1343,15 +1391,30 @@ __device__ void walk_phase(RoundSmem<M>& sm, int sched, int wait_limit) {
         }
         if (dead) pick = 0;
         int l, r;
-        pair_gains<M>(sm, pxi, txi, pick, l, r);
-        commit(pxi, txi, pick);
-        if (lane == pxi) vis |= 1u << (pick / M);
-        if (lane == txi) vis |= 1u << (pick % M);
+        if (sm.hsmall[col]) {  // the gains are the pick's key: (l + r + 2048) << 12 | (r + 2048)
+          if (pe == ~0u || dead) pe = ent[pick * HS + col];  // picked from the pops
+          const unsigned key = pe >> 8;
+          r = (int)(key & 4095u) - 2048;
+          l = (int)(key >> 12) - 2048 - r;
+        } else {
+          pair_gains<M>(sm, pxi, txi, pick, l, r);
+        }
+        const int i = pick / M, j = pick % M;
+        if (lane == 0) {
+          sm.swaps[2 * nsw] = sp * M + i;
+          sm.swaps[2 * nsw + 1] = sm.xseg[txi] * M + j;
+          sm.dest[pxi][i] = (uint8_t)((txi << 4) | j);
+          sm.dest[txi][j] = (uint8_t)((pxi << 4) | i);
+        }
+        ++nsw;
+        vp |= 1u << i;
+        if (lane == txi) vis |= 1u << j;
         pc -= l;
         tc -= r;
         if (lane == txi) cnt = tc;
         if (tc > 0) Um |= 1u << txi;
       }
+      if (lane == pxi) vis = vp;
       Wm = Um;
     }
   }
@@ -1497,6 +1560,7 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
   __shared__ unsigned long long g_start;  // the kernel's start (thread 0 of the leader), global timer
   if (threadIdx.x == 0) g_start = global_ns();
   const NMJob J = jobs[blockIdx.x / cs];
+  if (J.err && *J.err) return;  // every block of the cluster reads the same flag, before any barrier
   const int tid = threadIdx.x;
   int* cnt = cnt_in_smem ? smem_cnt : J.cnt;
   if (lead && cnt_in_smem)
@@ -1736,7 +1800,7 @@ static inline int grid_for(const vnm_ctx* ctx, long long n, int nt = 256) {
 
 size_t pattern_bytes(int R, int nnz) {
   size_t b = 0;
-  b += arena_bytes(1, sizeof(int));              // error word
+  b += arena_bytes(2, sizeof(int));              // the input check's flag and the entry count
   b += arena_bytes(nnz, sizeof(int));            // flags / positions
   b += 2 * arena_bytes(nnz, sizeof(int));        // prow, pcol
   const size_t ng = (size_t)ROW_GROUPS * R + 1;
@@ -1751,10 +1815,10 @@ size_t pattern_bytes(int R, int nnz) {
 
 template <int M>
 static vnm_status build_pattern_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, const int* d_col,
-                                  const float* d_val, int N, Pattern& P, int* h_scratch) {
+                                  const float* d_val, int N, Pattern& P, int* h_scratch, bool deferred) {
   P.R = R;
   P.nseg = R / M;
-  int* err = arena_take<int>(ctx, 1);
+  int* err = arena_take<int>(ctx, 2);  // [0] the input check's flag, [1] the pattern's entry count
   int* pos = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
   P.prow = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
   P.pcol = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
@@ -1765,52 +1829,67 @@ static vnm_status build_pattern_t(vnm_ctx* ctx, int R, int nnz, const int* d_row
   P.crow = arena_take<int>(ctx, nnz > 0 ? nnz : 1);
   P.inv0 = arena_take<int>(ctx, R / 2 + 1);
   P.pres0 = arena_take<int>(ctx, R / 2 + 1);
-  int* d_np = arena_take<int>(ctx, 1);
   int* d_tot = arena_take<int>(ctx, 1);
   if (!err || !pos || !P.prow || !P.pcol || !P.cptr || !P.csplit || !cfill || !P.crow || !P.inv0 || !P.pres0 ||
-      !d_np || !d_tot)
+      !d_tot)
     return VNM_ERR_NOMEM;
-  VNM_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  int* d_np = err + 1;
+  P.d_err = err;
+  VNM_CUDA_TRY(cudaMemsetAsync(err, 0, 2 * sizeof(int), ctx->stream));
   VNM_CUDA_TRY(cudaMemsetAsync(P.csplit, 0, sizeof(int) * ng, ctx->stream));
   VNM_CUDA_TRY(cudaMemsetAsync(cfill, 0, sizeof(int) * ng, ctx->stream));
   VNM_CUDA_TRY(cudaMemsetAsync(P.inv0, 0, sizeof(int) * (P.nseg + 1), ctx->stream));
   VNM_CUDA_TRY(cudaMemsetAsync(P.pres0, 0, sizeof(int) * (P.nseg + 1), ctx->stream));
   if (nnz > 0) {
-    // indices are checked before any kernel uses them as addresses
+    // indices are checked before any kernel uses them as addresses: here,
+    // or (deferred) by the kernels themselves, which skip their work when
+    // the flag is set
     VNM_LAUNCH(ctx, k_validate, grid_for(ctx, nnz), 256, 0, d_row, d_col, nnz, R, err);
-    VNM_CUDA_TRY(cudaMemcpyAsync(h_scratch, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    VNM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-    if (h_scratch[0] & 2) return VNM_ERR_RANGE;
-    if (h_scratch[0] & 1) return VNM_ERR_UNSORTED;
+    if (!deferred) {
+      VNM_CUDA_TRY(cudaMemcpyAsync(h_scratch, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      VNM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+      if (h_scratch[0] & 2) return VNM_ERR_RANGE;
+      if (h_scratch[0] & 1) return VNM_ERR_UNSORTED;
+    }
     VNM_LAUNCH(ctx, k_nonzero_flags, grid_for(ctx, nnz), 256, 0, d_val, nnz, pos);
     VNM_TRY(exclusive_scan(ctx, pos, pos, nnz, d_np));
     VNM_LAUNCH(ctx, k_compact, grid_for(ctx, nnz), 256, 0, d_row, d_col, d_val, pos, nnz, P.prow, P.pcol,
-               P.csplit);
-  } else {
-    VNM_CUDA_TRY(cudaMemsetAsync(d_np, 0, sizeof(int), ctx->stream));
+               P.csplit, err);
   }
   VNM_TRY(exclusive_scan(ctx, P.csplit, P.csplit, (int)ng, d_tot));
   VNM_LAUNCH(ctx, k_cptr_from_split, grid_for(ctx, (long long)R + 1), 256, 0, P.csplit, R, P.cptr);
+  if (deferred) {
+    // the entry count stays on the device (read back with the call's
+    // results); the grids cover every stored entry
+    P.np = -1;
+    if (nnz > 0) {
+      VNM_LAUNCH(ctx, k_csc_scatter, grid_for(ctx, nnz), 256, 0, P.prow, P.pcol, d_np, P.csplit, cfill, P.crow,
+                 err);
+      VNM_LAUNCH(ctx, k_locate<M>, grid_for(ctx, nnz), 256, 0, P.prow, P.pcol, d_np, N, P.inv0, P.pres0, err);
+    }
+    return VNM_OK;
+  }
   VNM_CUDA_TRY(cudaMemcpyAsync(h_scratch + 1, d_np, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   VNM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   P.np = h_scratch[1];
   if (P.np > 0) {
-    VNM_LAUNCH(ctx, k_csc_scatter, grid_for(ctx, P.np), 256, 0, P.prow, P.pcol, P.np, P.csplit, cfill, P.crow);
-    VNM_LAUNCH(ctx, k_locate<M>, grid_for(ctx, P.np), 256, 0, P.prow, P.pcol, P.np, N, P.inv0, P.pres0);
+    VNM_LAUNCH(ctx, k_csc_scatter, grid_for(ctx, P.np), 256, 0, P.prow, P.pcol, d_np, P.csplit, cfill, P.crow,
+               err);
+    VNM_LAUNCH(ctx, k_locate<M>, grid_for(ctx, P.np), 256, 0, P.prow, P.pcol, d_np, N, P.inv0, P.pres0, err);
   }
   return VNM_OK;
 }
 
 vnm_status build_pattern(vnm_ctx* ctx, int R, int nnz, const int* d_row, const int* d_col, const float* d_val,
-                         int N, int M, Pattern& P, int* h_scratch) {
+                         int N, int M, Pattern& P, int* h_scratch, bool deferred) {
   switch (M) {
-    case 2: return build_pattern_t<2>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch);
-    case 3: return build_pattern_t<3>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch);
-    case 4: return build_pattern_t<4>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch);
-    case 5: return build_pattern_t<5>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch);
-    case 6: return build_pattern_t<6>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch);
-    case 7: return build_pattern_t<7>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch);
-    case 8: return build_pattern_t<8>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch);
+    case 2: return build_pattern_t<2>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch, deferred);
+    case 3: return build_pattern_t<3>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch, deferred);
+    case 4: return build_pattern_t<4>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch, deferred);
+    case 5: return build_pattern_t<5>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch, deferred);
+    case 6: return build_pattern_t<6>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch, deferred);
+    case 7: return build_pattern_t<7>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch, deferred);
+    case 8: return build_pattern_t<8>(ctx, R, nnz, d_row, d_col, d_val, N, P, h_scratch, deferred);
   }
   return VNM_ERR_ARG;
 }
@@ -1846,6 +1925,7 @@ static vnm_status make_job(vnm_ctx* ctx, const Pattern& P, int sched, int maxite
   // from publishing, so the first wait runs out.  Unset, they change nothing.
   J.walk_wait_limit = WALK_WAIT_LIMIT;
   J.hold_heaps = 0;
+  J.err = nullptr;
   if (const char* e = getenv("VNM_NM_TEST_WAIT_LIMIT")) {
     const int v = atoi(e);
     if (v > 0 && v < WALK_WAIT_LIMIT) J.walk_wait_limit = v;
@@ -1996,7 +2076,7 @@ static vnm_status check_nm_args(int nrows, int nnz, const int* row, const int* c
 // find_best_2toX's choice (main.cu:80-113) from the four result vectors:
 // largest improve rate, ties to the lower schedule id; 0 when the matrix is
 // empty or has no invalid segment (main.cu:85).
-static int pick_best(const int* res, int nsched, int nnz) {
+__host__ __device__ static int pick_best(const int* res, int nsched, int nnz) {
   float max_imprv = 0.0f;
   int best = 0;
   for (int s = 0; s < nsched; ++s) {
@@ -2011,6 +2091,32 @@ static int pick_best(const int* res, int nsched, int nnz) {
   return best;
 }
 
+// newpos[orig[p]] = p for job `job`, or (job < 0) for the find_best_2toX
+// winner of the jobs' results, chosen on the device as pick_best does on
+// the host; the choice goes to *picked.
+__global__ void k_pick_invert(const NMJob* jobs, int njobs, int nnz, int job, int R, int* newpos, int* picked) {
+  __shared__ int s_job;
+  if (threadIdx.x == 0) {
+    if (job < 0) {
+      int r5[20];
+      for (int s = 0; s < njobs && s < 4; ++s)
+        for (int q = 0; q < 5; ++q) r5[5 * s + q] = jobs[s].res[q];
+      job = pick_best(r5, njobs < 4 ? njobs : 4, nnz);
+    }
+    s_job = job;
+    if (blockIdx.x == 0) *picked = job;
+  }
+  __syncthreads();
+  const int* orig = jobs[s_job].orig;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x) newpos[orig[i]] = i;
+}
+
+// Pinned host words of run_matrix: the jobs' results, then the input
+// check's flag, the pattern's entry count and the device's pick, then the
+// job records on their way to the device.
+constexpr int PIN_FLAGS = 4 * JOB_RES, PIN_JOBS = 256;
+static_assert(4 * sizeof(NMJob) <= 256 * sizeof(int), "four job records fit the pinned words after PIN_JOBS");
+
 // Run `nsched` jobs on one matrix (schedules sched0 .. sched0+nsched-1).
 // newpos_job >= 0 selects the job whose permutation goes to newpos_out;
 // -1 selects the find_best_2toX winner (reported in *picked).
@@ -2024,17 +2130,24 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
                 arena_bytes(R, sizeof(int)) + 3 * arena_bytes(nnz, sizeof(int)) +
                 arena_bytes(trace_pairs_cap * 2, sizeof(int)) + arena_bytes(trace_rounds_cap, sizeof(int)) + 4096;
   VNM_TRY(arena_reserve(ctx, need));
-  VNM_TRY(pinned_reserve(ctx, 256 + (size_t)trace_pairs_cap * 2 + trace_rounds_cap));
+  VNM_TRY(pinned_reserve(ctx, 512 + (size_t)trace_pairs_cap * 2 + trace_rounds_cap));
+  if (nsched < 1 || nsched > 4) return VNM_ERR_ARG;
   VNM_TRY(begin_call(ctx));
   const int *d_row, *d_col;
   const float* d_val;
   VNM_TRY(stage_in(ctx, row, nnz, mem, &d_row));
   VNM_TRY(stage_in(ctx, col, nnz, mem, &d_col));
   VNM_TRY(stage_in(ctx, val, nnz, mem, &d_val));
+  // No host synchronisation until the end of the call: the input check's
+  // flag and the pattern's entry count come back with the results (a
+  // flagged input makes every kernel after the check skip its work).
   Pattern P;
-  VNM_TRY(build_pattern(ctx, R, nnz, d_row, d_col, d_val, N, M, P, ctx->h_pinned));
+  VNM_TRY(build_pattern(ctx, R, nnz, d_row, d_col, d_val, N, M, P, ctx->h_pinned, true));
   NMJob hj[4];
-  for (int s = 0; s < nsched; ++s) VNM_TRY(make_job(ctx, P, sched0 + s, maxiter, hj[s]));
+  for (int s = 0; s < nsched; ++s) {
+    VNM_TRY(make_job(ctx, P, sched0 + s, maxiter, hj[s]));
+    hj[s].err = P.d_err;
+  }
   int* d_tp = nullptr;
   int* d_tr = nullptr;
   if (trace) {
@@ -2047,19 +2160,38 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
     hj[0].trace_cap_rounds = trace_rounds_cap;
   }
   NMJob* d_jobs = arena_take<NMJob>(ctx, nsched);
-  if (!d_jobs) return VNM_ERR_NOMEM;
-  VNM_CUDA_TRY(cudaMemcpyAsync(d_jobs, hj, sizeof(NMJob) * nsched, cudaMemcpyHostToDevice, ctx->stream));
+  int* d_newpos = newpos_out && R > 0 ? arena_take<int>(ctx, R) : nullptr;
+  if (!d_jobs || (newpos_out && R > 0 && !d_newpos)) return VNM_ERR_NOMEM;
+  // the job records go through pinned memory, so that the copy is queued
+  // behind the pattern build instead of waiting for it
+  NMJob* pj = reinterpret_cast<NMJob*>(ctx->h_pinned + PIN_JOBS);
+  memcpy(pj, hj, sizeof(NMJob) * nsched);
+  VNM_CUDA_TRY(cudaMemcpyAsync(d_jobs, pj, sizeof(NMJob) * nsched, cudaMemcpyHostToDevice, ctx->stream));
   VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main0, ctx->stream));
-  VNM_TRY(launch_rounds(ctx, d_jobs, nsched, N, M, P.nseg, nm_cluster_size(P.np)));
+  // the stored entries stand in for the pattern's (nonzero-valued) entries
+  // when sizing the clusters: their count is known without a readback
+  VNM_TRY(launch_rounds(ctx, d_jobs, nsched, N, M, P.nseg, nm_cluster_size(nnz)));
   VNM_CUDA_TRY(cudaEventRecord(ctx->ev_main1, ctx->stream));
-  int* hres = ctx->h_pinned;
+  int* hp = ctx->h_pinned;
   for (int s = 0; s < nsched; ++s)
-    VNM_CUDA_TRY(cudaMemcpyAsync(hres + JOB_RES * s, hj[s].res, sizeof(int) * JOB_RES, cudaMemcpyDeviceToHost,
+    VNM_CUDA_TRY(cudaMemcpyAsync(hp + JOB_RES * s, hj[s].res, sizeof(int) * JOB_RES, cudaMemcpyDeviceToHost,
                                  ctx->stream));
-  VNM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  VNM_CUDA_TRY(cudaMemcpyAsync(hp + PIN_FLAGS, P.d_err, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  if (d_newpos) {
+    VNM_LAUNCH(ctx, k_pick_invert, grid_for(ctx, R), 256, 0, d_jobs, nsched, nnz, newpos_job, R, d_newpos,
+               P.d_err + 1);  // the entry count was read back above: its word now takes the pick
+    VNM_CUDA_TRY(cudaMemcpyAsync(hp + PIN_FLAGS + 2, P.d_err + 1, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    VNM_CUDA_TRY(cudaMemcpyAsync(newpos_out, d_newpos, sizeof(int) * R, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  VNM_TRY(end_call(ctx));
   VNM_CUDA_TRY(cudaEventElapsedTime(&ctx->main_ms, ctx->ev_main0, ctx->ev_main1));
+  const int flag = hp[PIN_FLAGS];
+  if (flag & 2) return VNM_ERR_RANGE;
+  if (flag & 1) return VNM_ERR_UNSORTED;
+  P.np = nnz > 0 ? hp[PIN_FLAGS + 1] : 0;
+  const int dev_pick = hp[PIN_FLAGS + 2];
   int hres_copy[4 * JOB_RES];
-  memcpy(hres_copy, hres, sizeof(int) * JOB_RES * nsched);
+  memcpy(hres_copy, hp, sizeof(int) * JOB_RES * nsched);
   for (int q = 0; q < 28; ++q) ctx->stats[q] = 0;
   ctx->stats[3] = P.nseg;
   ctx->stats[4] = nsched;
@@ -2092,28 +2224,26 @@ static vnm_status run_matrix(vnm_ctx* ctx, int nrows, int nnz, const int* row, c
     ctx->stats[21] += h[25];
     for (int q = 0; q < 6; ++q) ctx->stats[22 + q] += h[26 + q];
   }
+  const int pick = newpos_job >= 0 ? newpos_job : pick_best(res5_out, nsched, nnz);
+  if (picked) *picked = pick;
+  if (d_newpos && dev_pick != pick) {  // the device chose from the same integers with the same arithmetic
+    VNM_LAUNCH(ctx, k_invert, grid_for(ctx, R), 256, 0, hj[pick].orig, R, d_newpos);
+    VNM_CUDA_TRY(cudaMemcpyAsync(newpos_out, d_newpos, sizeof(int) * R, cudaMemcpyDeviceToHost, ctx->stream));
+    VNM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  }
   if (trace) {
     const int committed = hres_copy[6];
     const int rounds = hres_copy[4];
     const int np = committed < trace_pairs_cap ? committed : trace_pairs_cap;
     const int nr = rounds < trace_rounds_cap ? rounds : trace_rounds_cap;
-    int* hp = ctx->h_pinned + 128;  // after the per-job results (24 ints each)
-    if (np) VNM_CUDA_TRY(cudaMemcpyAsync(hp, d_tp, sizeof(int) * 2 * np, cudaMemcpyDeviceToHost, ctx->stream));
+    int* ht = ctx->h_pinned + 128;  // over the per-job results, which were copied out above
+    if (np) VNM_CUDA_TRY(cudaMemcpyAsync(ht, d_tp, sizeof(int) * 2 * np, cudaMemcpyDeviceToHost, ctx->stream));
     if (nr)
-      VNM_CUDA_TRY(cudaMemcpyAsync(hp + 2 * np, d_tr, sizeof(int) * nr, cudaMemcpyDeviceToHost, ctx->stream));
+      VNM_CUDA_TRY(cudaMemcpyAsync(ht + 2 * np, d_tr, sizeof(int) * nr, cudaMemcpyDeviceToHost, ctx->stream));
     VNM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-    ctx->trace_pairs.assign(hp, hp + 2 * np);
-    ctx->trace_round_end.assign(hp + 2 * np, hp + 2 * np + nr);
+    ctx->trace_pairs.assign(ht, ht + 2 * np);
+    ctx->trace_round_end.assign(ht + 2 * np, ht + 2 * np + nr);
   }
-  if (newpos_job < 0) newpos_job = pick_best(res5_out, nsched, nnz);
-  if (picked) *picked = newpos_job;
-  if (newpos_out && R > 0) {
-    int* d_np = arena_take<int>(ctx, R);
-    if (!d_np) return VNM_ERR_NOMEM;
-    VNM_LAUNCH(ctx, k_invert, grid_for(ctx, R), 256, 0, hj[newpos_job].orig, R, d_np);
-    VNM_CUDA_TRY(cudaMemcpyAsync(newpos_out, d_np, sizeof(int) * R, cudaMemcpyDeviceToHost, ctx->stream));
-  }
-  VNM_TRY(end_call(ctx));
   return VNM_OK;
 }
 
@@ -2259,6 +2389,7 @@ static vnm_status run_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int6
     J.trace_cap_rounds = 0;
     J.walk_wait_limit = WALK_WAIT_LIMIT;
     J.hold_heaps = 0;
+    J.err = nullptr;
     if (J.nseg > max_nseg) max_nseg = J.nseg;
   }
   VNM_CUDA_TRY(cudaMemcpyAsync(d_jobs, hj.data(), sizeof(NMJob) * nmat, cudaMemcpyHostToDevice, ctx->stream));

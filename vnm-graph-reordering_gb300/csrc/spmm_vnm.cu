@@ -213,9 +213,10 @@ __device__ __forceinline__ unsigned low2(unsigned m) {  // the lowest two set bi
 // Count slices per block and per tile.  A block with fewer than dense_min
 // nonzeros gets no slice: its entries are flagged for the residual (by
 // original position), counted per row and per tile.
-__global__ void k_cmp_count(const unsigned long long* skeys, const int* spos, const int* gstart, int ngroups, int nnz,
-                            int M, int V, int nseg, int dense_min, int* gsl, int* tile_raw, int* valid_blocks,
+__global__ void k_cmp_count(const unsigned long long* skeys, const int* spos, const int* gstart, const int* d_ngroups,
+                            int nnz, int M, int V, int nseg, int dense_min, int* gsl, int* tile_raw, int* valid_blocks,
                             int* resflag, int* rowlen, int* tile_res) {
+  const int ngroups = *d_ngroups;
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += gridDim.x * blockDim.x) {
     const int b0 = gstart[g], b1 = g + 1 < ngroups ? gstart[g + 1] : nnz;
     const long long blk = (long long)(skeys[b0] / ((unsigned long long)V * M));
@@ -858,10 +859,13 @@ static vnm_status compress_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, con
   VNM_CUDA_TRY(cudaMemsetAsync(resflag, 0, sizeof(int) * n1, st));
   VNM_CUDA_TRY(cudaMemsetAsync(bmax, 0, sizeof(unsigned) * (nbrow + 1), st));
   VNM_CUDA_TRY(cudaMemsetAsync(counters, 0, sizeof(int) * 16, st));
-  int ngroups = 0;
   unsigned long long* skeys = keys;
   int* spos = nullptr;
   if (nnz > 0) {
+    // the group count stays on the device until the storage is sized: the
+    // counting grid covers every entry, and the scan of the slices per group
+    // runs over nnz words, zero past the last group
+    VNM_CUDA_TRY(cudaMemsetAsync(gsl, 0, sizeof(int) * n1, st));
     VNM_LAUNCH(ctx, k_cmp_keys, sp_grid(ctx, nnz), 256, 0, d_row, d_col, nnz, M, V, nseg, keys);
     const long long maxkey = ((long long)nbrow * nseg) * V * M;
     VNM_TRY(radix_sort_u64(ctx, keys, nullptr, nnz, sp_bits(maxkey), &skeys, &spos));
@@ -870,14 +874,9 @@ static vnm_status compress_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, con
     VNM_LAUNCH(ctx, k_cmp_group_start, sp_grid(ctx, nnz), 256, 0, flag, skeys, nnz, V * M, gstart);
     VNM_LAUNCH(ctx, k_cmp_scale, sp_grid(ctx, (nnz + SCALE_RUN - 1) / SCALE_RUN), 256, 0, skeys, spos, d_val, nnz,
                V * M, nseg, bmax);
-    VNM_CUDA_TRY(cudaMemcpyAsync(h, counters, sizeof(int), cudaMemcpyDeviceToHost, st));
-    VNM_CUDA_TRY(cudaStreamSynchronize(st));
-    ngroups = h[0];
-  }
-  if (ngroups > 0) {
-    VNM_LAUNCH(ctx, k_cmp_count, sp_grid(ctx, ngroups, 128), 128, 0, skeys, spos, gstart, ngroups, nnz, M, V, nseg,
+    VNM_LAUNCH(ctx, k_cmp_count, sp_grid(ctx, nnz, 128), 128, 0, skeys, spos, gstart, counters, nnz, M, V, nseg,
                dense_min, gsl, tile_raw, counters + 1, resflag, rowlen, tile_res);
-    VNM_TRY(exclusive_scan(ctx, gsl, gofs, ngroups, counters + 2));
+    VNM_TRY(exclusive_scan(ctx, gsl, gofs, nnz, counters + 2));
   }
   VNM_LAUNCH(ctx, k_cmp_pad, sp_grid(ctx, ntiles), 256, 0, tile_raw, ntiles, tile_pad, tile_has);
   VNM_TRY(exclusive_scan(ctx, tile_pad, tile_base, ntiles + 1, nullptr));
@@ -890,17 +889,18 @@ static vnm_status compress_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, con
   VNM_TRY(exclusive_scan(ctx, nst, st_off, R, counters + 6));
   VNM_TRY(exclusive_scan(ctx, nmr, mr_off, R, counters + 7));
   VNM_CUDA_TRY(cudaMemcpyAsync(h, tile_base + ntiles, sizeof(int), cudaMemcpyDeviceToHost, st));
-  VNM_CUDA_TRY(cudaMemcpyAsync(h + 1, counters + 1, 7 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  VNM_CUDA_TRY(cudaMemcpyAsync(h + 1, counters, 8 * sizeof(int), cudaMemcpyDeviceToHost, st));
   VNM_CUDA_TRY(cudaStreamSynchronize(st));
   const int padded = h[0];
-  out->valid_blocks = h[1];
-  out->slices = ngroups > 0 ? h[2] : 0;
-  out->ntt = h[3];
-  out->nres = h[4];
-  const int nmt_total = h[5], nst_total = h[6];
+  const int ngroups = nnz > 0 ? h[1] : 0;
+  out->valid_blocks = h[2];
+  out->slices = ngroups > 0 ? h[3] : 0;
+  out->ntt = h[4];
+  out->nres = h[5];
+  const int nmt_total = h[6], nst_total = h[7];
   out->nslots = nmt_total;
   out->ntask = nmt_total + nst_total;
-  out->nmulti = h[7];
+  out->nmulti = h[8];
   out->dense_min = dense_min;
   out->slices_padded = padded;
   out->groups = ngroups;
