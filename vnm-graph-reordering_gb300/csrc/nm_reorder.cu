@@ -291,6 +291,8 @@ struct RoundSmem {
   int newinv[K], newpres[K];
   int swaps[2 * K * M];        // committed swaps (positions)
   unsigned long long wtop[2][NW][K];
+  unsigned long long sel_top[15][2][K];  // leader: each helper's scan (top K both orders) ...
+  int sel_ls[15][2];                     // ... and its list size and total, pushed by the helper
   unsigned long long top[2][K];  // [0] Ldesc order (cnt desc, seg asc), [1] reverse
   unsigned long long red64[NW];
   int red32[2][NW];
@@ -335,15 +337,16 @@ __device__ __forceinline__ void topk_insert(unsigned long long (&a)[K], unsigned
   }
 }
 
-// merge the 32 lanes' sorted lists; lane 0 gets the warp's top K in out[]
-template <int K>
+// merge the sorted lists of lanes 0 .. W-1 (W a power of two; the other
+// lanes hold their own); lane 0 gets their top K in out[]
+template <int K, int W = 32>
 __device__ __forceinline__ void topk_warp_merge(unsigned long long (&a)[K], unsigned long long* out) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int q = 0; q < K; ++q) {
     unsigned long long h = a[0], m = h;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
+    for (int o = W / 2; o > 0; o >>= 1) {
       unsigned long long t = __shfl_xor_sync(FULL, m, o);
       m = t > m ? t : m;
     }
@@ -425,32 +428,30 @@ __device__ void select_phase(RoundSmem<M>& sm, const NMJob& J, const int* cnt) {
 
 // The same result as select_phase after a round, from the other blocks'
 // scans of all segments but this round's (made while the leader ran the
-// heaps and the walk; those counts did not change) and this round's
-// segments with their new counts (leader block of a cluster).
+// heaps and the walk; those counts did not change; each helper pushed its
+// result into sel_top / sel_ls) and this round's segments with their new
+// counts (leader block of a cluster).  Lane l holds helper l + 1's list:
+// at most 15 helpers and 9 round segments, so the lists sit in lanes 0-15.
 template <int M>
 __device__ void select_merge(RoundSmem<M>& sm, cg::cluster_group& cl, int cs, const int* cnt) {
   constexpr int K = M + 1;
+  static_assert(K <= 16, "the round's segments fit lanes 0-15");
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  (void)cl;
   if (w < 2) {  // warp 0 the descending lists, warp 1 the reverse ones
-    unsigned long long a[K];
+    unsigned long long a[K];  // a helper's list is sorted already
 #pragma unroll
-    for (int q = 0; q < K; ++q) a[q] = 0;
-    if (lane + 1 < cs) {
-      const RoundSmem<M>* rs = cl.map_shared_rank(&sm, lane + 1);
-#pragma unroll
-      for (int q = 0; q < K; ++q) topk_insert<K>(a, rs->top[w][q]);
-    }
+    for (int q = 0; q < K; ++q) a[q] = lane + 1 < cs ? sm.sel_top[lane][w][q] : 0ull;
     if (lane < sm.K_) {
       const int sg = sm.xseg[lane], c = cnt[sg];
       if (c > 0) topk_insert<K>(a, w == 0 ? desc_key(c, sg) : rev_key(c, sg));
     }
-    topk_warp_merge<K>(a, sm.top[w]);
+    topk_warp_merge<K, 16>(a, sm.top[w]);
   } else if (w == 2) {
     int v0 = 0, v1 = 0;
     if (lane + 1 < cs) {
-      const RoundSmem<M>* rs = cl.map_shared_rank(&sm, lane + 1);
-      v0 = rs->lsize;
-      v1 = rs->ltotal;
+      v0 = sm.sel_ls[lane][0];
+      v1 = sm.sel_ls[lane][1];
     }
     if (lane < sm.K_) {
       const int c = cnt[sm.xseg[lane]];
@@ -460,7 +461,7 @@ __device__ void select_merge(RoundSmem<M>& sm, cg::cluster_group& cl, int cs, co
       }
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
+    for (int o = 8; o > 0; o >>= 1) {  // lanes 0-15
       v0 += __shfl_xor_sync(FULL, v0, o);
       v1 += __shfl_xor_sync(FULL, v1, o);
     }
@@ -1664,6 +1665,11 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
         const int nh = cs - 1, hr = rank - 1;
         const int sb = (int)((long long)J.nseg * hr / nh), se = (int)((long long)J.nseg * (hr + 1) / nh);
         select_range<M>(sm, cnt_in_smem ? cl.map_shared_rank(smem_cnt, 0) : J.cnt, sb, se, sm.xseg, sm.K_);
+        // the scan's result into the leader's shared memory, read there
+        // after the barrier that follows the walk
+        RoundSmem<M>* ls = cl.map_shared_rank(&sm, 0);
+        if (tid < 2 * K) ls->sel_top[hr][tid / K][tid % K] = sm.top[tid / K][tid % K];
+        else if (tid < 2 * K + 2) ls->sel_ls[hr][tid - 2 * K] = tid == 2 * K ? sm.lsize : sm.ltotal;
       }
     }
     VNM_PHASE(3);
