@@ -520,51 +520,64 @@ __device__ __forceinline__ bool before_rev(int sa, int ca, int sb, int cb) {
 template <int M>
 __device__ void choose_segments(RoundSmem<M>& sm, int sched) {
   constexpr int K = M + 1;
-  if (threadIdx.x != 0) return;
+  if (threadIdx.x >= 32) return;  // warp 0; lane q handles list entry q
+  const int lane = threadIdx.x;
   const int L = sm.lsize;
-  int n = 0;
   if (L == 1) {
-    int s0 = seg_of_desc(sm.top[0][0]);
-    sm.xseg[0] = s0;
-    sm.xcnt[0] = cnt_of_desc(sm.top[0][0]);
-    if (sm.minseg == s0) {
-      sm.mode = 2;
-      n = 1;
-    } else {
-      sm.mode = 1;
-      sm.xseg[1] = sm.minseg;
-      sm.xcnt[1] = 0;
-      n = 2;
-    }
-  } else {
-    sm.mode = 0;
-    const int lim = L < K ? L : K;
-    if (sched == 0 || sched == 2) {  // primary and targets follow one order
-      const int o = sched == 0 ? 0 : 1;
-      for (int q = 0; q < lim; ++q) {
-        unsigned long long k = sm.top[o][q];
-        sm.xseg[n] = o == 0 ? seg_of_desc(k) : seg_of_rev(k);
-        sm.xcnt[n] = o == 0 ? cnt_of_desc(k) : cnt_of_rev(k);
-        ++n;
-      }
-    } else {  // primary from one end, targets from the other
-      const int po = sched == 1 ? 0 : 1, to = 1 - po;
-      unsigned long long pk = sm.top[po][0];
-      const int ps = po == 0 ? seg_of_desc(pk) : seg_of_rev(pk);
-      sm.xseg[0] = ps;
-      sm.xcnt[0] = po == 0 ? cnt_of_desc(pk) : cnt_of_rev(pk);
-      n = 1;
-      for (int q = 0; q < K && n < lim; ++q) {
-        unsigned long long k = sm.top[to][q];
-        int s = to == 0 ? seg_of_desc(k) : seg_of_rev(k);
-        if (s == ps) continue;
-        sm.xseg[n] = s;
-        sm.xcnt[n] = to == 0 ? cnt_of_desc(k) : cnt_of_rev(k);
-        ++n;
+    if (lane == 0) {
+      int s0 = seg_of_desc(sm.top[0][0]);
+      sm.xseg[0] = s0;
+      sm.xcnt[0] = cnt_of_desc(sm.top[0][0]);
+      if (sm.minseg == s0) {
+        sm.mode = 2;
+        sm.K_ = 1;
+      } else {
+        sm.mode = 1;
+        sm.xseg[1] = sm.minseg;
+        sm.xcnt[1] = 0;
+        sm.K_ = 2;
       }
     }
+    return;
   }
-  sm.K_ = n;
+  const int lim = L < K ? L : K;
+  if (sched == 0 || sched == 2) {  // primary and targets follow one order: the first lim entries
+    const int o = sched == 0 ? 0 : 1;
+    if (lane < lim) {
+      const unsigned long long k = sm.top[o][lane];
+      sm.xseg[lane] = o == 0 ? seg_of_desc(k) : seg_of_rev(k);
+      sm.xcnt[lane] = o == 0 ? cnt_of_desc(k) : cnt_of_rev(k);
+    }
+    if (lane == 0) {
+      sm.mode = 0;
+      sm.K_ = lim;
+    }
+    return;
+  }
+  // primary from one end, targets from the other: the first lim - 1
+  // entries of the other order that are not the primary
+  const int po = sched == 1 ? 0 : 1, to = 1 - po;
+  const unsigned long long pk = sm.top[po][0];
+  const int ps = po == 0 ? seg_of_desc(pk) : seg_of_rev(pk);
+  unsigned long long k = 0;
+  int sg = 0;
+  if (lane < K) {
+    k = sm.top[to][lane];
+    sg = to == 0 ? seg_of_desc(k) : seg_of_rev(k);
+  }
+  const unsigned keep = __ballot_sync(FULL, lane < K && sg != ps);
+  const int at = 1 + __popc(keep & ((1u << lane) - 1u));
+  if (((keep >> lane) & 1u) && at < lim) {
+    sm.xseg[at] = sg;
+    sm.xcnt[at] = to == 0 ? cnt_of_desc(k) : cnt_of_rev(k);
+  }
+  if (lane == 0) {
+    sm.mode = 0;
+    sm.xseg[0] = ps;
+    sm.xcnt[0] = po == 0 ? cnt_of_desc(pk) : cnt_of_rev(pk);
+    const int n = 1 + __popc(keep);
+    sm.K_ = n < lim ? n : lim;
+  }
 }
 
 template <int M>
