@@ -123,24 +123,31 @@ static inline int sp_bits(long long v) {
 // ---------------------------------------------------------------------------
 // Compressor
 // ---------------------------------------------------------------------------
-__global__ void k_cmp_keys(const int* row, const int* col, int nnz, int M, int V, int nseg,
+// An entry's sort key: its V x M block (block row, segment) in the high
+// bits, then the row inside the block (bv = log2 V bits; V is a power of
+// two) and the column inside the segment (bm = ceil(log2 M) bits), so that
+// every field comes out with a shift and a mask.  Sorted, the keys order the
+// entries by block, row, column.
+__host__ __device__ inline int key_bits_m(int M) { return M <= 2 ? 1 : M <= 4 ? 2 : 3; }
+
+__global__ void k_cmp_keys(const int* row, const int* col, int nnz, int M, int V, int nseg, int bm, int bv,
                            unsigned long long* keys) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += gridDim.x * blockDim.x) {
     const int r = row[i], c = col[i];
-    const unsigned long long blk = (unsigned long long)(r / V) * nseg + (unsigned)(c / M);
-    keys[i] = (blk * V + (unsigned)(r % V)) * M + (unsigned)(c % M);
+    const unsigned long long blk = (unsigned long long)(r >> bv) * nseg + (unsigned)(c / M);
+    keys[i] = (((blk << bv) | (unsigned)(r & (V - 1))) << bm) | (unsigned)(c % M);
   }
 }
 
-__global__ void k_cmp_heads(const unsigned long long* keys, int nnz, int VM, int* flag) {
+__global__ void k_cmp_heads(const unsigned long long* keys, int nnz, int sh, int* flag) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += gridDim.x * blockDim.x)
-    flag[i] = (i == 0) || (keys[i] / VM != keys[i - 1] / VM);
+    flag[i] = (i == 0) || ((keys[i] >> sh) != (keys[i - 1] >> sh));
 }
 
-__global__ void k_cmp_group_start(const int* flag_scan, const unsigned long long* keys, int nnz, int VM,
+__global__ void k_cmp_group_start(const int* flag_scan, const unsigned long long* keys, int nnz, int sh,
                                   int* gstart) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += gridDim.x * blockDim.x)
-    if (i == 0 || keys[i] / VM != keys[i - 1] / VM) gstart[flag_scan[i]] = i;
+    if (i == 0 || (keys[i] >> sh) != (keys[i - 1] >> sh)) gstart[flag_scan[i]] = i;
 }
 
 // max |a| per block row of V rows, over the entries in sorted order: a
@@ -148,15 +155,22 @@ __global__ void k_cmp_group_start(const int* flag_scan, const unsigned long long
 // row) and issues one atomic per block row it saw, instead of one per entry
 // all landing on a few hundred words.
 constexpr int SCALE_RUN = 16;
-__global__ void k_cmp_scale(const unsigned long long* skeys, const int* spos, const float* val, int nnz, int VM,
+__global__ void k_cmp_scale(const unsigned long long* skeys, const int* spos, const float* val, int nnz, int sh,
                             int nseg, unsigned* bmax) {
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t * SCALE_RUN < nnz;
        t += (long long)gridDim.x * blockDim.x) {
     const int b = (int)(t * SCALE_RUN), e = min(b + SCALE_RUN, nnz);
     long long cur = -1;
+    unsigned long long lo = 1, hi = 0;  // the blocks of block row `cur`: [lo, hi)
     unsigned m = 0;
     for (int i = b; i < e; ++i) {
-      const long long br = (long long)((skeys[i] / (unsigned long long)VM) / (unsigned long long)nseg);
+      const unsigned long long blk = skeys[i] >> sh;
+      long long br = cur;
+      if (blk < lo || blk >= hi) {  // a division only where the block row changes
+        br = (long long)(blk / (unsigned long long)nseg);
+        lo = (unsigned long long)br * (unsigned long long)nseg;
+        hi = lo + (unsigned long long)nseg;
+      }
       if (br != cur) {
         if (m) atomicMax(&bmax[cur], m);
         cur = br;
@@ -214,18 +228,19 @@ __device__ __forceinline__ unsigned low2(unsigned m) {  // the lowest two set bi
 // nonzeros gets no slice: its entries are flagged for the residual (by
 // original position), counted per row and per tile.
 __global__ void k_cmp_count(const unsigned long long* skeys, const int* spos, const int* gstart, const int* d_ngroups,
-                            int nnz, int M, int V, int nseg, int dense_min, int* gsl, int* tile_raw, int* valid_blocks,
-                            int* resflag, int* rowlen, int* tile_res) {
+                            int nnz, int M, int V, int nseg, int bm, int dense_min, int* gsl, int* tile_raw,
+                            int* valid_blocks, int* resflag, int* rowlen, int* tile_res) {
   const int ngroups = *d_ngroups;
+  const int sh = bm + __ffs(V) - 1;
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += gridDim.x * blockDim.x) {
     const int b0 = gstart[g], b1 = g + 1 < ngroups ? gstart[g + 1] : nnz;
-    const long long blk = (long long)(skeys[b0] / ((unsigned long long)V * M));
+    const long long blk = (long long)(skeys[b0] >> sh);
     const int brow = (int)(blk / nseg);
     unsigned char mask[128];
     int nr = 0, lastr = -1;
     for (int i = b0; i < b1; ++i) {
       const unsigned long long k = skeys[i];
-      const int rr = (int)((k / M) % V), o = (int)(k % M);
+      const int rr = (int)(k >> bm) & (V - 1), o = (int)(k & ((1u << bm) - 1u));
       if (rr != lastr) {
         mask[nr++] = 0;
         lastr = rr;
@@ -239,11 +254,15 @@ __global__ void k_cmp_count(const unsigned long long* skeys, const int* spos, co
       if (__popc(mask[r]) > 2) valid = 0;
     }
     if (__popc(orb) > 4) valid = 0;
-    if (valid) atomicAdd(valid_blocks, 1);
+    {  // one atomic per group of converged lanes: every block adds to this one word
+      const unsigned am = __activemask();
+      const unsigned vb = __ballot_sync(am, valid != 0);
+      if ((int)(threadIdx.x & 31) == __ffs(am) - 1 && vb) atomicAdd(valid_blocks, __popc(vb));
+    }
     if (b1 - b0 < dense_min) {
       for (int i = b0; i < b1; ++i) {
         resflag[spos[i]] = 1;
-        atomicAdd(&rowlen[brow * V + (int)((skeys[i] / M) % V)], 1);
+        atomicAdd(&rowlen[brow * V + ((int)(skeys[i] >> bm) & (V - 1))], 1);
       }
       atomicAdd(&tile_res[(brow * V) / SP_TM], b1 - b0);
       gsl[g] = 0;
@@ -341,13 +360,14 @@ __device__ __forceinline__ __half to_t<__half>(float x) {
 // Write every block's slices: B-row indices and A values in MMA layout.
 template <class T>
 __global__ void k_cmp_fill(const unsigned long long* skeys, const int* spos, const float* val, const int* gstart,
-                           int ngroups, int nnz, int M, int V, int nseg, int dense_min, const int* gofs,
+                           int ngroups, int nnz, int M, int V, int nseg, int bm, int dense_min, const int* gofs,
                            const int* tile_base, const int* tile_rawbase, const unsigned* bmax, int* cols,
                            unsigned char* a) {
+  const int sh = bm + __ffs(V) - 1;
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += gridDim.x * blockDim.x) {
     const int b0 = gstart[g], b1 = g + 1 < ngroups ? gstart[g + 1] : nnz;
     if (b1 - b0 < dense_min) continue;  // a residual block
-    const long long blk = (long long)(skeys[b0] / ((unsigned long long)V * M));
+    const long long blk = (long long)(skeys[b0] >> sh);
     const int brow = (int)(blk / nseg), seg = (int)(blk % nseg);
     const int t = (brow * V) / SP_TM;
     const float scale = bmax[brow] ? __uint_as_float(bmax[brow]) : 1.0f;
@@ -357,7 +377,7 @@ __global__ void k_cmp_fill(const unsigned long long* skeys, const int* spos, con
     int nr = 0, lastr = -1;
     for (int i = b0; i < b1; ++i) {
       const unsigned long long k = skeys[i];
-      const int rr = (int)((k / M) % V), o = (int)(k % M);
+      const int rr = (int)(k >> bm) & (V - 1), o = (int)(k & ((1u << bm) - 1u));
       if (rr != lastr) {
         rowin[nr] = rr;
         first[nr] = i;
@@ -820,6 +840,7 @@ static vnm_status compress_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, con
   const int nbrow = (R + V - 1) / V;
   const int ntiles = (R + SP_TM - 1) / SP_TM;
   const int dense_min = spmm_dense_min(V);
+  const int bm = key_bits_m(M), bv = __builtin_ctz((unsigned)V), sh = bm + bv;  // V is a power of two (divides 128)
   int* h = ctx->h_pinned;
   const size_t n1 = nnz > 0 ? (size_t)nnz : 1;
   unsigned long long* keys = arena_take<unsigned long long>(ctx, n1);
@@ -866,15 +887,15 @@ static vnm_status compress_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, con
     // counting grid covers every entry, and the scan of the slices per group
     // runs over nnz words, zero past the last group
     VNM_CUDA_TRY(cudaMemsetAsync(gsl, 0, sizeof(int) * n1, st));
-    VNM_LAUNCH(ctx, k_cmp_keys, sp_grid(ctx, nnz), 256, 0, d_row, d_col, nnz, M, V, nseg, keys);
-    const long long maxkey = ((long long)nbrow * nseg) * V * M;
+    VNM_LAUNCH(ctx, k_cmp_keys, sp_grid(ctx, nnz), 256, 0, d_row, d_col, nnz, M, V, nseg, bm, bv, keys);
+    const long long maxkey = ((long long)nbrow * nseg) << sh;
     VNM_TRY(radix_sort_u64(ctx, keys, nullptr, nnz, sp_bits(maxkey), &skeys, &spos));
-    VNM_LAUNCH(ctx, k_cmp_heads, sp_grid(ctx, nnz), 256, 0, skeys, nnz, V * M, flag);
+    VNM_LAUNCH(ctx, k_cmp_heads, sp_grid(ctx, nnz), 256, 0, skeys, nnz, sh, flag);
     VNM_TRY(exclusive_scan(ctx, flag, flag, nnz, counters));
-    VNM_LAUNCH(ctx, k_cmp_group_start, sp_grid(ctx, nnz), 256, 0, flag, skeys, nnz, V * M, gstart);
+    VNM_LAUNCH(ctx, k_cmp_group_start, sp_grid(ctx, nnz), 256, 0, flag, skeys, nnz, sh, gstart);
     VNM_LAUNCH(ctx, k_cmp_scale, sp_grid(ctx, (nnz + SCALE_RUN - 1) / SCALE_RUN), 256, 0, skeys, spos, d_val, nnz,
-               V * M, nseg, bmax);
-    VNM_LAUNCH(ctx, k_cmp_count, sp_grid(ctx, nnz, 128), 128, 0, skeys, spos, gstart, counters, nnz, M, V, nseg,
+               sh, nseg, bmax);
+    VNM_LAUNCH(ctx, k_cmp_count, sp_grid(ctx, nnz, 128), 128, 0, skeys, spos, gstart, counters, nnz, M, V, nseg, bm,
                dense_min, gsl, tile_raw, counters + 1, resflag, rowlen, tile_res);
     VNM_TRY(exclusive_scan(ctx, gsl, gofs, nnz, counters + 2));
   }
@@ -969,7 +990,7 @@ static vnm_status compress_t(vnm_ctx* ctx, int R, int nnz, const int* d_row, con
   VNM_CUDA_TRY(cudaMemsetAsync(out->a, 0, b_a, st));
   if (ngroups > 0 && out->nsteps > 0)
     VNM_LAUNCH(ctx, k_cmp_fill<T>, sp_grid(ctx, ngroups, 128), 128, 0, skeys, spos, d_val, gstart, ngroups, nnz, M,
-               V, nseg, dense_min, gofs, tile_base, tile_rawbase, bmax, out->cols, out->a);
+               V, nseg, bm, dense_min, gofs, tile_base, tile_rawbase, bmax, out->cols, out->a);
   VNM_LAUNCH(ctx, k_cmp_rscale, sp_grid(ctx, (long long)ntiles * SP_TM), 256, 0, bmax, ntiles, R, V, out->rscale,
              tile_base, out->tile_step);
   return VNM_OK;
