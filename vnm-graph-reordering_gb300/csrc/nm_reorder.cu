@@ -1689,7 +1689,7 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     if (lead) {
       rank_phase<M>(sm);
       VNM_PHASE(4);
-      const unsigned long long t_in = global_ns();
+      const unsigned long long t_in = tid == NM_THREADS - 32 ? global_ns() : 0ull;
       if (tid >= NM_THREADS - 32) walk_phase<M>(sm, J.sched, J.walk_wait_limit);  // the last warp walks ...
       else if (!J.hold_heaps) heap_sift<M>(sm);                                   // ... while the heaps pop
       if (tid == NM_THREADS - 32) s_tin[0] += global_ns() - t_in;
