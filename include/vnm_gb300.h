@@ -81,7 +81,7 @@ float vnm_last_main_kernel_ms(const vnm_ctx* ctx);
  * records of the rows it owns; summed over blocks and jobs), out[8..14]
  * time spent per round phase (select, choose, gather, process, heap
  * entries, swap heaps and walk overlapped, apply) in units of 1024 ns,
- * summed over jobs,
+ * summed over jobs (with vnm_nm_set_phase_timing on, else 0),
  * out[15] block-rounds whose row records were in global memory (the
  * block's entries would have filled more than 3/4 of its table), out[16]
  * the time from the round kernel's start to its end in units of 1024 ns
@@ -93,7 +93,8 @@ float vnm_last_main_kernel_ms(const vnm_ctx* ctx);
  * hold at once by the occupancy query (0 for single-block launches),
  * out[20], out[21] the leaders' own work in the process and apply phases
  * (before the barriers that close them), units of 1024 ns summed over
- * jobs, out[22..27] times inside phases in the same units: the walk warp,
+ * jobs, out[22..27] times inside phases in the same units (out[20..27]
+ * other than out[23] with vnm_nm_set_phase_timing on, else 0): the walk warp,
  * its waits for swap-heap pops, warp 0 of the leader over its rows in
  * the process phase and in the apply phase, and that warp's per-segment
  * masks and pair corrections in the process phase.  n <= 28 values. */
@@ -149,6 +150,13 @@ vnm_status vnm_nm_reorder_batch(vnm_ctx* ctx, int nmat, const int* nrows, const 
  * position pairs in commit order and round_end[r] the number of pairs
  * committed by the end of round r.  Tracing is off unless enabled. */
 vnm_status vnm_nm_set_trace(vnm_ctx* ctx, int enable);
+
+/* Per-phase timers of the round kernel (vnm_last_stats out[8..14] and
+ * out[20..27] other than out[23]).  Off by default: reading the global
+ * timer at every phase boundary on the leader's critical path costs about
+ * 2.5 % of the kernel's time, so those values read 0 unless this is
+ * enabled.  No counterpart in the reference. */
+vnm_status vnm_nm_set_phase_timing(vnm_ctx* ctx, int enable);
 vnm_status vnm_nm_get_trace(vnm_ctx* ctx, int* pairs, int cap_pairs, int* npairs, int* round_end, int cap_rounds,
                             int* nrounds);
 

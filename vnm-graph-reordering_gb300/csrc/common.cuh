@@ -80,6 +80,7 @@ struct vnm_ctx {
   size_t h_pinned_cap = 0;
   // swap trace of the last NM call (host copies)
   bool trace = false;
+  bool phase_timing = false;  // the round kernel's per-phase timers (vnm_nm_set_phase_timing)
   std::vector<int> trace_pairs, trace_round_end;
 };
 

@@ -128,6 +128,7 @@ struct NMJob {
   int walk_wait_limit;  // polls before a wait of the walk gives up (WALK_WAIT_LIMIT)
   int hold_heaps;       // test only: the swap heaps publish no pop, so a walk that waits runs out
   const int* err;       // the input check's flag (k_validate): nonzero, the job does nothing; null, no check
+  int timed;            // measure the round phases (the leader's thread 0 reads the global timer)
 };
 
 // ---------------------------------------------------------------------------
@@ -834,7 +835,8 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
   // this warp's row masks: VL[x][k] at vw[2x * M + k], VE[x][k] at vw[(2x + 1) * M + k]
   extern __shared__ uint4 smem_heap[];
   unsigned* vw_warp = reinterpret_cast<unsigned*>(smem_heap) + (threadIdx.x >> 5) * (2 * K * M);
-  const unsigned long long t_in = (threadIdx.x == 0 && sl.rank == 0) ? global_ns() : 0ull;
+  const bool tmain = threadIdx.x == 0 && sl.rank == 0 && J.timed;  // the leader's thread 0 times (when asked)
+  const unsigned long long t_in = tmain ? global_ns() : 0ull;
   // When every 32-row chunk's masks fit the scratch, each chunk leaves them
   // there and the sums are made afterwards over all chunks (gathered),
   // instead of a shared atomic per chunk, pair and entry: those atomics, and
@@ -848,7 +850,7 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
     (void)r;
     // chunk c's masks at c * 2KM when they are summed afterwards, else this warp's
     unsigned* vw = gathered ? reinterpret_cast<unsigned*>(smem_heap) + chunk * (2 * K * M) : vw_warp;
-    const unsigned long long t_a = (threadIdx.x == 0 && sl.rank == 0) ? global_ns() : 0ull;
+    const unsigned long long t_a = tmain ? global_ns() : 0ull;
     unsigned b[K];
     int p[K];
 #pragma unroll
@@ -909,7 +911,7 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
     // VE[a][i] lies inside NZ[a] (eL is empty when L is) and VL[c][j] inside
     // NZ[c], so CL(i, j) = popc(VE[a][i] & VL[c][j]) and likewise
     // CR(i, j) = popc(VL[a][i] & VE[c][j]).
-    const bool timed = threadIdx.x == 0 && sl.rank == 0;
+    const bool timed = tmain;
     const unsigned long long t_b = timed ? global_ns() : 0ull;
     if (timed) s_tin[4] += t_b - t_a;
     if (gathered) {  // the masks stay in this warp's scratch for the sums below
@@ -956,7 +958,7 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
   __syncthreads();
   if (gathered) {
     // sums over the chunks' masks (chunk c's at c * 2KM)
-    const unsigned long long t_g = (threadIdx.x == 0 && sl.rank == 0) ? global_ns() : 0ull;
+    const unsigned long long t_g = tmain ? global_ns() : 0ull;
     const unsigned* vb = reinterpret_cast<const unsigned*>(smem_heap);
     constexpr int NP = RoundSmem<M>::NPAIR;
     if constexpr (M % 4 == 0 && M >= 8) {
@@ -1042,10 +1044,10 @@ __device__ void process_phase(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl 
         }
       }
     }
-    if (threadIdx.x == 0 && sl.rank == 0) s_tin[5] += global_ns() - t_g;
+    if (tmain) s_tin[5] += global_ns() - t_g;
     __syncthreads();
   }
-  if (threadIdx.x == 0 && sl.rank == 0) s_tin[2] += global_ns() - t_in;
+  if (tmain) s_tin[2] += global_ns() - t_in;
 }
 
 // Pop order of every ordered pair's swap heap (fact 4).  The sift steps are
@@ -1477,7 +1479,8 @@ __device__ void apply_recount(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl)
     bitmove[xi][h][v] = make_uint4(o[0], o[1], o[2], 0u);
   }
   __syncthreads();
-  const unsigned long long t_in = (threadIdx.x == 0 && sl.rank == 0) ? global_ns() : 0ull;
+  const bool tmain = threadIdx.x == 0 && sl.rank == 0 && J.timed;
+  const unsigned long long t_in = tmain ? global_ns() : 0ull;
   for_rows_warp<M, 2>(sm, J, [&](int r, const uint4& w, bool valid, int chunk) {
     (void)chunk;
     // the row's groups after the swaps, packed like the record
@@ -1511,7 +1514,7 @@ __device__ void apply_recount(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl)
       else J.rec[r] = make_uint4(0u, 0u, 0u, 0u);
     }
   });
-  if (threadIdx.x == 0 && sl.rank == 0) s_tin[3] += global_ns() - t_in;
+  if (tmain) s_tin[3] += global_ns() - t_in;
   __syncthreads();
   if (threadIdx.x == 0) sm.tcount = 0;  // the table is empty again (before the next round's inserts)
 }
@@ -1616,14 +1619,17 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
   __shared__ unsigned long long tph[7];
   __shared__ unsigned long long tpo[2];  // the leader's own work in the process and apply phases
   __shared__ unsigned long long t0;
+  // (global timer reads on the leader's critical path cost ~2.5 % of the
+  // kernel's time, so they are made only when the caller asks: J.timed)
+  const bool timed = J.timed != 0;
   if (tid == 0) {
     for (int q = 0; q < 7; ++q) tph[q] = 0;
     tpo[0] = tpo[1] = 0;
     for (int q = 0; q < 6; ++q) s_tin[q] = 0;
-    t0 = global_ns();
+    t0 = timed ? global_ns() : 0ull;
   }
 #define VNM_PHASE(i)                                     \
-  if (tid == 0) {                                        \
+  if (tid == 0 && timed) {                               \
     const unsigned long long t1 = global_ns();           \
     tph[i] += t1 - t0;                                   \
     t0 = t1;                                             \
@@ -1667,7 +1673,7 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     }
     VNM_PHASE(2);
     process_phase<M>(sm, J, N, sl);
-    if (tid == 0) tpo[0] += global_ns() - t0;  // the leader's own part of the process phase
+    if (tid == 0 && timed) tpo[0] += global_ns() - t0;  // the leader's own part of the process phase
     if (cs > 1) {
       // (the leader pulling the helpers' sums over DSMEM instead was slower:
       // 8.92 against 8.55 ms at R-MAT 16384 2:4, 200.5 against 197.2 ms at
@@ -1689,10 +1695,10 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     if (lead) {
       rank_phase<M>(sm);
       VNM_PHASE(4);
-      const unsigned long long t_in = tid == NM_THREADS - 32 ? global_ns() : 0ull;
+      const unsigned long long t_in = (tid == NM_THREADS - 32 && timed) ? global_ns() : 0ull;
       if (tid >= NM_THREADS - 32) walk_phase<M>(sm, J.sched, J.walk_wait_limit);  // the last warp walks ...
       else if (!J.hold_heaps) heap_sift<M>(sm);                                   // ... while the heaps pop
-      if (tid == NM_THREADS - 32) s_tin[0] += global_ns() - t_in;
+      if (tid == NM_THREADS - 32 && timed) s_tin[0] += global_ns() - t_in;
       __syncthreads();
       VNM_PHASE(5);
       if (tid == 0 && J.trace_pairs) {
@@ -1715,7 +1721,7 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     }
     if (cs > 1) cl.sync();
     apply_recount<M>(sm, J, N, sl);
-    if (tid == 0) tpo[1] += global_ns() - t0;  // the leader's own part of the apply phase
+    if (tid == 0 && timed) tpo[1] += global_ns() - t0;  // the leader's own part of the apply phase
     if (cs > 1) {
       if (!lead) cluster_push(cl, &sm.newinv[0], 2 * K);
       cl.sync();
@@ -1945,6 +1951,7 @@ static vnm_status make_job(vnm_ctx* ctx, const Pattern& P, int sched, int maxite
   J.walk_wait_limit = WALK_WAIT_LIMIT;
   J.hold_heaps = 0;
   J.err = nullptr;
+  J.timed = ctx->phase_timing ? 1 : 0;
   if (const char* e = getenv("VNM_NM_TEST_WAIT_LIMIT")) {
     const int v = atoi(e);
     if (v > 0 && v < WALK_WAIT_LIMIT) J.walk_wait_limit = v;
@@ -2409,6 +2416,7 @@ static vnm_status run_batch(vnm_ctx* ctx, int nmat, const int* nrows, const int6
     J.walk_wait_limit = WALK_WAIT_LIMIT;
     J.hold_heaps = 0;
     J.err = nullptr;
+    J.timed = ctx->phase_timing ? 1 : 0;
     if (J.nseg > max_nseg) max_nseg = J.nseg;
   }
   VNM_CUDA_TRY(cudaMemcpyAsync(d_jobs, hj.data(), sizeof(NMJob) * nmat, cudaMemcpyHostToDevice, ctx->stream));
@@ -2480,6 +2488,12 @@ vnm_status vnm_nm_search(vnm_ctx* ctx, int nrows, int nnz, const int* row, const
 vnm_status vnm_nm_set_trace(vnm_ctx* ctx, int enable) {
   if (!ctx) return VNM_ERR_ARG;
   ctx->trace = enable != 0;
+  return VNM_OK;
+}
+
+vnm_status vnm_nm_set_phase_timing(vnm_ctx* ctx, int enable) {
+  if (!ctx) return VNM_ERR_ARG;
+  ctx->phase_timing = enable != 0;
   return VNM_OK;
 }
 

@@ -66,6 +66,7 @@ def lib():
     L.vnm_nm_reorder_batch.argtypes = [_vp, ctypes.c_int, _i32p, _i64p, _i32p, _i32p, _f32p, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p, _i32p]
     L.vnm_nm_set_trace.argtypes = [_vp, ctypes.c_int]
+    L.vnm_nm_set_phase_timing.argtypes = [_vp, ctypes.c_int]
     L.vnm_nm_get_trace.argtypes = [_vp, _i32p, ctypes.c_int, _i32p, _i32p, ctypes.c_int, _i32p]
     L.vnm_permute_coo.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, ctypes.c_int, _vp]
     L.vnm_nm_segment_counts.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
@@ -204,6 +205,11 @@ class Context:
 
     def set_trace(self, on):
         _check(lib().vnm_nm_set_trace(self.h, 1 if on else 0), "vnm_nm_set_trace")
+
+    def set_phase_timing(self, on):
+        """Per-phase timers of the round kernel (last_stats' phase_us,
+        leader_own_us, inside_us); off by default, as they cost time."""
+        _check(lib().vnm_nm_set_phase_timing(self.h, 1 if on else 0), "vnm_nm_set_phase_timing")
 
     def get_trace(self):
         """Swaps of the last traced job: list of per-round (k, 2) arrays."""
