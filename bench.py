@@ -602,7 +602,7 @@ def run_ours(args, rank, world, local):
                                     "group; %d groups" % groups,
                      # dram__bytes_read.sum + dram__bytes_write.sum of one launch, from the ncu
                      # capture summarised in profiles/k_nm_rounds_c2_rmat16384_m4.md
-                     "traffic": 1.078e6, "traffic_unit": "bytes per launch",
+                     "traffic": 1.079e6, "traffic_unit": "bytes per launch",
                      "traffic_source": "profiles/k_nm_rounds_c2_rmat16384_m4.md",
                      "alg_bytes_per_launch": alg_bytes / args.steps,
                      "kernel_ms_per_launch": tot["rounds_kernel_ms"] / args.steps,
