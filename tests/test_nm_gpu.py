@@ -49,6 +49,25 @@ def test_reorder_matches_oracle_every_case(ctx, goldens):
     assert not bad, bad[:5]
 
 
+def test_phase_timers_change_nothing_but_the_stats(ctx, goldens):
+    """The round kernel's phase timers are off by default (their stats read
+    0); on, they fill the stats, and the results are the same either way."""
+    nr, r, c, v = nm_input(goldens, "rmat_2048__n2_m4")
+    best0, res0, pos0 = ctx.nm_search(nr, r, c, v, 2, 4)
+    st = ctx.last_stats()
+    assert sum(st["phase_us"].values()) == 0 and st["inside_us"]["walk"] == 0
+    assert st["rounds"] > 0 and st["kernel_us"] > 0
+    ctx.set_phase_timing(True)
+    try:
+        best1, res1, pos1 = ctx.nm_search(nr, r, c, v, 2, 4)
+        st = ctx.last_stats()
+    finally:
+        ctx.set_phase_timing(False)
+    assert all(st["phase_us"][k] > 0 for k in ("gather", "process", "heaps_and_walk", "apply"))
+    assert st["inside_us"]["walk"] > 0
+    assert best0 == best1 and np.array_equal(res0, res1) and np.array_equal(pos0, pos1)
+
+
 def test_reorder_trace_matches_oracle(ctx, goldens):
     ctx.set_trace(True)
     try:
