@@ -215,6 +215,21 @@ def test_host_outputs_given_by_the_caller(ctx):
     A.close()
 
 
+@pytest.mark.parametrize("M", [2, 3, 5, 6, 7])
+@pytest.mark.parametrize("split", [TENSOR_ONLY, RESIDUAL_ONLY])
+def test_spmm_every_group_size(ctx, M, split):
+    """Group sizes other than 4 and 8 (the compressor's sort keys hold the
+    column inside a segment in ceil(log2 M) bits), on both paths."""
+    rng = np.random.default_rng(M)
+    nr = 13440  # a multiple of 128 and of every M
+    idx = np.unique(rng.integers(0, nr * nr, 120000))
+    r, c = (idx // nr).astype(np.int32), (idx % nr).astype(np.int32)
+    v = rng.standard_normal(len(r)).astype(np.float32)
+    with _dense_min(split):
+        err, info = _run(ctx, nr, r, c, v, M, 32, 64, "bf16")
+    assert err < TOL, (M, err, info)
+
+
 @pytest.mark.parametrize("V", [32, 64, 128])
 def test_full_vnm_blocks_go_to_the_tensor_cores(ctx, V):
     """A matrix in full V:2:8 form (every block 2V nonzeros): by default
