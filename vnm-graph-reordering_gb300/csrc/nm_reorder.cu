@@ -1519,24 +1519,45 @@ __device__ void apply_recount(RoundSmem<M>& sm, const NMJob& J, int N, Slice sl)
   if (threadIdx.x == 0) sm.tcount = 0;  // the table is empty again (before the next round's inserts)
 }
 
-// The new counts of the round's segments (leader block).
+// The new counts of the round's segments (leader block), and the leader's
+// partial sums cleared for the next round: the walk read the scores last,
+// and each thread clears the recount words it read (what clear_round_smem
+// does, without a barrier of its own).
 template <int M>
 __device__ void apply_finish(RoundSmem<M>& sm, const NMJob& J, int* cnt) {
+  constexpr int K = M + 1;
   const int tid = threadIdx.x;
-  if (tid < sm.K_) {
-    cnt[sm.xseg[tid]] = sm.newinv[tid];
-    J.zc[sm.xseg[tid]] = J.R - sm.newpres[tid];
+  if (tid < K) {
+    if (tid < sm.K_) {
+      cnt[sm.xseg[tid]] = sm.newinv[tid];
+      J.zc[sm.xseg[tid]] = J.R - sm.newpres[tid];
+    }
+    sm.newinv[tid] = 0;
+    sm.newpres[tid] = 0;
+  }
+  for (int i = tid; i < K * M; i += NM_THREADS) (&sm.S[0][0])[i] = 0;
+  for (int i = tid; i < RoundSmem<M>::NPAIR * RoundSmem<M>::MM; i += NM_THREADS) {
+    (&sm.CL[0][0])[i] = 0;
+    (&sm.CR[0][0])[i] = 0;
+  }
+  if (tid == 0) {
+    sm.ntouched = 0;
+    sm.nswaps = 0;
   }
   __syncthreads();
 }
 
 // Helper block: add its nonzero partial sums of n ints at `mine` into the
-// leader's copy (remote atomics, complete at the next cluster barrier).
+// leader's copy (remote atomics, complete at the next cluster barrier) and
+// clear them for the next round (nothing reads them again this round).
 __device__ void cluster_push(cg::cluster_group& cl, int* mine, int n) {
   int* lead_arr = cl.map_shared_rank(mine, 0);
   for (int i = threadIdx.x; i < n; i += NM_THREADS) {
     const int v = mine[i];
-    if (v) atomicAdd(lead_arr + i, v);
+    if (v) {
+      atomicAdd(lead_arr + i, v);
+      mine[i] = 0;
+    }
   }
 }
 
@@ -1660,10 +1681,8 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     }
     if (cs > 1) cl.sync();
     if (!sm.go) break;  // the same decision in every block of the job
-    if (!lead) {        // the block pushed last round's partial sums before the last barrier
-      clear_round_smem<M>(sm);
-      __syncthreads();
-    }
+    // (a helper cleared its partial sums as it pushed them last round, the
+    // leader in apply_finish)
     // the block's own rows: no barrier between its gather and its process phase
     gather_phase<M>(sm, J, sl);
     if (tid == 0) {
@@ -1723,13 +1742,14 @@ __global__ void __launch_bounds__(NM_THREADS, 1) k_nm_rounds(const NMJob* __rest
     apply_recount<M>(sm, J, N, sl);
     if (tid == 0 && timed) tpo[1] += global_ns() - t0;  // the leader's own part of the apply phase
     if (cs > 1) {
-      if (!lead) cluster_push(cl, &sm.newinv[0], 2 * K);
+      if (!lead) {
+        cluster_push(cl, &sm.newinv[0], 2 * K);
+        if (tid == 0) sm.ntouched = 0;  // (read last by the recount, before its closing __syncthreads)
+      }
       cl.sync();
     }
     if (lead) {
-      apply_finish<M>(sm, J, cnt);
-      clear_round_smem<M>(sm);
-      __syncthreads();
+      apply_finish<M>(sm, J, cnt);  // also clears the leader's sums for the next round
       VNM_PHASE(6);
       if (cs > 1) select_merge<M>(sm, cl, cs, cnt);
       else select_phase<M>(sm, J, cnt);
