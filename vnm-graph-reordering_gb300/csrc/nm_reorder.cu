@@ -1232,15 +1232,17 @@ __device__ void heap_sift(RoundSmem<M>& sm) {
   }
 }
 
-// The greedy walk of run_onepair* over this round's segments, on warp 0.
+// The greedy walk of run_onepair* over this round's segments, on one warp.
 // Lane q holds round segment q: its current count and visited bits.  The
 // list is a set (the primary is the list's top and the targets follow in
 // traversal order, both strict total orders on (count, segment)), kept as
 // a lane mask; each step is a few warp votes and shuffles:
-//   - primary: the largest list key among the list's lanes;
-//   - targets: each lane's position in traversal order by comparing keys;
-//   - the first unvisited swap of a pair's pop order: a ballot over all
-//     pops at once;
+//   - primary: the largest list key among the list's lanes; its visited
+//     bits then live in a register of every lane for the pass;
+//   - targets: each lane's position in traversal order by comparing keys,
+//     inverted once per pass into a list of the targets' lanes;
+//   - the first unvisited swap of a pair's pop order: the unique largest
+//     qualifying key read off the entries, else a ballot over the pops;
 //   - each committed swap's bit moves go straight into dest.
 __device__ __forceinline__ unsigned order_key_hi(int c, bool rev) {  // count, order-preserving
   const unsigned u = (unsigned)c ^ 0x80000000u;
